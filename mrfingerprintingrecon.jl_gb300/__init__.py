@@ -1,0 +1,16 @@
+"""GB300 (sm_103a) subspace normal operator for MRISubspaceRecon.jl workloads.
+
+Python mirror of the reference's public API for the hot path, backed by the
+C-ABI library ``libmrsr.so`` (hand-written CUDA kernels, ``csrc/``).  There is
+no CPU implementation: every call runs on the current CUDA device.
+"""
+from . import _lib
+from .normalop import NFFTNormalOp, FFTNormalOp, NormalOperator
+from .arrays import jl_empty, jl_zeros, to_jl, to_host
+
+__all__ = ["NFFTNormalOp", "FFTNormalOp", "NormalOperator", "jl_empty", "jl_zeros", "to_jl", "to_host"]
+
+
+def library():
+    """The loaded ``libmrsr.so`` (raises if it has not been built)."""
+    return _lib.load()

@@ -1,0 +1,63 @@
+// Internal state of a subspace Toeplitz normal operator handle.
+#pragma once
+#include "fft.cuh"
+
+namespace mrsr {
+
+// How the per-voxel K x K kernel is stored.
+enum LamMode : int {
+  LAM_PACKED_REAL = 0,  // P = K(K+1)/2 reals, symmetric (real basis, ext:140-191)
+  LAM_PACKED_CPLX = 1,  // P complex, Hermitian upper triangle (ext:89-137)
+  LAM_FULL_CPLX = 2     // K*K complex, column-major (FFTNormalOp, src/FFTNormalOp.jl:331)
+};
+
+struct OpGeom {
+  int ndims = 2;
+  int64_t n[3] = {1, 1, 1};  // image shape
+  int64_t g[3] = {1, 1, 1};  // FFT grid (2n for the NFFT operator, n for the FFT operator)
+  int K = 1;
+  int ncoils = 1;
+  int64_t nimg() const { return n[0] * n[1] * n[2]; }
+  int64_t ngrid() const { return g[0] * g[1] * g[2]; }
+  // Λ-pass (last axis) tiling
+  int64_t inner() const { return ndims == 2 ? g[0] : g[0] * g[1]; }
+  int64_t glast() const { return g[ndims - 1]; }
+  int64_t nlast() const { return n[ndims - 1]; }
+};
+
+}  // namespace mrsr
+
+struct mrsr_normalop {
+  int kind = MRSR_KIND_NFFT;
+  int precision = MRSR_PREC_FP32;
+  mrsr::OpGeom geo;
+  int lam_mode = mrsr::LAM_PACKED_CPLX;
+  int P = 1;      // kernel entries per voxel in the internal layout
+  int64_t nk = 0;
+  int TC = 4;     // Λ-pass tile width (columns)
+  int Cg = 1;     // coils per group
+  int launches = 0;
+  mrsr::DevBuf kmask;      // int64 nk, 1-based column-major grid indices
+  mrsr::DevBuf lam;        // [tile][f_last][P][TC] of float / float2 / half / half2
+  mrsr::DevBuf lam_scale;  // fp16: one float per tile
+  mrsr::DevBuf cmaps;      // (img..., ncoils) complex; empty = unit coil
+  mrsr::DevBuf stack1, stack2;  // intermediates of one coil group
+  mrsr::DevBuf scale1, scale2;  // fp16 per-line scales
+  mrsr::DevBuf errflag;         // device int
+  mrsr::FftPlanHost plan[3];
+};
+
+namespace mrsr {
+// Build helpers shared by the constructors (normalop.cu).
+int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_shape, int K,
+                     int ncoils, int precision);
+int op_set_cmaps(mrsr_normalop* op, const float* cmaps, cudaStream_t st);
+int op_finalize(mrsr_normalop* op, cudaStream_t st);
+// Λ from the reference's packed (P, nk) layout at 1-based kmask cells.
+int op_set_lambda_packed(mrsr_normalop* op, const void* lam_packed, int is_complex, const int64_t* kmask,
+                         int64_t nk, cudaStream_t st);
+// Λ of an FFT operator from the reference's full (K, K, grid...) complex array; kmask = Λ[1,1,:] .!= 0.
+int op_set_lambda_full(mrsr_normalop* op, const float2* lam_full, cudaStream_t st);
+// Stream compaction: 1-based indices of nonzero flags, sorted.
+int compact_nonzero(const uint8_t* flags, int64_t n, DevBuf& out, int64_t* count, cudaStream_t st);
+}  // namespace mrsr
