@@ -1,0 +1,430 @@
+// Register four-step versions of the apply passes (see fft4.cuh).
+//
+// Same data flow as the generic kernels in normalop.cu; each line transform
+// is two register DFT steps with one shared-memory exchange, and the Λ pass
+// keeps its spectrum in the exchange buffer for the K x K product.
+#include "fft4.cuh"
+#include "passes.cuh"
+#include "tma.cuh"
+#include "tmap.cuh"
+
+#include <algorithm>
+#include <cstdlib>
+
+namespace mrsr {
+
+// ---------------------------------------------------------- kernels ---
+
+template <class SP>
+__global__ void __launch_bounds__(512) k4_rows_fwd(RowsFwdArgs a, Slots sl) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* sm = smem + L;
+  load_twiddles(tw, a.pl);
+  const int cl = blockIdx.y;
+  const int c = a.c0 + cl;
+  const int64_t row0 = (int64_t)blockIdx.x * a.rpc;
+  const int nr = (int)min((int64_t)a.rpc, a.nrows - row0);
+  const int NO = a.rpc * a.K;
+  const int nload = (a.n1 * 2 == L) ? R1 / 2 : R1;
+  __syncthreads();
+  step_a<SP, -1>(sm, sl, NO, tw, nload, [&](int lo, int, int n) -> float2 {
+    const int rl = lo / a.K, k = lo - rl * a.K;
+    if (rl >= nr || n >= a.n1) return make_float2(0.f, 0.f);
+    const int64_t r = row0 + rl;
+    float2 v = a.x[n + (int64_t)a.n1 * (r + a.nrows * k)];
+    if (a.cmaps) v = cmul(a.cmaps[n + (int64_t)a.n1 * (r + a.nrows * c)], v);
+    return v;
+  });
+  __syncthreads();
+  step_b<SP, -1>(sm, sl, NO, R2, [&](int lo, int, int f1, int f2, float2 v) {
+    const int rl = lo / a.K, k = lo - rl * a.K;
+    if (rl < nr) a.out[(((int64_t)cl * a.K + k) * a.nrows + row0 + rl) * L + f1 + R1 * f2] = v;
+  });
+}
+
+template <class SP>
+__global__ void __launch_bounds__(512) k4_rows_inv(RowsInvArgs a, Slots sl) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* sm = smem + L;
+  load_twiddles(tw, a.pl);
+  const int k = blockIdx.y;
+  const int64_t row0 = (int64_t)blockIdx.x * a.rpc;
+  const int nr = (int)min((int64_t)a.rpc, a.nrows - row0);
+  const int NO = a.rpc * a.ncg;
+  const int nkeep = (a.n1 * 2 == L) ? R2 / 2 : R2;
+  __syncthreads();
+  step_a<SP, +1>(sm, sl, NO, tw, R1, [&](int lo, int, int m) -> float2 {
+    const int rl = lo / a.ncg, cl = lo - rl * a.ncg;
+    if (rl >= nr) return make_float2(0.f, 0.f);
+    return a.stack[(((int64_t)cl * a.K + k) * a.nrows + row0 + rl) * L + m];
+  });
+  __syncthreads();
+  step_b<SP, +1>(sm, sl, NO, nkeep, [&](int lo, int li, int f1, int f2, float2 v) { sm[sl.at(lo, f1, f2, li, R1)] = v; });
+  __syncthreads();
+  for (int e = threadIdx.x; e < nr * a.n1; e += blockDim.x) {
+    const int rl = e / a.n1, i1 = e - rl * a.n1;
+    const int f1 = i1 % R1, f2 = i1 / R1;
+    const int64_t r = row0 + rl;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int cl = 0; cl < a.ncg; ++cl) {
+      const float2 v = sm[sl.at(rl * a.ncg + cl, f1, f2, 0, R1)];
+      if (a.cmaps)
+        acc = cadd(acc, cmulc(v, a.cmaps[i1 + (int64_t)a.n1 * (r + a.nrows * (a.c0 + cl))]));
+      else
+        acc = cadd(acc, v);
+    }
+    const int64_t yi = i1 + (int64_t)a.n1 * (r + a.nrows * k);
+    float2 yv;
+    if (a.first)
+      yv = (a.beta.x == 0.f && a.beta.y == 0.f) ? make_float2(0.f, 0.f) : cmul(a.beta, a.y[yi]);
+    else
+      yv = a.y[yi];
+    a.y[yi] = cadd(yv, cmul(a.alpha, acc));
+  }
+}
+
+template <class SP>
+__global__ void __launch_bounds__(256, 2) k4_lambda(LamPassArgs a, Slots sl) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* sm = smem + L;
+  load_twiddles(tw, a.pl);
+  const int cl = blockIdx.y;
+  const int64_t tile = blockIdx.x;
+  const int64_t plane = (int64_t)a.nrow * a.inner;
+  float2* base = a.stack + (int64_t)cl * a.K * plane + tile * a.TC;
+  const int nload = (a.nin * 2 == L) ? R1 / 2 : R1;
+  const int nkeep = (a.nout * 2 == L) ? R1 / 2 : R1;
+  __syncthreads();
+  step_a<SP, -1>(sm, sl, a.K, tw, nload, [&](int k, int li, int n) -> float2 {
+    return (n < a.nin) ? base[k * plane + (int64_t)n * a.inner + li] : make_float2(0.f, 0.f);
+  });
+  __syncthreads();
+  step_b<SP, -1>(sm, sl, a.K, R2, [&](int lo, int li, int f1, int f2, float2 v) { sm[sl.at(lo, f1, f2, li, R1)] = v; });
+  __syncthreads();
+  // per-voxel K x K product at every frequency f = f1 + R1 f2 of the tile
+  for (int t = threadIdx.x; t < (L << sl.tcs); t += blockDim.x) {
+    const int li = t & (a.TC - 1);
+    const int r = t >> sl.tcs;
+    const int f1 = r % R1, f2 = r / R1;
+    const int f = f1 + R1 * f2;
+    float2 X[KMAX], Y[KMAX];
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) X[k] = (k < a.K) ? sm[sl.at(k, f1, f2, li, R1)] : make_float2(0.f, 0.f);
+    const int64_t lbase = lam_elem(tile, f, li, 0, a.TC, a.P, a.FC, a.NCH);
+    lam_apply<KMAX>(a, lbase, (int64_t)a.FC * a.TC, X, Y);
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k)
+      if (k < a.K) sm[sl.at(k, f1, f2, li, R1)] = Y[k];
+  }
+  __syncthreads();
+  inv_step_a_slots<SP>(sm, sl, a.K, tw);
+  __syncthreads();
+  inv_step_b_slots<SP>(sm, sl, a.K, nkeep, [&](int k, int li, int n, float2 v) {
+    if (n < a.nout) base[k * plane + (int64_t)n * a.inner + li] = v;
+  });
+}
+
+template <class SP, int S>
+__global__ void __launch_bounds__(512) k4_mid(MidArgs a, Slots sl) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* sm = smem + L;
+  load_twiddles(tw, a.pl);
+  const int64_t col0 = (int64_t)blockIdx.x * a.TC;
+  const int64_t o0 = (int64_t)blockIdx.y * a.NOo;
+  const int no = (int)min((int64_t)a.NOo, a.n3 - o0);
+  const int64_t p = blockIdx.z;
+  const float2* ib = a.in + (p * a.n3 + o0) * a.nin * a.width + col0;
+  float2* ob = a.out + (p * a.n3 + o0) * a.nout * a.width + col0;
+  const int nload = (a.nin * 2 == L) ? R1 / 2 : R1;
+  const int nkeep = (a.nout * 2 == L) ? R2 / 2 : R2;
+  __syncthreads();
+  step_a<SP, S>(sm, sl, a.NOo, tw, nload, [&](int o, int li, int n) -> float2 {
+    return (o < no && n < a.nin) ? ib[((int64_t)o * a.nin + n) * a.width + li] : make_float2(0.f, 0.f);
+  });
+  __syncthreads();
+  step_b<SP, S>(sm, sl, a.NOo, nkeep, [&](int o, int li, int f1, int f2, float2 v) {
+    const int n = f1 + R1 * f2;
+    if (o < no && n < a.nout) ob[((int64_t)o * a.nout + n) * a.width + li] = v;
+  });
+}
+
+
+// Persistent Λ pass with TMA.  Each CTA walks over (tile, coil) items with a
+// grid stride.  The input tile (K planes x nin rows x TC columns) of the next
+// item is fetched by one cp.async.bulk.tensor copy into the second of two
+// staging buffers while the current item is transformed; Λ streams through a
+// ring of kLamRing chunk buffers filled by 1D bulk copies.  Both are tracked
+// by transaction-count mbarriers; waits are bounded and report KERR_MBAR_TIMEOUT.
+constexpr int kLamRing = 3;
+
+struct Lam5Cfg {
+  int nboxes, box_rows;   // input row boxes (box_rows <= 256)
+  int in_elems;           // float2 per input buffer = K * nboxes * box_rows * TC
+  int chunk_bytes;        // bytes per Λ chunk
+  int64_t ntiles, nitems;
+  int* err;
+  uint32_t off_tw, off_in0, off_in1, off_ring, off_slots;  // byte offsets in dynamic smem
+};
+
+template <class SP>
+__global__ void __launch_bounds__(512, 1) k5_lambda(LamPassArgs a, Slots sl, Lam5Cfg cf,
+                                                    const __grid_constant__ CUtensorMap tin) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  extern __shared__ __align__(1024) unsigned char sraw[];
+  uint64_t* bar_in = reinterpret_cast<uint64_t*>(sraw);
+  uint64_t* bar_lam = bar_in + 2;
+  float2* tw = reinterpret_cast<float2*>(sraw + cf.off_tw);
+  float2* in0 = reinterpret_cast<float2*>(sraw + cf.off_in0);
+  float2* in1 = reinterpret_cast<float2*>(sraw + cf.off_in1);
+  unsigned char* ring = sraw + cf.off_ring;
+  float2* sm = reinterpret_cast<float2*>(sraw + cf.off_slots);
+  const bool leader = threadIdx.x == 0;
+  if (leader) {
+    mbar_init(&bar_in[0], 1);
+    mbar_init(&bar_in[1], 1);
+    for (int r = 0; r < kLamRing; ++r) mbar_init(&bar_lam[r], 1);
+    fence_mbar_init();
+  }
+  load_twiddles(tw, a.pl);
+  __syncthreads();
+  const int64_t G = gridDim.x;
+  const int64_t first = blockIdx.x;
+  const int nload = (a.nin * 2 == L) ? R1 / 2 : R1;
+  const int nkeep = (a.nout * 2 == L) ? R1 / 2 : R1;
+  const int64_t plane = (int64_t)a.nrow * a.inner;
+  const uint32_t in_bytes = (uint32_t)cf.in_elems * 8u;
+
+  auto issue_input = [&](int64_t item, int buf) {
+    const int64_t tile = item % cf.ntiles;
+    const int cl = (int)(item / cf.ntiles);
+    float2* dst = buf ? in1 : in0;
+    mbar_arrive_expect_tx(&bar_in[buf], in_bytes);
+    for (int b = 0; b < cf.nboxes; ++b)
+      tma_g2s_3d(dst + (int64_t)b * a.K * cf.box_rows * a.TC, &tin, (int)(2 * tile * a.TC), b * cf.box_rows,
+                 cl * a.K, &bar_in[buf]);
+  };
+  auto issue_chunk = [&](int64_t s) {  // s: this CTA's running chunk number
+    const int64_t j = s / a.NCH;
+    const int ch = (int)(s - j * a.NCH);
+    const int64_t item = first + j * G;
+    if (item >= cf.nitems) return;
+    const int64_t tile = item % cf.ntiles;
+    const int r = (int)(s % kLamRing);
+    const unsigned char* src = reinterpret_cast<const unsigned char*>(a.lam) + (tile * a.NCH + ch) * (int64_t)cf.chunk_bytes;
+    mbar_arrive_expect_tx(&bar_lam[r], (uint32_t)cf.chunk_bytes);
+    bulk_g2s(ring + (int64_t)r * cf.chunk_bytes, src, (uint32_t)cf.chunk_bytes, &bar_lam[r]);
+  };
+
+  if (leader) {
+    if (first < cf.nitems) issue_input(first, 0);
+    for (int s = 0; s < kLamRing; ++s) issue_chunk(s);
+  }
+  int failed = 0;
+  for (int64_t j = 0; first + j * G < cf.nitems; ++j) {
+    const int64_t item = first + j * G;
+    const int64_t tile = item % cf.ntiles;
+    const int cl = (int)(item / cf.ntiles);
+    const int buf = (int)(j & 1);
+    if (leader && item + G < cf.nitems) {
+      fence_proxy_async_smem();
+      issue_input(item + G, buf ^ 1);
+    }
+    const bool ok_in = mbar_wait(&bar_in[buf], (uint32_t)((j >> 1) & 1));
+    if (__syncthreads_or(!ok_in)) { failed = 1; break; }
+    const float2* ib = buf ? in1 : in0;
+    float2* base = a.stack + (int64_t)cl * a.K * plane + tile * a.TC;
+    step_a<SP, -1>(sm, sl, a.K, tw, nload, [&](int k, int li, int n) -> float2 {
+      if (n >= a.nin) return make_float2(0.f, 0.f);
+      const int b = n / cf.box_rows, rr = n - b * cf.box_rows;
+      return ib[(((int64_t)b * a.K + k) * cf.box_rows + rr) * a.TC + li];
+    });
+    __syncthreads();
+    step_b<SP, -1>(sm, sl, a.K, R2, [&](int lo, int li, int f1, int f2, float2 v) { sm[sl.at(lo, f1, f2, li, R1)] = v; });
+    __syncthreads();
+    for (int ch = 0; ch < a.NCH; ++ch) {
+      const int64_t s = j * a.NCH + ch;
+      const int r = (int)(s % kLamRing);
+      const bool ok = mbar_wait(&bar_lam[r], (uint32_t)((s / kLamRing) & 1));
+      if (__syncthreads_or(!ok)) { failed = 1; break; }
+      const unsigned char* lc = ring + (int64_t)r * cf.chunk_bytes;
+      for (int t = threadIdx.x; t < a.FC * a.TC; t += blockDim.x) {
+        const int li = t & (a.TC - 1);
+        const int fc = t >> sl.tcs;
+        const int f = ch * a.FC + fc;
+        const int f1 = f % R1, f2 = f / R1;
+        float2 X[KMAX], Y[KMAX];
+#pragma unroll
+        for (int k = 0; k < KMAX; ++k) X[k] = (k < a.K) ? sm[sl.at(k, f1, f2, li, R1)] : make_float2(0.f, 0.f);
+        lam_apply_ptr<KMAX>(a.lam_mode, a.K, lc, (int64_t)fc * a.TC + li, (int64_t)a.FC * a.TC, X, Y);
+#pragma unroll
+        for (int k = 0; k < KMAX; ++k)
+          if (k < a.K) sm[sl.at(k, f1, f2, li, R1)] = Y[k];
+      }
+      __syncthreads();
+      if (leader) {
+        fence_proxy_async_smem();
+        issue_chunk(s + kLamRing);
+      }
+    }
+    if (failed) break;
+    inv_step_a_slots<SP>(sm, sl, a.K, tw);
+    __syncthreads();
+    inv_step_b_slots<SP>(sm, sl, a.K, nkeep, [&](int k, int li, int n, float2 v) {
+      if (n < a.nout) base[k * plane + (int64_t)n * a.inner + li] = v;
+    });
+    __syncthreads();
+  }
+  if (failed) {
+    if (leader) atomicExch(cf.err, KERR_MBAR_TIMEOUT);
+    // give copies still in flight a bounded chance to land before the CTA exits
+    for (int b = 0; b < 2; ++b) (void)mbar_try_wait(&bar_in[b], 0);
+    __syncthreads();
+  }
+}
+
+// -------------------------------------------------------- dispatch ---
+
+template <class F>
+static int with_split(int L, F f) {
+  switch (L) {
+    case 64: return f(Split<8, 8>());
+    case 128: return f(Split<8, 16>());
+    case 256: return f(Split<16, 16>());
+    case 384: return f(Split<12, 32>());
+    case 512: return f(Split<16, 32>());
+    case 768: return f(Split<24, 32>());
+    case 1024: return f(Split<32, 32>());
+    default: return MRSR_ERR_UNSUPPORTED;
+  }
+}
+
+bool fast_length(int L) { return L == 64 || L == 128 || L == 256 || L == 384 || L == 512 || L == 768 || L == 1024; }
+
+static Slots make_slots(int R2, int TC) {
+  Slots s;
+  s.TC = TC;
+  s.tcs = 0;
+  while ((1 << s.tcs) < TC) ++s.tcs;
+  s.W = slots_width(R2, TC);
+  return s;
+}
+
+template <class K, class A>
+static int launch(K k, dim3 grid, int threads, size_t smem, cudaStream_t st, const A& a, const Slots& sl) {
+  MRSR_REQUIRE(smem <= 227 * 1024, MRSR_ERR_UNSUPPORTED, "shared memory request %zu too large", smem);
+  if (smem > 48 * 1024) MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+  k<<<grid, threads, smem, st>>>(a, sl);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+static int round_threads(int tasks) {
+  int t = ((tasks + 31) / 32) * 32;
+  return t < 128 ? 128 : (t > 512 ? 512 : t);
+}
+
+int fast_rows_fwd(const RowsFwdArgs& a, int64_t nrows, int ncg, cudaStream_t st) {
+  return with_split(a.pl.L, [&](auto sp) -> int {
+    using SP = decltype(sp);
+    const Slots sl = make_slots(SP::R2, 1);
+    const int NO = a.rpc * a.K;
+    const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)NO * SP::R1 * sl.W);
+    dim3 grid((unsigned)cdiv(nrows, a.rpc), ncg);
+    return launch(k4_rows_fwd<SP>, grid, round_threads(NO * SP::R1), smem, st, a, sl);
+  });
+}
+
+int fast_rows_inv(const RowsInvArgs& a, int64_t nrows, cudaStream_t st) {
+  return with_split(a.pl.L, [&](auto sp) -> int {
+    using SP = decltype(sp);
+    const Slots sl = make_slots(SP::R2, 1);
+    const int NO = a.rpc * a.ncg;
+    const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)NO * SP::R1 * sl.W);
+    dim3 grid((unsigned)cdiv(nrows, a.rpc), a.K);
+    return launch(k4_rows_inv<SP>, grid, round_threads(NO * SP::R1), smem, st, a, sl);
+  });
+}
+
+static int num_sms() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+static uint32_t align128(uint32_t x) { return (x + 127u) & ~127u; }
+
+int fast_lambda(const LamPassArgs& a, int ncg, int planes_total, int* errword, cudaStream_t st) {
+  return with_split(a.pl.L, [&](auto sp) -> int {
+    using SP = decltype(sp);
+    const Slots sl = make_slots(SP::R2, a.TC);
+    const int esz = a.lam_mode == LAM_PACKED_REAL ? 4 : 8;
+    // TMA pipeline: needs >= 16-byte column boxes and everything in shared memory
+    Lam5Cfg cf{};
+    cf.nboxes = (a.nin + 255) / 256;
+    cf.box_rows = (a.nin + cf.nboxes - 1) / cf.nboxes;
+    cf.in_elems = a.K * cf.nboxes * cf.box_rows * a.TC;
+    cf.chunk_bytes = a.P * a.FC * a.TC * esz;
+    cf.ntiles = a.inner / a.TC;
+    cf.nitems = cf.ntiles * ncg;
+    cf.err = errword;
+    uint32_t off = 128;  // mbarriers
+    cf.off_tw = off;
+    off = align128(off + SP::L * 8);
+    cf.off_in0 = off;
+    off = align128(off + cf.in_elems * 8);
+    cf.off_in1 = off;
+    off = align128(off + cf.in_elems * 8);
+    cf.off_ring = off;
+    off = align128(off + kLamRing * cf.chunk_bytes);
+    cf.off_slots = off;
+    off += (uint32_t)(a.K * SP::R1 * sl.W * 8);
+    const bool box_aligned = ((int64_t)a.K * cf.box_rows * a.TC * 8) % 128 == 0 || cf.nboxes == 1;
+    const bool tma_ok = a.TC >= 2 && off <= 227u * 1024u && cf.chunk_bytes % 16 == 0 && box_aligned &&
+                        std::getenv("MRSR_TMA_LAMBDA") != nullptr;
+    if (tma_ok) {
+      CUtensorMap tm;
+      const uint64_t dims[3] = {(uint64_t)(2 * a.inner), (uint64_t)a.nrow, (uint64_t)planes_total};
+      const uint64_t strides[2] = {(uint64_t)(2 * a.inner * 4), (uint64_t)(2 * a.inner * 4) * (uint64_t)a.nrow};
+      const uint32_t box[3] = {(uint32_t)(2 * a.TC), (uint32_t)cf.box_rows, (uint32_t)a.K};
+      MRSR_TRY(encode_tmap_f32_3d(&tm, a.stack, dims, strides, box));
+      auto k = k5_lambda<SP>;
+      MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)off));
+      MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+      const int64_t grid = std::min<int64_t>(cf.nitems, num_sms());
+      k<<<(unsigned)grid, 512, off, st>>>(a, sl, cf, tm);
+      MRSR_LAUNCH_CHECK();
+      return MRSR_OK;
+    }
+    const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)a.K * SP::R1 * sl.W);
+    dim3 grid((unsigned)(a.inner / a.TC), ncg);
+    return launch(k4_lambda<SP>, grid, 256, smem, st, a, sl);
+  });
+}
+
+int fast_mid(const MidArgs& a, int nplanes, cudaStream_t st) {
+  return with_split(a.pl.L, [&](auto sp) -> int {
+    using SP = decltype(sp);
+    const Slots sl = make_slots(SP::R2, a.TC);
+    const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)a.NOo * SP::R1 * sl.W);
+    dim3 grid((unsigned)(a.width / a.TC), (unsigned)cdiv(a.n3, a.NOo), (unsigned)nplanes);
+    const int thr = round_threads(a.NOo * a.TC * SP::R1);
+    if (a.sgn < 0) return launch(k4_mid<SP, -1>, grid, thr, smem, st, a, sl);
+    return launch(k4_mid<SP, +1>, grid, thr, smem, st, a, sl);
+  });
+}
+
+}  // namespace mrsr

@@ -1,0 +1,32 @@
+"""Generates twiddles.cuh: __constant__ tables exp(2 pi i m / R) for the
+register DFT base lengths (values computed in float64, rounded to float32)."""
+import math
+import struct
+from pathlib import Path
+
+BASES = (32, 24, 20, 30)
+
+
+def main():
+    lines = ["// Generated by gen_twiddles.py: c_tw<R>[m] = (cos(2 pi m/R), sin(2 pi m/R)), m < R.",
+             "#pragma once", "#include <cuda_runtime.h>", "", "namespace mrsr {", ""]
+    for R in BASES:
+        vals = []
+        for m in range(R):
+            a = 2.0 * math.pi * m / R
+            c, s = math.cos(a), math.sin(a)
+            c = 0.0 if abs(c) < 1e-12 else c  # exact zeros at multiples of pi/2
+            s = 0.0 if abs(s) < 1e-12 else s
+            c32, s32 = (struct.unpack("f", struct.pack("f", v))[0] for v in (c, s))  # round to float32
+            vals.append(f"{{{float.hex(c32)}f, {float.hex(s32)}f}}")
+        lines.append(f"static __constant__ float2 c_tw{R}[{R}] = {{")
+        for i in range(0, R, 4):
+            lines.append("    " + ", ".join(vals[i:i + 4]) + ",")
+        lines.append("};")
+        lines.append("")
+    lines.append("}  // namespace mrsr")
+    Path(__file__).with_name("twiddles.cuh").write_text("\n".join(lines) + "\n")
+
+
+if __name__ == "__main__":
+    main()

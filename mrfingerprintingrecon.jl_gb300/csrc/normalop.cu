@@ -20,24 +20,13 @@
 #include <cstring>
 #include <vector>
 
-#include "normalop.cuh"
+#include "passes.cuh"
 
 namespace mrsr {
 
 // ------------------------------------------------------------- kernels ---
 
-struct RowsFwdArgs {
-  FftPlan pl;        // along dim 1, L = g1
-  int n1;            // valid input length (image dim 1)
-  int64_t nrows;     // rows per plane: n2 * n3
-  int rpc;           // rows per CTA
-  int K;
-  int c0;            // first coil of the group
-  int lstride;       // smem line stride (float2)
-  const float2* x;   // (n1, nrows, K)
-  const float2* cmaps;  // (n1, nrows, ncoils) or null
-  float2* out;       // [cl][k][row][L]
-};
+
 
 __global__ void __launch_bounds__(512) k_rows_fwd(RowsFwdArgs a) {
   extern __shared__ float2 smem[];
@@ -81,73 +70,9 @@ __global__ void __launch_bounds__(512) k_rows_fwd(RowsFwdArgs a) {
   }
 }
 
-struct LamPassArgs {
-  FftPlan pl;          // along the last dim
-  int nin, nout;       // valid input rows / kept output rows (same storage rows: nrow)
-  int nrow;            // stored rows of a plane along the last dim
-  int64_t inner;       // stored plane width (contiguous)
-  int TC, K, P;
-  int lam_mode;
-  int lstride;         // = L * TC (+ pad)
-  const void* lam;     // [tile][f][P][TC]
-  float2* stack;       // planes [cl][k][row][inner], in place
-};
 
-// Per-voxel K x K product Y = Λ X at one frequency (X, Y in registers).
-template <int KMAX>
-__device__ __forceinline__ void lam_apply(const LamPassArgs& a, int64_t lbase, const float2* X, float2* Y) {
-#pragma unroll
-  for (int j = 0; j < KMAX; ++j) Y[j] = make_float2(0.f, 0.f);
-  if (a.lam_mode == LAM_PACKED_REAL) {
-    const float* lam = reinterpret_cast<const float*>(a.lam);
-    int p = 0;
-#pragma unroll
-    for (int k2 = 0; k2 < KMAX; ++k2) {
-#pragma unroll
-      for (int k1 = 0; k1 <= k2; ++k1) {
-        if (k2 < a.K) {
-          const float l = lam[lbase + (int64_t)p * a.TC];
-          Y[k1].x += l * X[k2].x;
-          Y[k1].y += l * X[k2].y;
-          if (k1 != k2) {
-            Y[k2].x += l * X[k1].x;
-            Y[k2].y += l * X[k1].y;
-          }
-        }
-        ++p;
-      }
-    }
-  } else if (a.lam_mode == LAM_PACKED_CPLX) {
-    const float2* lam = reinterpret_cast<const float2*>(a.lam);
-    int p = 0;
-#pragma unroll
-    for (int k2 = 0; k2 < KMAX; ++k2) {
-#pragma unroll
-      for (int k1 = 0; k1 <= k2; ++k1) {
-        if (k2 < a.K) {
-          const float2 l = lam[lbase + (int64_t)p * a.TC];
-          Y[k1] = cadd(Y[k1], cmul(l, X[k2]));
-          if (k1 != k2) Y[k2] = cadd(Y[k2], cmul(cconj(l), X[k1]));
-        }
-        ++p;
-      }
-    }
-  } else {
-    const float2* lam = reinterpret_cast<const float2*>(a.lam);
-#pragma unroll
-    for (int k2 = 0; k2 < KMAX; ++k2) {
-#pragma unroll
-      for (int k1 = 0; k1 < KMAX; ++k1) {
-        if (k1 < a.K && k2 < a.K) {
-          const float2 l = lam[lbase + (int64_t)(k1 + a.K * k2) * a.TC];
-          Y[k1] = cadd(Y[k1], cmul(l, X[k2]));
-        }
-      }
-    }
-  }
-}
 
-constexpr int KMAX = 8;
+
 
 __global__ void __launch_bounds__(512) k_lambda_pass(LamPassArgs a) {
   extern __shared__ float2 smem[];
@@ -189,8 +114,8 @@ __global__ void __launch_bounds__(512) k_lambda_pass(LamPassArgs a) {
     float2 X[KMAX], Y[KMAX];
 #pragma unroll
     for (int k = 0; k < KMAX; ++k) X[k] = (k < a.K) ? X0[k * a.lstride + pos] : make_float2(0.f, 0.f);
-    const int64_t lbase = ((tile * L + f) * (int64_t)a.P) * a.TC + li;
-    lam_apply<KMAX>(a, lbase, X, Y);
+    const int64_t lbase = lam_elem(tile, f, li, 0, a.TC, a.P, a.FC, a.NCH);
+    lam_apply<KMAX>(a, lbase, (int64_t)a.FC * a.TC, X, Y);
 #pragma unroll
     for (int k = 0; k < KMAX; ++k)
       if (k < a.K) X0[k * a.lstride + pos] = Y[k];
@@ -206,17 +131,7 @@ __global__ void __launch_bounds__(512) k_lambda_pass(LamPassArgs a) {
   }
 }
 
-struct MidArgs {
-  FftPlan pl;        // along dim 2
-  int nin, nout;     // valid input rows / kept output rows along dim 2
-  int64_t width;     // contiguous extent (g1)
-  int64_t n3;        // outer count (image dim 3)
-  int TC, NOo;       // columns and outer slices per CTA
-  int lstride;
-  float sgn;
-  const float2* in;  // planes [p][i3][nin][width]
-  float2* out;       // planes [p][i3][nout][width]
-};
+
 
 __global__ void __launch_bounds__(512) k_mid_fft(MidArgs a) {
   extern __shared__ float2 smem[];
@@ -261,21 +176,7 @@ __global__ void __launch_bounds__(512) k_mid_fft(MidArgs a) {
   }
 }
 
-struct RowsInvArgs {
-  FftPlan pl;        // along dim 1
-  int n1;            // kept output length
-  int64_t nrows;
-  int rpc;
-  int K;
-  int c0, ncg;       // coils of this group
-  int lstride;
-  int first;         // first coil group: apply beta
-  float2 alpha;      // alpha / prod(grid)
-  float2 beta;
-  const float2* stack;  // [cl][k][row][L]
-  const float2* cmaps;  // (n1, nrows, ncoils) or null
-  float2* y;            // (n1, nrows, K)
-};
+
 
 __global__ void __launch_bounds__(512) k_rows_inv(RowsInvArgs a) {
   extern __shared__ float2 smem[];
@@ -326,7 +227,7 @@ __global__ void __launch_bounds__(512) k_rows_inv(RowsInvArgs a) {
 struct LamLayout {
   int64_t inner;   // Λ-pass plane width
   int64_t L;       // last-dim grid length
-  int TC, P;
+  int TC, P, FC, NCH;
   int64_t ngrid;
 };
 
@@ -335,7 +236,7 @@ __device__ __forceinline__ int64_t lam_int_index(const LamLayout& g, int64_t cel
   const int64_t in = cell - f * g.inner;
   const int64_t tile = in / g.TC;
   const int64_t li = in - tile * g.TC;
-  return ((tile * g.L + f) * g.P + p) * g.TC + li;
+  return lam_elem(tile, (int)f, (int)li, p, g.TC, g.P, g.FC, g.NCH);
 }
 
 template <class T>
@@ -485,6 +386,7 @@ template <class Args>
 static int launch_fft_kernel(void (*k)(Args), dim3 grid, int threads, size_t smem, cudaStream_t st, const Args& a) {
   MRSR_REQUIRE(smem <= 227 * 1024, MRSR_ERR_UNSUPPORTED, "shared memory request %zu too large", smem);
   if (smem > 48 * 1024) MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
   k<<<grid, threads, smem, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
@@ -550,7 +452,10 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       RowTiling t = rows_tiling(L1, K, nrows);
       RowsFwdArgs a{op->plan[0].plan, (int)g.n[0], nrows, t.rpc, K, c0, t.lstride, x, cm, st1};
       dim3 grid((unsigned)cdiv(nrows, t.rpc), ncg);
-      MRSR_TRY(launch_fft_kernel<RowsFwdArgs>(k_rows_fwd, grid, t.threads, t.smem, st, a));
+      if (fast_length(L1))
+        MRSR_TRY(fast_rows_fwd(a, nrows, ncg, st));
+      else
+        MRSR_TRY(launch_fft_kernel<RowsFwdArgs>(k_rows_fwd, grid, t.threads, t.smem, st, a));
       MRSR_TRY(rec.record());
     }
     float2* lam_stack = st1;
@@ -563,7 +468,10 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       MidArgs a{op->plan[1].plan, (int)g.n[1], L2, g.g[0], g.n[2], TC, NOo, L2 * TC, -1.f, st1, st2};
       dim3 grid((unsigned)(g.g[0] / TC), (unsigned)cdiv(g.n[2], NOo), (unsigned)(ncg * K));
       const size_t smem = sizeof(float2) * ((size_t)L2 + 2 * (size_t)NOo * a.lstride);
-      MRSR_TRY(launch_fft_kernel<MidArgs>(k_mid_fft, grid, 256, smem, st, a));
+      if (fast_length(L2))
+        MRSR_TRY(fast_mid(a, ncg * K, st));
+      else
+        MRSR_TRY(launch_fft_kernel<MidArgs>(k_mid_fft, grid, 256, smem, st, a));
       MRSR_TRY(rec.record());
       lam_stack = st2;
     }
@@ -572,10 +480,13 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       const int Ll = (int)g.glast();
       const int TC = op->TC;
       LamPassArgs a{op->plan[g.ndims - 1].plan, (int)g.nlast(), (int)g.nlast(), (int)g.nlast(), g.inner(), TC, K,
-                    op->P, op->lam_mode, Ll * TC, op->lam.p, lam_stack};
+                    op->P, op->lam_mode, Ll * TC, op->lam.p, lam_stack, op->FC, (int)(Ll / op->FC)};
       dim3 grid((unsigned)(g.inner() / TC), ncg);
       const size_t smem = sizeof(float2) * ((size_t)Ll + 2 * (size_t)K * a.lstride);
-      MRSR_TRY(launch_fft_kernel<LamPassArgs>(k_lambda_pass, grid, 512, smem, st, a));
+      if (fast_length(Ll))
+        MRSR_TRY(fast_lambda(a, ncg, op->Cg * K, op->errflag.as<int>(), st));
+      else
+        MRSR_TRY(launch_fft_kernel<LamPassArgs>(k_lambda_pass, grid, 512, smem, st, a));
       MRSR_TRY(rec.record());
     }
     if (g.ndims == 3) {
@@ -586,7 +497,10 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       MidArgs a{op->plan[1].plan, L2, (int)g.n[1], g.g[0], g.n[2], TC, NOo, L2 * TC, +1.f, st2, st1};
       dim3 grid((unsigned)(g.g[0] / TC), (unsigned)cdiv(g.n[2], NOo), (unsigned)(ncg * K));
       const size_t smem = sizeof(float2) * ((size_t)L2 + 2 * (size_t)NOo * a.lstride);
-      MRSR_TRY(launch_fft_kernel<MidArgs>(k_mid_fft, grid, 256, smem, st, a));
+      if (fast_length(L2))
+        MRSR_TRY(fast_mid(a, ncg * K, st));
+      else
+        MRSR_TRY(launch_fft_kernel<MidArgs>(k_mid_fft, grid, 256, smem, st, a));
       MRSR_TRY(rec.record());
     }
     // P3: rows inverse + crop + coil combine
@@ -595,7 +509,10 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       RowsInvArgs a{op->plan[0].plan, (int)g.n[0], nrows, t.rpc, K, c0, ncg, t.lstride, grp == 0 ? 1 : 0, al, beta,
                     st1, cm, y};
       dim3 grid((unsigned)cdiv(nrows, t.rpc), K);
-      MRSR_TRY(launch_fft_kernel<RowsInvArgs>(k_rows_inv, grid, t.threads, t.smem, st, a));
+      if (fast_length(L1))
+        MRSR_TRY(fast_rows_inv(a, nrows, st));
+      else
+        MRSR_TRY(launch_fft_kernel<RowsInvArgs>(k_rows_inv, grid, t.threads, t.smem, st, a));
       MRSR_TRY(rec.record());
     }
   }
@@ -636,8 +553,10 @@ int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_
     MRSR_TRY(op->plan[i].init((int)g.g[i]));
   }
   // Λ-pass tile width: up to 8 columns, a divisor of the plane width, <= 16384 elements per CTA
+  // generic kernels: two K*TC*L buffers; four-step kernels: one K*TC*L exchange buffer (<= ~110 KB, 2 CTAs/SM)
   int TC = (int)env_int("MRSR_LAMBDA_TC", 8);
-  while (TC > 1 && ((int64_t)K * TC * g.glast() > 12288 || g.inner() % TC != 0)) TC >>= 1;
+  const int64_t budget = fast_length((int)g.glast()) ? 13000 : 12288;
+  while (TC > 1 && ((int64_t)K * TC * g.glast() > budget || g.inner() % TC != 0)) TC >>= 1;
   op->TC = TC;
   MRSR_TRY(op->errflag.alloc(sizeof(int)));
   return MRSR_OK;
@@ -686,8 +605,25 @@ static LamLayout lam_layout(const mrsr_normalop* op) {
   l.L = op->geo.glast();
   l.TC = op->TC;
   l.P = op->P;
+  l.FC = op->FC;
+  l.NCH = (int)(l.L / op->FC);
   l.ngrid = op->geo.ngrid();
   return l;
+}
+
+// Λ chunk length: the largest divisor of L with at most 256 positions (FC*TC)
+// and at most 16 KB per chunk, so a chunk streams through a small shared ring.
+static void choose_fc(mrsr_normalop* op) {
+  const int L = (int)op->geo.glast();
+  const int esz = op->lam_mode == LAM_PACKED_REAL ? 4 : 8;
+  int best = 1;
+  for (int fc = 1; fc <= L; ++fc) {
+    if (L % fc) continue;
+    if ((int64_t)fc * op->TC > 256) continue;
+    if ((int64_t)fc * op->TC * op->P * esz > 16384) continue;
+    best = fc;
+  }
+  op->FC = best;
 }
 
 int op_set_lambda_packed(mrsr_normalop* op, const void* lam_packed, int is_complex, const int64_t* kmask, int64_t nk,
@@ -698,6 +634,7 @@ int op_set_lambda_packed(mrsr_normalop* op, const void* lam_packed, int is_compl
   op->lam_mode = is_complex ? LAM_PACKED_CPLX : LAM_PACKED_REAL;
   op->P = K * (K + 1) / 2;
   op->nk = nk;
+  choose_fc(op);
   const size_t esz = is_complex ? sizeof(float2) : sizeof(float);
   MRSR_TRY(op->lam.alloc(esz * op->P * op->geo.ngrid()));
   MRSR_CHECK_CUDA(cudaMemsetAsync(op->lam.p, 0, op->lam.bytes, st));
@@ -735,6 +672,7 @@ int op_set_lambda_full(mrsr_normalop* op, const float2* lam_full, cudaStream_t s
   op->lam_mode = LAM_FULL_CPLX;
   op->P = K * K;
   op->nk = nk;
+  choose_fc(op);
   MRSR_TRY(op->lam.alloc(sizeof(float2) * op->P * ng));
   MRSR_CHECK_CUDA(cudaMemsetAsync(op->lam.p, 0, op->lam.bytes, st));
   DevBuf packed;

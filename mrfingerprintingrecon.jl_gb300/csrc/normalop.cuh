@@ -35,10 +35,11 @@ struct mrsr_normalop {
   int P = 1;      // kernel entries per voxel in the internal layout
   int64_t nk = 0;
   int TC = 4;     // Λ-pass tile width (columns)
+  int FC = 1;     // Λ chunk length along the last dim
   int Cg = 1;     // coils per group
   int launches = 0;
   mrsr::DevBuf kmask;      // int64 nk, 1-based column-major grid indices
-  mrsr::DevBuf lam;        // [tile][f_last][P][TC] of float / float2 / half / half2
+  mrsr::DevBuf lam;        // [tile][chunk][P][FC][TC] of float / float2 (chunked along f_last)
   mrsr::DevBuf lam_scale;  // fp16: one float per tile
   mrsr::DevBuf cmaps;      // (img..., ncoils) complex; empty = unit coil
   mrsr::DevBuf stack1, stack2;  // intermediates of one coil group

@@ -43,6 +43,11 @@ def _problem(seed, img, K, Nc, density=0.8, complex_lam=True):
     ((16, 16), 1, 0, True),      # cmaps=(1,)
     ((8, 12, 16), 3, 2, True),   # 3D
     ((16, 16, 8), 4, 3, False),  # 3D real kernel
+    ((128, 128), 5, 3, False),   # four-step kernels: 256 = 16 x 16
+    ((256, 64), 4, 2, True),     # 512 = 16 x 32 and 128 = 8 x 16
+    ((192, 96), 3, 2, True),     # 384 = 12 x 32 and 192 (generic)
+    ((32, 32, 32), 5, 2, False), # 3D four-step: 64 = 8 x 8
+    ((32, 64, 32), 3, 2, True),  # 3D mixed: 64 / 128
 ])
 def test_nfft_apply_matches_oracle(mr, cuda, img, K, Nc, cplx):
     lam, cells, cm, x = _problem(1, img, K, Nc, complex_lam=cplx)
