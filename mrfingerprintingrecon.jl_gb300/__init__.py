@@ -6,9 +6,13 @@ no CPU implementation: every call runs on the current CUDA device.
 """
 from . import _lib
 from .normalop import NFFTNormalOp, FFTNormalOp, NormalOperator
-from .arrays import jl_empty, jl_zeros, to_jl, to_host
+from .backprojection import calculate_backprojection, forward_model
+from .solvers import cg, cg_refined
+from .arrays import jl_empty, jl_zeros, jl_reshape, to_jl, to_host
 
-__all__ = ["NFFTNormalOp", "FFTNormalOp", "NormalOperator", "jl_empty", "jl_zeros", "to_jl", "to_host"]
+__all__ = ["NFFTNormalOp", "FFTNormalOp", "NormalOperator", "calculate_backprojection", "forward_model", "cg",
+           "cg_refined",
+           "jl_empty", "jl_zeros", "jl_reshape", "to_jl", "to_host"]
 
 
 def library():

@@ -57,6 +57,17 @@ def to_jl(a, dtype):
     return out
 
 
+def jl_reshape(t, shape):
+    """Julia ``reshape`` (column-major) of a column-major tensor; shares memory."""
+    shape = list(shape)
+    if -1 in shape:
+        i = shape.index(-1)
+        rest = int(np.prod([s for j, s in enumerate(shape) if j != i]))
+        shape[i] = t.numel() // rest
+    c = t.permute(*reversed(range(t.dim())))
+    return c.reshape(tuple(shape[::-1])).permute(*reversed(range(len(shape))))
+
+
 def to_host(t):
     """numpy copy of a device tensor, keeping the Julia index order."""
     return t.detach().cpu().numpy()

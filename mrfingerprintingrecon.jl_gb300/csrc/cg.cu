@@ -1,0 +1,292 @@
+// Conjugate gradients on a normal operator, as IterativeSolvers.jl 0.9 `cg`
+// runs it (x0 = 0): per iteration
+//   u = r + (|r|^2 / prev^2) u,  c = A u,  alpha = |r|^2 / <u, c>,
+//   x += alpha u,  r -= alpha c,  prev = |r|,  |r| = norm(r)
+// stopping once |r| <= max(reltol |b|, abstol) or after maxiter iterations.
+// Vectors are ComplexF32; inner products, norms, alpha and beta are float64
+// on the device.  Reductions are deterministic (per-block partials summed in
+// a fixed order by the last block).  A device "done" flag makes iterations
+// after convergence no-ops, so the host launches without synchronising.
+#include <algorithm>
+#include <cmath>
+
+#include "cg.cuh"
+#include "normalop.cuh"
+
+namespace mrsr {
+
+constexpr int kCgThreads = 256;
+constexpr int kCgBlocks = 1024;
+
+struct CgState {
+  double res;         // |r|
+  double prev;        // previous |r| (1 before the first iteration)
+  double tol;         // max(reltol |b|, abstol)
+  double ar, ai;      // alpha (complex)
+  int it;             // iterations done
+  int maxiter;
+  int done;
+  unsigned int ticket;
+};
+
+__device__ __forceinline__ double2 block_sum2(double2 v) {
+  __shared__ double2 red[kCgThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double2 s = make_double2(0.0, 0.0);
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kCgThreads / 32; ++w) {
+      s.x += red[w].x;
+      s.y += red[w].y;
+    }
+  return s;
+}
+
+// Last block to finish sums the partials in block order; returns true in that block's thread 0.
+__device__ __forceinline__ bool last_block(CgState* st, double2* partial, double2 mine, double2* total) {
+  __shared__ bool is_last;
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = mine;
+    __threadfence();
+    const unsigned t = atomicAdd(&st->ticket, 1u);
+    is_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    double2 s = make_double2(0.0, 0.0);
+    for (unsigned b = 0; b < gridDim.x; ++b) {
+      const volatile double* p = reinterpret_cast<volatile double*>(partial + b);
+      s.x += p[0];
+      s.y += p[1];
+    }
+    *total = s;
+    st->ticket = 0;
+  }
+  return threadIdx.x == 0;
+}
+
+// x = 0, r = b, u = 0, res = |b|
+__global__ void k_cg_init(const float2* b, float2* x, float2* r, float2* u, int64_t n, double reltol, double abstol,
+                          int maxiter, CgState* st, double2* partial) {
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 v = b[i];
+    x[i] = make_float2(0.f, 0.f);
+    r[i] = v;
+    u[i] = make_float2(0.f, 0.f);
+    acc += (double)v.x * v.x + (double)v.y * v.y;
+  }
+  double2 s = block_sum2(make_double2(acc, 0.0));
+  double2 tot;
+  if (last_block(st, partial, s, &tot)) {
+    const double res = sqrt(tot.x);
+    st->res = res;
+    st->prev = 1.0;
+    st->tol = fmax(reltol * res, abstol);
+    st->it = 0;
+    st->maxiter = maxiter;
+    st->done = (maxiter <= 0 || res <= st->tol) ? 1 : 0;
+  }
+}
+
+// u = r + beta u with beta = res^2 / prev^2
+__global__ void k_cg_dir(const float2* r, float2* u, int64_t n, const CgState* st) {
+  if (st->done) return;
+  const double beta = (st->res * st->res) / (st->prev * st->prev);
+  const float b = (float)beta;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 rv = r[i], uv = u[i];
+    u[i] = make_float2(rv.x + b * uv.x, rv.y + b * uv.y);
+  }
+}
+
+// alpha = res^2 / <u, c>  (<u, c> = sum conj(u) c)
+__global__ void k_cg_alpha(const float2* u, const float2* c, int64_t n, CgState* st, double2* partial) {
+  if (st->done) return;
+  double re = 0.0, im = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = u[i], b = c[i];
+    re += (double)a.x * b.x + (double)a.y * b.y;
+    im += (double)a.x * b.y - (double)a.y * b.x;
+  }
+  double2 s = block_sum2(make_double2(re, im));
+  double2 tot;
+  if (last_block(st, partial, s, &tot)) {
+    const double r2 = st->res * st->res;
+    const double den = tot.x * tot.x + tot.y * tot.y;
+    // r2 / (tot.x + i tot.y)
+    st->ar = den > 0.0 ? r2 * tot.x / den : 0.0;
+    st->ai = den > 0.0 ? -r2 * tot.y / den : 0.0;
+  }
+}
+
+// x += alpha u, r -= alpha c, then res = |r|, it += 1, done flag
+__global__ void k_cg_update(float2* x, float2* r, const float2* u, const float2* c, int64_t n, CgState* st,
+                            double2* partial) {
+  if (st->done) return;
+  const float ar = (float)st->ar, ai = (float)st->ai;
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 uv = u[i], cv = c[i];
+    float2 xv = x[i], rv = r[i];
+    xv.x += ar * uv.x - ai * uv.y;
+    xv.y += ar * uv.y + ai * uv.x;
+    rv.x -= ar * cv.x - ai * cv.y;
+    rv.y -= ar * cv.y + ai * cv.x;
+    x[i] = xv;
+    r[i] = rv;
+    acc += (double)rv.x * rv.x + (double)rv.y * rv.y;
+  }
+  double2 s = block_sum2(make_double2(acc, 0.0));
+  double2 tot;
+  if (last_block(st, partial, s, &tot)) {
+    st->prev = st->res;
+    st->res = sqrt(tot.x);
+    st->it += 1;
+    st->done = (st->res <= st->tol || st->it >= st->maxiter) ? 1 : 0;
+  }
+}
+
+static unsigned vec_blocks(int64_t n) {
+  return (unsigned)std::min<int64_t>(kCgBlocks, std::max<int64_t>(1, cdiv(n, kCgThreads)));
+}
+
+int CgWork::ensure(int64_t n_) {
+  if (n == n_ && r.p) return MRSR_OK;
+  n = n_;
+  MRSR_TRY(r.alloc(sizeof(float2) * n));
+  MRSR_TRY(u.alloc(sizeof(float2) * n));
+  MRSR_TRY(c.alloc(sizeof(float2) * n));
+  MRSR_TRY(state.alloc(sizeof(CgState)));
+  MRSR_TRY(partial.alloc(sizeof(double2) * kCgBlocks));
+  MRSR_CHECK_CUDA(cudaMemset(state.p, 0, sizeof(CgState)));
+  return MRSR_OK;
+}
+
+int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter, double reltol, double abstol,
+           cudaStream_t st, int* iters, double* res) {
+  const int64_t n = op->geo.nimg() * op->geo.K;
+  MRSR_TRY(w.ensure(n));
+  CgState* s = w.state.as<CgState>();
+  double2* part = w.partial.as<double2>();
+  const unsigned nb = vec_blocks(n);
+  k_cg_init<<<nb, kCgThreads, 0, st>>>(b, x, w.r.as<float2>(), w.u.as<float2>(), n, reltol, abstol, maxiter, s, part);
+  MRSR_LAUNCH_CHECK();
+  // launch iterations in chunks; between chunks read the done flag so a
+  // converged solve does not keep paying for applies
+  const int chunk = 8;
+  for (int it0 = 0; it0 < maxiter; it0 += chunk) {
+    const int nit = std::min(chunk, maxiter - it0);
+    for (int k = 0; k < nit; ++k) {
+      k_cg_dir<<<nb, kCgThreads, 0, st>>>(w.r.as<float2>(), w.u.as<float2>(), n, s);
+      MRSR_LAUNCH_CHECK();
+      MRSR_TRY(normalop_apply_internal(op, w.u.as<float2>(), w.c.as<float2>(), make_float2(1.f, 0.f),
+                                       make_float2(0.f, 0.f), st));
+      k_cg_alpha<<<nb, kCgThreads, 0, st>>>(w.u.as<float2>(), w.c.as<float2>(), n, s, part);
+      MRSR_LAUNCH_CHECK();
+      k_cg_update<<<nb, kCgThreads, 0, st>>>(x, w.r.as<float2>(), w.u.as<float2>(), w.c.as<float2>(), n, s, part);
+      MRSR_LAUNCH_CHECK();
+    }
+    if (it0 + nit < maxiter) {
+      CgState h;
+      MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+      MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+      if (h.done) break;
+    }
+  }
+  CgState h;
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (iters) *iters = h.it;
+  if (res) *res = h.res;
+  return MRSR_OK;
+}
+
+// r = b - A x  (outer residual of the refinement, float32 operator)
+__global__ void k_copy(const float2* a, float2* b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) b[i] = a[i];
+}
+__global__ void k_axpy(float2* y, const float2* x, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = x[i];
+    float2 b = y[i];
+    b.x += a.x;
+    b.y += a.y;
+    y[i] = b;
+  }
+}
+__global__ void k_norm2(const float2* a, int64_t n, double* out) {
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += (double)a[i].x * a[i].x + (double)a[i].y * a[i].y;
+  double2 s = block_sum2(make_double2(acc, 0.0));
+  if (threadIdx.x == 0) atomicAdd(out, s.x);
+}
+
+}  // namespace mrsr
+
+using namespace mrsr;
+
+extern "C" int mrsr_cg(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
+                       int* iters_out, double* resnorm_out, mrsr_stream_t stream) {
+  MRSR_REQUIRE(op && b && x, MRSR_ERR_ARG, "NULL argument to mrsr_cg");
+  MRSR_REQUIRE((const void*)b != (const void*)x, MRSR_ERR_ARG, "b and x must not alias");
+  MRSR_REQUIRE(maxiter >= 0, MRSR_ERR_ARG, "maxiter must be >= 0");
+  return cg_run(op, op->cg, reinterpret_cast<const float2*>(b), reinterpret_cast<float2*>(x), maxiter, reltol, abstol,
+                reinterpret_cast<cudaStream_t>(stream), iters_out, resnorm_out);
+}
+
+extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const float* b, float* x, int inner_iters,
+                               int max_outer, double tol, int* outer_out, double* relres_out, mrsr_stream_t stream) {
+  MRSR_REQUIRE(op_lo && op_hi && b && x, MRSR_ERR_ARG, "NULL argument to mrsr_cg_refined");
+  MRSR_REQUIRE(op_lo->geo.nimg() == op_hi->geo.nimg() && op_lo->geo.K == op_hi->geo.K, MRSR_ERR_ARG,
+               "operators of different sizes");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int64_t n = op_hi->geo.nimg() * op_hi->geo.K;
+  const float2* bb = reinterpret_cast<const float2*>(b);
+  float2* xx = reinterpret_cast<float2*>(x);
+  DevBuf r, d, nrm;
+  MRSR_TRY(r.alloc(sizeof(float2) * n));
+  MRSR_TRY(d.alloc(sizeof(float2) * n));
+  MRSR_TRY(nrm.alloc(sizeof(double) * 2));
+  const unsigned nb = vec_blocks(n);
+  MRSR_CHECK_CUDA(cudaMemsetAsync(xx, 0, sizeof(float2) * n, st));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(nrm.p, 0, sizeof(double) * 2, st));
+  k_norm2<<<nb, kCgThreads, 0, st>>>(bb, n, nrm.as<double>());
+  MRSR_LAUNCH_CHECK();
+  double hn[2];
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(hn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  const double bnorm = std::sqrt(hn[0]);
+  double relres = bnorm > 0 ? 1.0 : 0.0;
+  int outer = 0;
+  k_copy<<<nb, kCgThreads, 0, st>>>(bb, r.as<float2>(), n);
+  MRSR_LAUNCH_CHECK();
+  while (outer < max_outer && relres > tol) {
+    int it = 0;
+    double rr = 0;
+    MRSR_TRY(cg_run(op_lo, op_lo->cg, r.as<float2>(), d.as<float2>(), inner_iters, 0.0, 0.0, st, &it, &rr));
+    k_axpy<<<nb, kCgThreads, 0, st>>>(xx, d.as<float2>(), n);
+    MRSR_LAUNCH_CHECK();
+    // r = b - A_hi x
+    k_copy<<<nb, kCgThreads, 0, st>>>(bb, r.as<float2>(), n);
+    MRSR_LAUNCH_CHECK();
+    MRSR_TRY(normalop_apply_internal(op_hi, xx, r.as<float2>(), make_float2(-1.f, 0.f), make_float2(1.f, 0.f), st));
+    MRSR_CHECK_CUDA(cudaMemsetAsync(nrm.p, 0, sizeof(double), st));
+    k_norm2<<<nb, kCgThreads, 0, st>>>(r.as<float2>(), n, nrm.as<double>());
+    MRSR_LAUNCH_CHECK();
+    MRSR_CHECK_CUDA(cudaMemcpyAsync(hn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+    relres = std::sqrt(hn[0]) / bnorm;
+    ++outer;
+  }
+  if (outer_out) *outer_out = outer;
+  if (relres_out) *relres_out = relres;
+  return MRSR_OK;
+}

@@ -1,0 +1,23 @@
+// Conjugate-gradient workspace and driver (cg.cu).
+#pragma once
+#include "common.cuh"
+
+struct mrsr_normalop;
+
+namespace mrsr {
+
+struct CgWork {
+  int64_t n = 0;
+  DevBuf r, u, c;   // residual, direction, A*direction
+  DevBuf state;     // device CgState (float64 scalars, iteration count, done flag)
+  DevBuf partial;   // per-block float64 partial sums
+  int ensure(int64_t n);
+};
+
+// y <- beta y + alpha A x on the operator's stream-ordered passes (normalop.cu)
+int normalop_apply_internal(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st);
+
+int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter, double reltol, double abstol,
+           cudaStream_t st, int* iters, double* res);
+
+}  // namespace mrsr

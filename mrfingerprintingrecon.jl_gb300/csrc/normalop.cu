@@ -519,6 +519,10 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
   return MRSR_OK;
 }
 
+int normalop_apply_internal(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st) {
+  return apply_impl(op, x, y, alpha, beta, st, Recorder{});
+}
+
 // ---------------------------------------------------------- builders ---
 
 static int64_t env_int(const char* name, int64_t dflt) {
@@ -548,7 +552,7 @@ int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_
   for (int i = 0; i < ndims; ++i) {
     int rad[kMaxStages], ns;
     MRSR_REQUIRE(build_radices((int)g.g[i], rad, &ns), MRSR_ERR_ARG,
-                 "img_shape_os has to be composed of the prime factors 2, 3, and 5 (dimension %d has %lld)", i + 1,
+                 "AssertionError: img_shape_os has to be composed of the prime factors 2, 3, and 5 (dimension %d has %lld)", i + 1,
                  (long long)g.g[i]);
     MRSR_TRY(op->plan[i].init((int)g.g[i]));
   }
@@ -761,11 +765,42 @@ extern "C" int mrsr_normalop_get_kmask(const mrsr_normalop* op, int64_t* out, mr
   return MRSR_OK;
 }
 
+// packed upper triangle (P, nk) -> full (K, K, nk) complex (FFTNormalOp's Λ layout)
+__global__ void k_unpack_full(const void* packed, int real, int K, int64_t nk, float2* out) {
+  const int P = K * (K + 1) / 2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nk; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int k2 = 0; k2 < K; ++k2)
+      for (int k1 = 0; k1 < K; ++k1) {
+        const int a = k1 <= k2 ? k1 : k2, b = k1 <= k2 ? k2 : k1;
+        const int p = a + b * (b + 1) / 2;
+        float2 v = real ? make_float2(reinterpret_cast<const float*>(packed)[p + (int64_t)P * i], 0.f)
+                        : reinterpret_cast<const float2*>(packed)[p + (int64_t)P * i];
+        if (k1 > k2) v.y = -v.y;
+        out[k1 + (int64_t)K * (k2 + (int64_t)K * i)] = v;
+      }
+  }
+}
+
 extern "C" int mrsr_normalop_get_lambda(const mrsr_normalop* op, void* out, mrsr_stream_t stream) {
   MRSR_REQUIRE(op && out, MRSR_ERR_ARG, "NULL argument");
   cudaStream_t st = as_stream(stream);
   LamLayout l = lam_layout(op);
   const unsigned blocks = (unsigned)std::min<int64_t>(cdiv(op->nk, 256), 65535);
+  if (op->kind == MRSR_KIND_FFT && op->lam_mode != LAM_FULL_CPLX) {
+    const int real = op->lam_mode == LAM_PACKED_REAL;
+    DevBuf packed;
+    MRSR_TRY(packed.alloc((real ? 4 : 8) * (size_t)op->P * op->nk));
+    if (real)
+      k_lam_to_packed<float><<<blocks, 256, 0, st>>>(l, op->lam.as<float>(), op->kmask.as<int64_t>(), op->nk,
+                                                     packed.as<float>());
+    else
+      k_lam_to_packed<float2><<<blocks, 256, 0, st>>>(l, op->lam.as<float2>(), op->kmask.as<int64_t>(), op->nk,
+                                                      packed.as<float2>());
+    k_unpack_full<<<blocks, 256, 0, st>>>(packed.p, real, op->geo.K, op->nk, reinterpret_cast<float2*>(out));
+    MRSR_LAUNCH_CHECK();
+    MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+    return MRSR_OK;
+  }
   if (op->lam_mode == LAM_PACKED_REAL)
     k_lam_to_packed<float><<<blocks, 256, 0, st>>>(l, op->lam.as<float>(), op->kmask.as<int64_t>(), op->nk, (float*)out);
   else

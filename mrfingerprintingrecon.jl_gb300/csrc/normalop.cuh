@@ -1,5 +1,6 @@
 // Internal state of a subspace Toeplitz normal operator handle.
 #pragma once
+#include "cg.cuh"
 #include "fft.cuh"
 
 namespace mrsr {
@@ -46,6 +47,7 @@ struct mrsr_normalop {
   mrsr::DevBuf scale1, scale2;  // fp16 per-line scales
   mrsr::DevBuf errflag;         // device int
   mrsr::FftPlanHost plan[3];
+  mrsr::CgWork cg;              // CG vectors, allocated on first solve
 };
 
 namespace mrsr {

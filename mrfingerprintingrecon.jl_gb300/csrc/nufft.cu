@@ -1,0 +1,696 @@
+// NUFFT kernels and the paths built on them:
+//  * calculate_kmask_indcs / calculate_kernel_noncartesian -> NFFTNormalOp(img_shape, trj, U)
+//    (src/NFFTNormalOp.jl:106-225, ext/MRISubspaceReconCUDAExt/NFFTNormalOp.jl:75-191)
+//  * calculate_backprojection (src/BackProjection.jl:23-102, ext/.../BackProjection.jl:1-71)
+//  * the forward model of the reference tests (test/reconstruct_radial.jl:62-74)
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "normalop.cuh"
+#include "nufft.cuh"
+
+namespace mrsr {
+
+// ------------------------------------------------------------ samples ---
+
+__device__ __forceinline__ int64_t sample_lin(const SampleSet& S, int64_t i) { return S.list ? S.list[i] - 1 : i; }
+
+__global__ void k_mask_to_flags(const uint8_t* mask, int64_t n, uint8_t* flags) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    flags[i] = mask[i] ? 1 : 0;
+}
+
+int SampleList::init(int d, const float* trj, int64_t ns_pf, int64_t nt, const uint8_t* mask, cudaStream_t st) {
+  set.trj = trj;
+  set.d = d;
+  set.ns_pf = ns_pf;
+  set.nt = nt;
+  const int64_t n = ns_pf * nt;
+  if (!mask) {
+    set.list = nullptr;
+    set.n = n;
+    return MRSR_OK;
+  }
+  DevBuf flags;
+  MRSR_TRY(flags.alloc(std::max<int64_t>(n, 1)));
+  k_mask_to_flags<<<(unsigned)std::min<int64_t>(cdiv(n, 256), 65535), 256, 0, st>>>(mask, n, flags.as<uint8_t>());
+  MRSR_LAUNCH_CHECK();
+  int64_t cnt = 0;
+  MRSR_TRY(compact_nonzero(flags.as<uint8_t>(), n, list, &cnt, st));
+  set.list = list.as<int64_t>();
+  set.n = cnt;
+  return MRSR_OK;
+}
+
+// ------------------------------------------------------- ES kernel ---
+
+static double es_phi_host(double z) {
+  if (std::fabs(z) >= 1.0) return 0.0;
+  return std::exp((double)kEsBeta * (std::sqrt(1.0 - z * z) - 1.0));
+}
+
+// Gauss-Legendre nodes/weights on [-1, 1] (Newton iteration on P_n from the Chebyshev guess).
+static void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  for (int i = 0; i < (n + 1) / 2; ++i) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+    double pp = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double p1 = 1.0, p2 = 0.0;
+      for (int j = 1; j <= n; ++j) {
+        const double p3 = p2;
+        p2 = p1;
+        p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1.0);
+      const double dz = p1 / pp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-15) break;
+    }
+    x[i] = -z;
+    x[n - 1 - i] = z;
+    w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * pp * pp);
+  }
+}
+
+// psi_hat(j) = (w/2) int_{-1}^{1} phi(z) cos(pi j w z / M) dz
+int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, DevBuf& out) {
+  static std::vector<double> gx, gw;
+  if (gx.empty()) gauss_legendre(200, gx, gw);
+  std::vector<float> h(count);
+  const double hw = 0.5 * kEsWidth;
+  for (int64_t i = 0; i < count; ++i) {
+    const double j = (double)(jmin + i);
+    double s = 0.0;
+    for (size_t q = 0; q < gx.size(); ++q) s += gw[q] * es_phi_host(gx[q]) * std::cos(M_PI * j * kEsWidth * gx[q] / (double)M);
+    h[i] = (float)(1.0 / (hw * s));
+  }
+  MRSR_TRY(out.alloc(sizeof(float) * count));
+  MRSR_CHECK_CUDA(cudaMemcpy(out.p, h.data(), sizeof(float) * count, cudaMemcpyHostToDevice));
+  return MRSR_OK;
+}
+
+// Tap weights of one sample: lane i < w*d computes the weight of tap (i % w)
+// of dimension i / w; the first tap index per dimension is l0[d].
+// u = k * M is formed in float64 so the kernel argument (l - u) / (w/2) is exact
+// before rounding to float (float32 k times a non-power-of-two M is not exact).
+__device__ __forceinline__ void es_lane_weight(const float* kd, const int64_t* M, int d, int lane, float* wt_out,
+                                               int64_t* l0) {
+  const int hw = kEsWidth / 2;
+  float wt = 0.f;
+#pragma unroll
+  for (int dd = 0; dd < 3; ++dd) {
+    if (dd < d) {
+      const double u = (double)kd[dd] * (double)M[dd];
+      const int64_t l = (int64_t)ceil(u - hw);
+      l0[dd] = l;
+      if (lane / kEsWidth == dd) {
+        const int t = lane % kEsWidth;
+        const float z = (float)(((double)(l + t) - u) / hw);
+        wt = (fabsf(z) < 1.f) ? expf(kEsBeta * (sqrtf(1.f - z * z) - 1.f)) : 0.f;
+      }
+    }
+  }
+  *wt_out = wt;
+}
+
+__device__ __forceinline__ int64_t wrap(int64_t l, int64_t M) {
+  l %= M;
+  return l < 0 ? l + M : l;
+}
+
+// --------------------------------------------------------- spreading ---
+
+// one warp per kept sample; lanes cover the w^d taps
+__global__ void __launch_bounds__(256) k_spread_lambda(SpreadLambdaArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int d = a.S.d;
+  const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
+  for (int64_t n = warp; n < a.S.n; n += nwarps) {
+    const int64_t li = sample_lin(a.S, n);
+    const int64_t t = li / a.S.ns_pf;
+    float kd[3] = {0.f, 0.f, 0.f};
+    for (int dd = 0; dd < d; ++dd) kd[dd] = a.S.trj[dd + (int64_t)d * li];
+    float wt;
+    int64_t l0[3] = {0, 0, 0};
+    es_lane_weight(kd, a.M, d, lane, &wt, l0);
+    // basis values of this frame
+    float2 u[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      u[k] = make_float2(0.f, 0.f);
+      if (k < a.K) {
+        if (a.u_complex)
+          u[k] = reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k];
+        else
+          u[k].x = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
+      }
+    }
+    for (int tt = lane; tt < ntap; tt += 32) {
+      const int t1 = tt % kEsWidth, t2 = (tt / kEsWidth) % kEsWidth, t3 = tt / (kEsWidth * kEsWidth);
+      float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
+      if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
+      int64_t cell = wrap(l0[0] + t1, a.M[0]) + a.M[0] * wrap(l0[1] + t2, a.M[1]);
+      if (d == 3) cell += a.M[0] * a.M[1] * wrap(l0[2] + t3, a.M[2]);
+      int p = 0;
+#pragma unroll
+      for (int k2 = 0; k2 < 8; ++k2) {
+#pragma unroll
+        for (int k1 = 0; k1 <= k2; ++k1) {
+          if (k2 < a.K && p >= a.p0 && p < a.p0 + a.np) {
+            const float2 v = cmulc(u[k2], u[k1]);  // conj(U[t,k1]) * U[t,k2]
+            atomicAdd(&a.grid[(int64_t)(p - a.p0) * a.cells + cell], make_float2(v.x * w, v.y * w));
+          }
+          ++p;
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_spread_data(SpreadDataArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int d = a.S.d;
+  const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
+  for (int64_t n = warp; n < a.S.n; n += nwarps) {
+    const int64_t li = sample_lin(a.S, n);
+    const int64_t t = li / a.S.ns_pf;
+    float kd[3] = {0.f, 0.f, 0.f};
+    for (int dd = 0; dd < d; ++dd) kd[dd] = a.S.trj[dd + (int64_t)d * li];
+    float dcf = 1.f;
+    if (a.dcf_kind == MRSR_DCF_RADIAL_3D || a.dcf_kind == MRSR_DCF_RADIAL_2D) {
+      float s2 = 0.f;
+      for (int dd = 0; dd < d; ++dd) s2 = __fadd_rn(s2, __fmul_rn(kd[dd], kd[dd]));
+      dcf = a.dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
+    } else if (a.dcf_kind == MRSR_DCF_ARRAY) {
+      dcf = a.dcf[n];
+    }
+    float wt;
+    int64_t l0[3] = {0, 0, 0};
+    es_lane_weight(kd, a.M, d, lane, &wt, l0);
+    const int64_t ns_tot = a.S.ns_pf * a.S.nt;
+    for (int tt = lane; tt < ntap; tt += 32) {
+      const int t1 = tt % kEsWidth, t2 = (tt / kEsWidth) % kEsWidth, t3 = tt / (kEsWidth * kEsWidth);
+      float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
+      if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
+      w *= dcf;
+      int64_t cell = wrap(l0[0] + t1, a.M[0]) + a.M[0] * wrap(l0[1] + t2, a.M[1]);
+      if (d == 3) cell += a.M[0] * a.M[1] * wrap(l0[2] + t3, a.M[2]);
+      for (int c = 0; c < a.nc; ++c) {
+        const float2 y = a.data[li + ns_tot * (a.c0 + c)];
+        const int kb = a.U ? 0 : (int)t;               // U = I(nt): only coefficient t
+        const int ke = a.U ? a.K : (int)t + 1;
+        for (int k = kb; k < ke; ++k) {
+          float2 v;
+          if (!a.U) {
+            v = y;
+          } else if (a.u_complex) {
+            v = cmulc(y, reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k]);  // y * conj(U)
+          } else {
+            const float uu = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
+            v = make_float2(y.x * uu, y.y * uu);
+          }
+          atomicAdd(&a.grid[((int64_t)c * a.K + k) * a.cells + cell], make_float2(v.x * w, v.y * w));
+        }
+      }
+    }
+  }
+}
+
+static unsigned spread_blocks(int64_t n) { return (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(n * 32, 256), 1), 152 * 64); }
+
+int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
+  if (a.S.n == 0) return MRSR_OK;
+  k_spread_lambda<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+int spread_data(const SpreadDataArgs& a, cudaStream_t st) {
+  if (a.S.n == 0) return MRSR_OK;
+  k_spread_data<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+// ----------------------------------------------------------- kmask ---
+
+// Gaussian-footprint mask: cells i0-3 .. i0+4 (mod G) per dimension around
+// i0 = floor(fl32(-k * G)) for every kept sample (src/NFFTNormalOp.jl:106-118).
+__global__ void k_kmask_mark(SampleSet S, int64_t G0, int64_t G1, int64_t G2, uint8_t* flags) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int d = S.d;
+  const int ntap = d == 2 ? 64 : 512;
+  const int64_t G[3] = {G0, G1, G2};
+  for (int64_t n = warp; n < S.n; n += nwarps) {
+    const int64_t li = sample_lin(S, n);
+    int64_t i0[3] = {0, 0, 0};
+    for (int dd = 0; dd < d; ++dd) {
+      const float p = __fmul_rn(-S.trj[dd + (int64_t)d * li], (float)G[dd]);
+      i0[dd] = (int64_t)floorf(p);
+    }
+    for (int tt = lane; tt < ntap; tt += 32) {
+      const int t1 = tt % 8, t2 = (tt / 8) % 8, t3 = tt / 64;
+      int64_t cell = wrap(i0[0] - 3 + t1, G0) + G0 * wrap(i0[1] - 3 + t2, G1);
+      if (d == 3) cell += G0 * G1 * wrap(i0[2] - 3 + t3, G2);
+      flags[cell] = 1;
+    }
+  }
+}
+
+// ----------------------------------------------------- Λ precompute ---
+
+struct FoldArgs {
+  int d;
+  int64_t G[3], M[3];
+  int64_t gcells, mcells;
+  int P;
+  int real_u;
+  const float2* g;        // [P][mcells] after the inverse DFT
+  const float* ipsi[3];   // 1/psi_hat(j) for j = -G/2 .. G/2
+  float2* c;              // [P][gcells]
+};
+
+// c~[p] for the Toeplitz kernel: complex basis uses j in [-G/2, G/2) (FFT
+// order, src/NFFTNormalOp.jl:142-158); a real basis follows the real-input
+// transform + brfft of :197-214: along dim 1 only j1 in [0, G1/2] is used,
+// interior terms doubled, and Λ = Re(FFT(c~)).
+__global__ void k_lambda_fold(FoldArgs a) {
+  const int64_t total = a.gcells * a.P;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int p = (int)(e / a.gcells);
+    int64_t cell = e - (int64_t)p * a.gcells;
+    int64_t pd[3] = {0, 0, 0};
+    pd[0] = cell % a.G[0];
+    cell /= a.G[0];
+    pd[1] = cell % a.G[1];
+    pd[2] = cell / a.G[1];
+    float scale = 1.f;
+    int64_t l = 0, mul = 1;
+    bool zero = false;
+    for (int dd = 0; dd < a.d; ++dd) {
+      const int64_t Gd = a.G[dd], half = Gd / 2;
+      int64_t j;
+      if (a.real_u && dd == 0) {
+        if (pd[0] > half) {
+          zero = true;
+          j = 0;
+        } else {
+          j = pd[0];
+          if (j != 0 && j != half) scale *= 2.f;
+        }
+      } else {
+        j = pd[dd] < half ? pd[dd] : pd[dd] - Gd;
+      }
+      scale *= a.ipsi[dd][j + half];
+      l += wrap(j, a.M[dd]) * mul;
+      mul *= a.M[dd];
+    }
+    float2 v = zero ? make_float2(0.f, 0.f) : a.g[(int64_t)p * a.mcells + l];
+    a.c[e] = make_float2(v.x * scale, v.y * scale);
+  }
+}
+
+__global__ void k_lambda_gather(const float2* lam, int64_t gcells, int P, const int64_t* kmask, int64_t nk, int real_u,
+                                void* packed) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nk; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cell = kmask[i] - 1;
+    for (int p = 0; p < P; ++p) {
+      const float2 v = lam[(int64_t)p * gcells + cell];
+      if (real_u)
+        reinterpret_cast<float*>(packed)[p + (int64_t)P * i] = v.x;
+      else
+        reinterpret_cast<float2*>(packed)[p + (int64_t)P * i] = v;
+    }
+  }
+}
+
+static unsigned grid1d(int64_t n) { return (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(n, 256), 1), 65535); }
+
+// kmask + packed Λ (P, nk) for a trajectory and basis
+static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const void* U, int u_complex, int K, DevBuf& kmask,
+                          int64_t* nk_out, DevBuf& packed, cudaStream_t st) {
+  const int64_t gcells = G[0] * G[1] * (d == 3 ? G[2] : 1);
+  MRSR_REQUIRE(S.n > 0, MRSR_ERR_ARG, "AssertionError: Mask removes all samples, cannot compute kernel.");
+  // kmask
+  {
+    DevBuf flags;
+    MRSR_TRY(flags.alloc(gcells));
+    MRSR_CHECK_CUDA(cudaMemsetAsync(flags.p, 0, gcells, st));
+    k_kmask_mark<<<spread_blocks(S.n), 256, 0, st>>>(S, G[0], G[1], d == 3 ? G[2] : 1, flags.as<uint8_t>());
+    MRSR_LAUNCH_CHECK();
+    MRSR_TRY(compact_nonzero(flags.as<uint8_t>(), gcells, kmask, nk_out, st));
+  }
+  const int P = K * (K + 1) / 2;
+  int64_t M[3] = {1, 1, 1};
+  for (int i = 0; i < d; ++i) M[i] = 2 * G[i];
+  const int64_t mcells = M[0] * M[1] * M[2];
+  FftNd fM, fG;
+  MRSR_TRY(fM.init(d, M));
+  MRSR_TRY(fG.init(d, G));
+  DevBuf ipsi[3];
+  for (int i = 0; i < d; ++i) MRSR_TRY(es_inv_psi_table(M[i], -G[i] / 2, G[i] + 1, ipsi[i]));
+  // channel batches bounded to ~2 GB of upsampled grid
+  const int64_t max_bytes = 2ll << 30;
+  const int pb = (int)std::max<int64_t>(1, std::min<int64_t>(P, max_bytes / (mcells * (int64_t)sizeof(float2))));
+  DevBuf grid, cgrid;
+  MRSR_TRY(grid.alloc(sizeof(float2) * mcells * pb));
+  MRSR_TRY(cgrid.alloc(sizeof(float2) * gcells * P));
+  MRSR_TRY(packed.alloc((u_complex ? 8 : 4) * (size_t)P * std::max<int64_t>(*nk_out, 1)));
+  // channels in batches of pb: spread, inverse DFT on the upsampled grid, deconvolve and fold onto the 2x grid
+  for (int p0 = 0; p0 < P; p0 += pb) {
+    const int np = std::min(pb, P - p0);
+    MRSR_CHECK_CUDA(cudaMemsetAsync(grid.p, 0, sizeof(float2) * mcells * np, st));
+    SpreadLambdaArgs sa{S, {M[0], M[1], M[2]}, mcells, U, u_complex, K, P, p0, np, grid.as<float2>()};
+    MRSR_TRY(spread_lambda(sa, st));
+    MRSR_TRY(fM.run(grid.as<float2>(), np, +1, 1.0f, st));
+    FoldArgs fa;
+    fa.d = d;
+    for (int i = 0; i < 3; ++i) {
+      fa.G[i] = i < d ? G[i] : 1;
+      fa.M[i] = M[i];
+      fa.ipsi[i] = i < d ? ipsi[i].as<float>() : nullptr;
+    }
+    fa.gcells = gcells;
+    fa.mcells = mcells;
+    fa.P = np;
+    fa.real_u = u_complex ? 0 : 1;
+    fa.g = grid.as<float2>();
+    fa.c = cgrid.as<float2>() + (int64_t)p0 * gcells;
+    k_lambda_fold<<<grid1d(gcells * np), 256, 0, st>>>(fa);
+    MRSR_LAUNCH_CHECK();
+  }
+  MRSR_TRY(fG.run(cgrid.as<float2>(), P, -1, 1.0f, st));
+  k_lambda_gather<<<grid1d(*nk_out), 256, 0, st>>>(cgrid.as<float2>(), gcells, P, kmask.as<int64_t>(), *nk_out,
+                                                   u_complex ? 0 : 1, packed.p);
+  MRSR_LAUNCH_CHECK();
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  return MRSR_OK;
+}
+
+
+// ------------------------------------------------ backprojection fold ---
+
+struct BpFoldArgs {
+  int d;
+  int64_t N[3], M[3], nimg, mcells;
+  int K, c0, nc, ncoils;
+  const float2* g;        // [(c - c0) K + k][mcells]
+  const float* ipsi[3];   // 1/psi_hat(j), j = -N/2 ...
+  const float2* cmaps;    // (img..., ncoils) or null -> per-coil output
+  float2* out;
+};
+
+// out[r, k] += sum_c conj(S_c(r)) x_ck(r)  (src/BackProjection.jl:96), or
+// out[r, k, c] = x_ck(r) without coil maps (:54); x_ck(r) = g[(r - N/2) mod M] / psi_hat.
+__global__ void k_bp_fold(BpFoldArgs a) {
+  const int64_t total = a.nimg * a.K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e / a.nimg);
+    const int64_t r = e - (int64_t)k * a.nimg;
+    int64_t rr = r, l = 0, mul = 1;
+    float sc = 1.f;
+    for (int dd = 0; dd < a.d; ++dd) {
+      const int64_t rd = rr % a.N[dd];
+      rr /= a.N[dd];
+      const int64_t j = rd - a.N[dd] / 2;
+      sc *= a.ipsi[dd][rd];
+      l += wrap(j, a.M[dd]) * mul;
+      mul *= a.M[dd];
+    }
+    if (a.cmaps) {
+      float2 acc = make_float2(0.f, 0.f);
+      for (int c = 0; c < a.nc; ++c) {
+        const float2 v = a.g[((int64_t)c * a.K + k) * a.mcells + l];
+        acc = cadd(acc, cmulc(v, a.cmaps[r + a.nimg * (a.c0 + c)]));
+      }
+      a.out[e] = cadd(a.out[e], cscale(acc, sc));
+    } else {
+      for (int c = 0; c < a.nc; ++c) {
+        const float2 v = a.g[((int64_t)c * a.K + k) * a.mcells + l];
+        a.out[r + a.nimg * (k + (int64_t)a.K * (a.c0 + c))] = cscale(v, sc);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------ forward model ---
+
+struct FwdPlaceArgs {
+  int d;
+  int64_t N[3], M[3], nimg, mcells;
+  int K, c;
+  const float2* x;       // (img..., K)
+  const float2* cmaps;   // (img..., ncoils) or null
+  const float* ipsi[3];
+  float2* g;             // [K][mcells], zeroed
+};
+
+__global__ void k_fwd_place(FwdPlaceArgs a) {
+  const int64_t total = a.nimg * a.K;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(e / a.nimg);
+    const int64_t r = e - (int64_t)k * a.nimg;
+    int64_t rr = r, l = 0, mul = 1;
+    float sc = 1.f;
+    for (int dd = 0; dd < a.d; ++dd) {
+      const int64_t rd = rr % a.N[dd];
+      rr /= a.N[dd];
+      sc *= a.ipsi[dd][rd];
+      l += wrap(rd - a.N[dd] / 2, a.M[dd]) * mul;
+      mul *= a.M[dd];
+    }
+    float2 v = a.x[e];
+    if (a.cmaps) v = cmul(a.cmaps[r + a.nimg * a.c], v);
+    a.g[(int64_t)k * a.mcells + l] = cscale(v, sc);
+  }
+}
+
+struct InterpArgs {
+  SampleSet S;
+  int64_t M[3], mcells;
+  int K, c, u_complex;
+  const void* U;
+  const float2* g;       // [K][mcells] after the forward DFT
+  float2* data;          // (ns_pf, nt, ncoils)
+};
+
+__global__ void __launch_bounds__(256) k_interp(InterpArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int d = a.S.d;
+  const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
+  const int64_t ns_tot = a.S.ns_pf * a.S.nt;
+  for (int64_t n = warp; n < a.S.n; n += nwarps) {
+    const int64_t li = sample_lin(a.S, n);
+    const int64_t t = li / a.S.ns_pf;
+    float kd[3] = {0.f, 0.f, 0.f};
+    for (int dd = 0; dd < d; ++dd) kd[dd] = a.S.trj[dd + (int64_t)d * li];
+    float wt;
+    int64_t l0[3] = {0, 0, 0};
+    es_lane_weight(kd, a.M, d, lane, &wt, l0);
+    float2 z[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) z[k] = make_float2(0.f, 0.f);
+    for (int tt = lane; tt < ntap; tt += 32) {
+      const int t1 = tt % kEsWidth, t2 = (tt / kEsWidth) % kEsWidth, t3 = tt / (kEsWidth * kEsWidth);
+      float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
+      if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
+      int64_t cell = wrap(l0[0] + t1, a.M[0]) + a.M[0] * wrap(l0[1] + t2, a.M[1]);
+      if (d == 3) cell += a.M[0] * a.M[1] * wrap(l0[2] + t3, a.M[2]);
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (k < a.K) {
+          const float2 gv = a.g[(int64_t)k * a.mcells + cell];
+          z[k].x += w * gv.x;
+          z[k].y += w * gv.y;
+        }
+    }
+    float2 y = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k < a.K) {
+        float2 v = z[k];
+        for (int o = 16; o > 0; o >>= 1) {
+          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (a.u_complex)
+          y = cadd(y, cmul(reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k], v));
+        else
+          y = cadd(y, cscale(v, reinterpret_cast<const float*>(a.U)[t + a.S.nt * k]));
+      }
+    }
+    if (lane == 0) a.data[li + ns_tot * a.c] = y;
+  }
+}
+
+static int check_smooth(int d, const int64_t* G) {
+  for (int i = 0; i < d; ++i) {
+    int rad[kMaxStages], ns;
+    MRSR_REQUIRE(build_radices((int)G[i], rad, &ns), MRSR_ERR_ARG,
+                 "AssertionError: img_shape_os has to be composed of the prime factors 2, 3, and 5 (cf. NonuniformFFTs.jl "
+                 "documentation).");
+  }
+  return MRSR_OK;
+}
+
+}  // namespace mrsr
+
+using namespace mrsr;
+
+static cudaStream_t nstream(mrsr_stream_t s) { return reinterpret_cast<cudaStream_t>(s); }
+
+extern "C" int mrsr_nfft_normalop_create(int ndims, const int64_t* img_shape, int64_t ns_per_frame, int64_t nt,
+                                         const float* trj, const uint8_t* sample_mask, const void* U, int u_is_complex,
+                                         int K, const float* cmaps, int ncoils, int precision, mrsr_stream_t stream,
+                                         mrsr_normalop** out) {
+  MRSR_REQUIRE(out, MRSR_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  MRSR_REQUIRE(trj && U, MRSR_ERR_ARG, "trj and U must be device pointers");
+  MRSR_REQUIRE(ns_per_frame >= 1 && nt >= 1, MRSR_ERR_ARG, "empty trajectory");
+  cudaStream_t st = nstream(stream);
+  mrsr_normalop* op = new mrsr_normalop();
+  int s = op_init_geometry(op, MRSR_KIND_NFFT, ndims, img_shape, K, cmaps ? ncoils : 1, precision);
+  if (s == MRSR_OK) s = op_set_cmaps(op, cmaps, st);
+  SampleList sl;
+  DevBuf kmask, packed;
+  int64_t nk = 0;
+  if (s == MRSR_OK) s = check_smooth(ndims, op->geo.g);
+  if (s == MRSR_OK) s = sl.init(ndims, trj, ns_per_frame, nt, sample_mask, st);
+  if (s == MRSR_OK) s = compute_lambda(ndims, op->geo.g, sl.set, U, u_is_complex, K, kmask, &nk, packed, st);
+  if (s == MRSR_OK) s = op_set_lambda_packed(op, packed.p, u_is_complex, kmask.as<int64_t>(), nk, st);
+  if (s == MRSR_OK) s = op_finalize(op, st);
+  if (s != MRSR_OK) {
+    delete op;
+    return s;
+  }
+  *out = op;
+  return MRSR_OK;
+}
+
+extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t ns_per_frame, int64_t nt, int ncoils,
+                                   const float* data, const float* trj, const uint8_t* sample_mask, const void* U,
+                                   int u_is_complex, int K, const float* cmaps, int dcf_kind, const float* dcf_array,
+                                   float* out, mrsr_stream_t stream) {
+  MRSR_REQUIRE(ndims == 2 || ndims == 3, MRSR_ERR_ARG, "ndims must be 2 or 3");
+  MRSR_REQUIRE(img_shape && data && trj && out, MRSR_ERR_ARG, "NULL argument to mrsr_backprojection");
+  MRSR_REQUIRE(ncoils >= 1 && ns_per_frame >= 1 && nt >= 1, MRSR_ERR_ARG, "empty data");
+  if (!U) K = (int)nt;
+  MRSR_REQUIRE(K >= 1, MRSR_ERR_ARG, "K must be >= 1");
+  MRSR_REQUIRE(U != nullptr || K <= 1 << 20, MRSR_ERR_ARG, "too many frames for an identity basis");
+  MRSR_REQUIRE(dcf_kind >= MRSR_DCF_NONE && dcf_kind <= MRSR_DCF_ARRAY, MRSR_ERR_ARG,
+               "`density_compensation` can only be `:radial_3D`, `:radial_2D`, `:none`, or of type `AbstractArray`");
+  MRSR_REQUIRE(dcf_kind != MRSR_DCF_ARRAY || dcf_array, MRSR_ERR_ARG, "density compensation array is NULL");
+  cudaStream_t st = nstream(stream);
+  int64_t N[3] = {1, 1, 1}, M[3] = {1, 1, 1};
+  for (int i = 0; i < ndims; ++i) {
+    N[i] = img_shape[i];
+    M[i] = 2 * N[i];
+  }
+  MRSR_TRY(check_smooth(ndims, M));
+  const int64_t nimg = N[0] * N[1] * N[2], mcells = M[0] * M[1] * M[2];
+  SampleList sl;
+  MRSR_TRY(sl.init(ndims, trj, ns_per_frame, nt, sample_mask, st));
+  MRSR_REQUIRE(sl.set.n > 0, MRSR_ERR_ARG, "AssertionError: Sample mask removes all samples, cannot compute backprojection.");
+  FftNd fM;
+  MRSR_TRY(fM.init(ndims, M));
+  DevBuf ipsi[3];
+  for (int i = 0; i < ndims; ++i) MRSR_TRY(es_inv_psi_table(M[i], -(N[i] / 2), N[i], ipsi[i]));
+  const int64_t max_bytes = 2ll << 30;
+  const int64_t per_coil = (int64_t)K * mcells * (int64_t)sizeof(float2);
+  const int cc = (int)std::max<int64_t>(1, std::min<int64_t>(ncoils, max_bytes / std::max<int64_t>(per_coil, 1)));
+  DevBuf grid;
+  MRSR_TRY(grid.alloc((size_t)per_coil * cc));
+  const int64_t out_elems = nimg * K * (cmaps ? 1 : ncoils);
+  if (cmaps) MRSR_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(float2) * out_elems, st));
+  for (int c0 = 0; c0 < ncoils; c0 += cc) {
+    const int nc = std::min(cc, ncoils - c0);
+    MRSR_CHECK_CUDA(cudaMemsetAsync(grid.p, 0, (size_t)per_coil * nc, st));
+    SpreadDataArgs sa{sl.set, {M[0], M[1], M[2]}, mcells, reinterpret_cast<const float2*>(data), c0, nc, U,
+                      u_is_complex, K, dcf_kind, dcf_array, grid.as<float2>()};
+    MRSR_TRY(spread_data(sa, st));
+    MRSR_TRY(fM.run(grid.as<float2>(), (int64_t)nc * K, +1, 1.0f, st));
+    BpFoldArgs fa;
+    fa.d = ndims;
+    for (int i = 0; i < 3; ++i) {
+      fa.N[i] = N[i];
+      fa.M[i] = M[i];
+      fa.ipsi[i] = i < ndims ? ipsi[i].as<float>() : nullptr;
+    }
+    fa.nimg = nimg;
+    fa.mcells = mcells;
+    fa.K = K;
+    fa.c0 = c0;
+    fa.nc = nc;
+    fa.ncoils = ncoils;
+    fa.g = grid.as<float2>();
+    fa.cmaps = reinterpret_cast<const float2*>(cmaps);
+    fa.out = reinterpret_cast<float2*>(out);
+    k_bp_fold<<<grid1d(nimg * K), 256, 0, st>>>(fa);
+    MRSR_LAUNCH_CHECK();
+  }
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  return MRSR_OK;
+}
+
+extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t ns_per_frame, int64_t nt, int ncoils,
+                                  const float* x, const float* trj, const void* U, int u_is_complex, int K,
+                                  const float* cmaps, float* data_out, mrsr_stream_t stream) {
+  MRSR_REQUIRE(ndims == 2 || ndims == 3, MRSR_ERR_ARG, "ndims must be 2 or 3");
+  MRSR_REQUIRE(img_shape && x && trj && U && data_out, MRSR_ERR_ARG, "NULL argument to mrsr_forward_model");
+  MRSR_REQUIRE(K >= 1 && K <= 8, MRSR_ERR_UNSUPPORTED, "forward model supports 1 <= K <= 8");
+  MRSR_REQUIRE(ncoils >= 1, MRSR_ERR_ARG, "ncoils must be >= 1");
+  MRSR_REQUIRE(cmaps || ncoils == 1, MRSR_ERR_ARG, "cmaps == NULL requires ncoils == 1");
+  cudaStream_t st = nstream(stream);
+  int64_t N[3] = {1, 1, 1}, M[3] = {1, 1, 1};
+  for (int i = 0; i < ndims; ++i) {
+    N[i] = img_shape[i];
+    M[i] = 2 * N[i];
+  }
+  MRSR_TRY(check_smooth(ndims, M));
+  const int64_t nimg = N[0] * N[1] * N[2], mcells = M[0] * M[1] * M[2];
+  SampleList sl;
+  MRSR_TRY(sl.init(ndims, trj, ns_per_frame, nt, nullptr, st));
+  FftNd fM;
+  MRSR_TRY(fM.init(ndims, M));
+  DevBuf ipsi[3];
+  for (int i = 0; i < ndims; ++i) MRSR_TRY(es_inv_psi_table(M[i], -(N[i] / 2), N[i], ipsi[i]));
+  DevBuf grid;
+  MRSR_TRY(grid.alloc(sizeof(float2) * K * mcells));
+  for (int c = 0; c < ncoils; ++c) {
+    MRSR_CHECK_CUDA(cudaMemsetAsync(grid.p, 0, sizeof(float2) * K * mcells, st));
+    FwdPlaceArgs pa;
+    pa.d = ndims;
+    for (int i = 0; i < 3; ++i) {
+      pa.N[i] = N[i];
+      pa.M[i] = M[i];
+      pa.ipsi[i] = i < ndims ? ipsi[i].as<float>() : nullptr;
+    }
+    pa.nimg = nimg;
+    pa.mcells = mcells;
+    pa.K = K;
+    pa.c = c;
+    pa.x = reinterpret_cast<const float2*>(x);
+    pa.cmaps = reinterpret_cast<const float2*>(cmaps);
+    pa.g = grid.as<float2>();
+    k_fwd_place<<<grid1d(nimg * K), 256, 0, st>>>(pa);
+    MRSR_LAUNCH_CHECK();
+    MRSR_TRY(fM.run(grid.as<float2>(), K, -1, 1.0f, st));
+    InterpArgs ia{sl.set, {M[0], M[1], M[2]}, mcells, K, c, u_is_complex, U, grid.as<float2>(),
+                  reinterpret_cast<float2*>(data_out)};
+    k_interp<<<spread_blocks(sl.set.n), 256, 0, st>>>(ia);
+    MRSR_LAUNCH_CHECK();
+  }
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  return MRSR_OK;
+}

@@ -122,8 +122,9 @@ def calculate_kernel_noncartesian(img_shape_os, trj, U, sample_mask=None):
                 c = psf(G, pts, w)
                 lam = np.fft.fftn(c)
                 v = lam.ravel(order="F")[kmask - 1]
-                Lam[k1, k2] = v
+                # statement order of src/NFFTNormalOp.jl:161-162: the mirror first, so the diagonal keeps λ
                 Lam[k2, k1] = np.conj(v)
+                Lam[k1, k2] = v
     if real_u:
         Lam = Lam.real.astype(np.float64) + 0j
     return Lam, kmask

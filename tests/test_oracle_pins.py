@@ -72,8 +72,8 @@ def test_toeplitz_embedding_equals_direct_normal_operator_2d(cplx):
             w = np.conj(U[t_of, k1].astype(np.complex128)) * U[t_of, k2]
             c = onormal.psf((2 * N, 2 * N), pts, w)
             lam = np.fft.fftn(c).ravel(order="F")
-            Lfull[k1, k2] = lam
             Lfull[k2, k1] = np.conj(lam)
+            Lfull[k1, k2] = lam
     cm = [rand_c(rng, img).astype(np.complex128) for _ in range(2)]
     x = rand_c(rng, img + (K,)).astype(np.complex128)
     y = onormal.nfft_normalop_apply(x, Lfull, all_cells, img, cmaps=cm)
@@ -115,6 +115,22 @@ def test_real_and_complex_kernels_agree_on_the_operator():
     yr = onormal.nfft_normalop_apply(x, Lr, km, (N, N))
     yc = onormal.nfft_normalop_apply(x, Lc, km, (N, N))
     assert rel_l2(yr, yc) < 5e-3  # differ only through the grid-edge convention of the two PSFs
+
+
+def test_kernel_diagonal_keeps_lambda():
+    """The diagonal blocks are λ itself, not its conjugate (src/NFFTNormalOp.jl:161-162 order)."""
+    rng = np.random.default_rng(5)
+    N, K, Nt = 8, 2, 4
+    trj = _radial(N, 2, Nt)
+    U = np.linalg.svd(rand_c(rng, (Nt, K)), full_matrices=False)[0].astype(np.complex64)
+    Lam, km = onormal.calculate_kernel_noncartesian((2 * N, 2 * N), trj, U)
+    mask = np.ones(trj.shape[1:], dtype=bool)
+    pts = onormal.masked_points(trj, mask)
+    t_of = onormal.frame_of_sample(mask)
+    w = np.abs(U[t_of, 0].astype(np.complex128)) ** 2
+    lam = np.fft.fftn(onormal.psf((2 * N, 2 * N), pts, w)).ravel(order="F")[km - 1]
+    np.testing.assert_allclose(Lam[0, 0], lam, rtol=1e-12, atol=1e-9)
+    assert np.abs(lam.imag).max() > 1e-6  # the grid-edge PSF entry makes the diagonal slightly complex
 
 
 def test_packing_roundtrip():
