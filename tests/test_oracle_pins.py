@@ -139,3 +139,34 @@ def test_packing_roundtrip():
     L = rand_c(rng, (K, K, 7)).astype(np.complex128)
     L = (L + np.conj(np.transpose(L, (1, 0, 2)))) / 2
     np.testing.assert_allclose(onormal.unpack_lambda(onormal.pack_lambda(L), K), L)
+
+
+def test_cpu_baseline_apply_matches_oracle():
+    """The float32 CPU restatement timed as the baseline computes the same operator."""
+    from oracle.cpu_apply import CpuNFFTNormalOp
+    rng = np.random.default_rng(7)
+    for img in ((12, 16), (8, 6, 10)):
+        K, Nc = 3, 2
+        G = tuple(2 * n for n in img)
+        km = np.flatnonzero(rng.random(int(np.prod(G))) < 0.7) + 1
+        P = K * (K + 1) // 2
+        Lp = rand_c(rng, (P, km.size)).astype(np.complex128)
+        Lam = onormal.unpack_lambda(Lp, K)
+        cm = rand_c(rng, img + (Nc,))
+        x = rand_c(rng, img + (K,))
+        y = CpuNFFTNormalOp(img, Lam, km, cm, workers=2).apply(x)
+        ref = onormal.nfft_normalop_apply(x, Lam, km, img, cmaps=[cm[..., c] for c in range(Nc)])
+        assert rel_l2(y, ref) < 1e-5
+
+
+def test_package_trajectories_match_oracle(mr):
+    """The package's input generators reproduce the oracle restatement of src/Trajectories.jl."""
+    from importlib import import_module
+    tr = import_module("mrsr_gb300.trajectories")
+    np.testing.assert_array_equal(tr.traj_2d_radial_goldenratio(64, 2, 7), otraj.traj_2d_radial_goldenratio(64, 2, 7))
+    np.testing.assert_array_equal(tr.traj_kooshball_goldenratio(32, 3, 4, thetaRot=0.2, phiRot=0.1),
+                                  otraj.traj_kooshball_goldenratio(32, 3, 4, thetaRot=0.2, phiRot=0.1))
+    np.testing.assert_array_equal(tr.traj_cartesian(4, 3, 2, 2, T=np.int32), otraj.traj_cartesian(4, 3, 2, 2, T=np.int32))
+    g1, g2 = tr.calculate_golden_means()
+    o1, o2 = otraj.calculate_golden_means()
+    assert abs(g1 - o1) < 1e-14 and abs(g2 - o2) < 1e-14
