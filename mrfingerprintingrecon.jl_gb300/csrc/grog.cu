@@ -109,8 +109,13 @@ __device__ void gj_solve(double2* M, double2* R, int n, int* piv_s) {
       __syncthreads();
     }
     const double2 pivot = M[k + n * k];
-    // row k scaled
     __syncthreads();
+    if (zabs2(pivot) < 1e-280) {  // exactly singular column: basic solution with x_k = 0
+      for (int c = threadIdx.x; c < n; c += blockDim.x) R[k + n * c] = make_double2(0.0, 0.0);
+      __syncthreads();
+      continue;
+    }
+    // row k scaled
     for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) {
       double2* col = c < n ? M + n * c : R + n * (c - n);
       col[k] = zdiv(col[k], pivot);

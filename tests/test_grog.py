@@ -18,16 +18,21 @@ def _grog_data(N=16, Ncyc=3, Nt=40, Nc=8, seed=0):
     Nr = 2 * N
     trj = otraj.traj_2d_radial_goldenratio(Nr, Ncyc, Nt)
     g = np.meshgrid(np.linspace(-1, 1, N), np.linspace(-1, 1, N), indexing="ij")
-    x = ((g[0] ** 2 + 1.5 * g[1] ** 2) < 0.6).astype(float) + 0.5 * ((g[0] - 0.2) ** 2 + g[1] ** 2 < 0.05)
+    # asymmetric object and jittered coil positions: symmetric data makes the spoke Gram matrices singular
+    x = ((g[0] ** 2 + 1.5 * g[1] ** 2) < 0.6).astype(float) + 0.5 * ((g[0] - 0.2) ** 2 + (g[1] - 0.3) ** 2 < 0.05)
+    x = x * (1.0 + 0.3 * g[0] + 0.2 * g[1] ** 2)
     maps = []
     for c in range(Nc):
-        a = 2 * np.pi * c / Nc
+        a = 2 * np.pi * c / Nc + rng.uniform(-0.2, 0.2)
         maps.append(np.exp(-((g[0] - 1.2 * np.cos(a)) ** 2 + (g[1] - 1.2 * np.sin(a)) ** 2) / 1.5)
                     * np.exp(1j * np.pi * 0.2 * (g[0] * np.cos(a) + g[1] * np.sin(a))))
     maps = np.stack(maps, -1)
     maps /= np.sqrt(np.sum(np.abs(maps) ** 2, -1, keepdims=True))
     pts = trj.reshape(2, -1, order="F").astype(np.float64)
     data = np.stack([nudft.forward(maps[..., c] * x, pts).reshape(trj.shape[1:], order="F") for c in range(Nc)], -1)
+    # 1% complex Gaussian noise, as in the synthetic benchmark data
+    sigma = 0.01 * np.sqrt(np.mean(np.abs(data) ** 2))
+    data = data + sigma * (rng.standard_normal(data.shape) + 1j * rng.standard_normal(data.shape)) / np.sqrt(2)
     return trj, data.astype(np.complex64), Nr, (N, N), maps.astype(np.complex64), x
 
 
