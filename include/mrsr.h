@@ -207,6 +207,20 @@ int mrsr_grog_gridding(int ndims, const int64_t* img_shape, int64_t nr, int64_t 
 int mrsr_cg(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
             int* iters_out, double* resnorm_out, mrsr_stream_t stream);
 
+/* CG as mrsr_cg, without any device allocation (no counterpart in the
+ * reference).  For callers that cannot let the library call cudaMalloc: a host
+ * framework that hands out all device memory through its own pool, or a loop
+ * that must not allocate after start-up.  The three work vectors live in a
+ * static 32 MiB device array compiled into the library, so the solve is
+ * limited to about 1.39 million unknowns (nimg * K); larger operators are
+ * rejected with MRSR_ERR_UNSUPPORTED.  The first call on each device looks up
+ * the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  The operator itself must already exist. */
+int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
+                    int* iters_out, double* resnorm_out, mrsr_stream_t stream);
+
 /* Mixed-precision iterative refinement (no counterpart in the reference):
  * outer residual r = b - A_hi x with the float32 operator, inner CG on the
  * fp16-storage operator op_lo, until ||r|| <= tol*||b|| or max_outer.

@@ -41,6 +41,7 @@ SIGNATURES = {
     "mrsr_grog_gridding": [i32, i64p, i64, i64, i64, i32, i32, p, p, p, p, p],
     "mrsr_cg": [p, p, p, i32, f64, f64, C.POINTER(i32), C.POINTER(f64), p],
     "mrsr_cg_refined": [p, p, p, p, i32, i32, f64, C.POINTER(i32), C.POINTER(f64), p],
+    "mrsr_cg_noalloc": [p, p, p, i32, f64, f64, C.POINTER(i32), C.POINTER(f64), p],
 }
 _VOID = {"mrsr_normalop_destroy"}
 _STR = {"mrsr_last_error"}

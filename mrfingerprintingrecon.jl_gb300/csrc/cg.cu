@@ -9,6 +9,7 @@
 // after convergence no-ops, so the host launches without synchronising.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "cg.cuh"
 #include "normalop.cuh"
@@ -290,3 +291,100 @@ extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const
   if (relres_out) *relres_out = relres;
   return MRSR_OK;
 }
+
+// ---------------------------------------------------------------------------
+// CG without device allocation.
+//
+// mrsr_cg allocates its three work vectors with cudaMalloc on the first solve
+// of an operator.  Some callers cannot allow that: a host framework that
+// reserves device memory up front through its own pool (Julia's CUDA.jl, a
+// serving process with a fixed memory budget) or a latency-critical loop that
+// forbids allocation after start-up.  mrsr_cg_noalloc runs the same kernels
+// with its work vectors in one statically sized device array that is part of
+// this library: every GPU that loads the library holds kNoAllocScratchBytes
+// (32 MiB) for as long as the process lives, and nothing is allocated per call.
+// ---------------------------------------------------------------------------
+namespace mrsr {
+
+constexpr size_t kNoAllocScratchBytes = 32u << 20;
+static __device__ __align__(256) unsigned char g_cg_scratch[kNoAllocScratchBytes];
+
+static size_t noalloc_align(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Device address of g_cg_scratch on the current device.  In host code the
+// symbol is only a host-side stand-in, never a device pointer, so the address
+// is looked up once per device (with that device current) and cached.
+static int noalloc_scratch(unsigned char** out) {
+  static std::mutex mu;
+  static unsigned char* addr[64] = {nullptr};
+  int dev = 0;
+  MRSR_CHECK_CUDA(cudaGetDevice(&dev));
+  MRSR_REQUIRE(dev >= 0 && dev < 64, MRSR_ERR_DEVICE, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    MRSR_CHECK_CUDA(cudaGetSymbolAddress(&p, g_cg_scratch));
+    addr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = addr[dev];
+  return MRSR_OK;
+}
+
+}  // namespace mrsr
+
+extern "C" int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
+                               int* iters_out, double* resnorm_out, mrsr_stream_t stream) {
+  using namespace mrsr;
+  MRSR_REQUIRE(op && b && x, MRSR_ERR_ARG, "NULL argument to mrsr_cg_noalloc");
+  MRSR_REQUIRE((const void*)b != (const void*)x, MRSR_ERR_ARG, "b and x must not alias");
+  MRSR_REQUIRE(maxiter >= 0, MRSR_ERR_ARG, "maxiter must be >= 0");
+  const int64_t n = op->geo.nimg() * op->geo.K;
+  const size_t off_part = noalloc_align(sizeof(CgState));
+  const size_t off_r = noalloc_align(off_part + sizeof(double2) * kCgBlocks);
+  const size_t vec = noalloc_align(sizeof(float2) * (size_t)n);
+  const size_t need = off_r + 3 * vec;
+  MRSR_REQUIRE(need <= kNoAllocScratchBytes, MRSR_ERR_UNSUPPORTED,
+               "mrsr_cg_noalloc: the problem needs %zu bytes of work space but the static scratch holds %zu "
+               "(at most %lld unknowns); use mrsr_cg",
+               need, kNoAllocScratchBytes, (long long)((kNoAllocScratchBytes - off_r) / (3 * sizeof(float2))));
+  unsigned char* base = nullptr;
+  MRSR_TRY(noalloc_scratch(&base));
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  CgState* s = reinterpret_cast<CgState*>(base);
+  double2* part = reinterpret_cast<double2*>(base + off_part);
+  float2* r = reinterpret_cast<float2*>(base + off_r);
+  float2* u = reinterpret_cast<float2*>(base + off_r + vec);
+  float2* c = reinterpret_cast<float2*>(base + off_r + 2 * vec);
+  // the scratch keeps the previous call's contents: the reduction ticket must start at zero
+  MRSR_CHECK_CUDA(cudaMemsetAsync(s, 0, sizeof(CgState), st));
+  const float2* bb = reinterpret_cast<const float2*>(b);
+  float2* xx = reinterpret_cast<float2*>(x);
+  const unsigned nb = vec_blocks(n);
+  k_cg_init<<<nb, kCgThreads, 0, st>>>(bb, xx, r, u, n, reltol, abstol, maxiter, s, part);
+  MRSR_LAUNCH_CHECK();
+  const int chunk = 8;
+  CgState h;
+  for (int it0 = 0; it0 < maxiter; it0 += chunk) {
+    const int nit = std::min(chunk, maxiter - it0);
+    for (int k = 0; k < nit; ++k) {
+      k_cg_dir<<<nb, kCgThreads, 0, st>>>(r, u, n, s);
+      MRSR_LAUNCH_CHECK();
+      MRSR_TRY(normalop_apply_internal(op, u, c, make_float2(1.f, 0.f), make_float2(0.f, 0.f), st));
+      k_cg_alpha<<<nb, kCgThreads, 0, st>>>(u, c, n, s, part);
+      MRSR_LAUNCH_CHECK();
+      k_cg_update<<<nb, kCgThreads, 0, st>>>(xx, r, u, c, n, s, part);
+      MRSR_LAUNCH_CHECK();
+    }
+    if (it0 + nit < maxiter) {
+      MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+      MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+      if (h.done) break;
+    }
+  }
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (iters_out) *iters_out = h.it;
+  if (resnorm_out) *resnorm_out = h.res;
+  return MRSR_OK;
+}
+

@@ -1,0 +1,65 @@
+"""mrsr_cg_noalloc: the CG solve for callers that cannot let the library allocate.
+
+Such callers (a Julia session whose CUDA.jl pool owns the device memory, a
+serving loop that must not allocate after start-up) use this entry point; it
+keeps its work vectors in a static device array of the library instead of
+cudaMalloc'd buffers.  Its results must equal those of mrsr_cg, the regular
+entry point, call after call: the shared array keeps the previous call's
+contents, so a second solve in a row checks that nothing stale leaks in.
+Everything goes through the C ABI with ctypes.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import normalop as onormal
+from oracle import trajectories as otraj
+from tests.helpers import rand_c, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _solve(lib, entry, A, b, maxiter, reltol):
+    x = torch.zeros_like(b)
+    it = C.c_int(0)
+    rn = C.c_double(0.0)
+    st = torch.cuda.current_stream().cuda_stream
+    status = getattr(lib, entry)(A.handle, b.data_ptr(), x.data_ptr(), maxiter, reltol, 0.0, C.byref(it),
+                                 C.byref(rn), st)
+    return status, x, it.value, rn.value
+
+
+def test_cg_noalloc_matches_cg_on_consecutive_calls(mr, cuda):
+    lib = mr.library()
+    rng = np.random.default_rng(11)
+    N, K, Nc, Nt = 32, 4, 3, 10
+    trj = otraj.traj_2d_radial_goldenratio(2 * N, 3, Nt)
+    U = np.linalg.svd(rand_c(rng, (Nt, K)), full_matrices=False)[0].astype(np.complex64)
+    cm = rand_c(rng, (N, N, Nc))
+    Lam, km = onormal.calculate_kernel_noncartesian((2 * N, 2 * N), trj, U)
+    A = mr.NFFTNormalOp((N, N), onormal.pack_lambda(Lam).astype(np.complex64), km,
+                        cmaps=[cm[..., c] for c in range(Nc)])
+    for call, (maxiter, reltol) in enumerate(((15, 0.0), (40, 1e-3))):
+        b = torch.from_numpy(rand_c(rng, (N * N * K,))).cuda()
+        s_ref, x_ref, it_ref, rn_ref = _solve(lib, "mrsr_cg", A, b, maxiter, reltol)
+        s_new, x_new, it_new, rn_new = _solve(lib, "mrsr_cg_noalloc", A, b, maxiter, reltol)
+        torch.cuda.synchronize()
+        assert s_ref == 0 and s_new == 0, lib.mrsr_last_error()
+        assert it_new == it_ref
+        assert rel_l2(x_new.cpu().numpy(), x_ref.cpu().numpy()) < 1e-6, f"call {call}"
+        assert abs(rn_new - rn_ref) <= 1e-6 * max(rn_ref, 1e-30)
+
+
+def test_cg_noalloc_rejects_problems_beyond_its_scratch(mr, cuda):
+    lib = mr.library()
+    N, K = 1024, 2  # 2,097,152 unknowns > the static work array's limit
+    G = 2 * N
+    km = np.arange(1, 4097, dtype=np.int64)
+    lam = np.ones((K * (K + 1) // 2, km.size), dtype=np.float32)
+    A = mr.NFFTNormalOp((N, N), lam, km)
+    b = torch.zeros(N * N * K, dtype=torch.complex64, device="cuda")
+    status, _, _, _ = _solve(lib, "mrsr_cg_noalloc", A, b, 2, 0.0)
+    assert status == 4  # MRSR_ERR_UNSUPPORTED
+    assert b"static scratch" in lib.mrsr_last_error()
