@@ -1,0 +1,554 @@
+// Mixed-precision apply: the oversampled K-stack and the Toeplitz kernel are
+// stored in fp16 with one float32 scale per tile; all arithmetic (FFTs, the
+// K x K product, coil sums) is float32.  Same pass structure as the float32
+// four-step kernels (apply_fast.cu).  Each producing CTA writes its results to
+// shared memory, reduces the largest component magnitude of its tile, and
+// stores value / scale as half2 with scale = max / kHalfTarget; the consumer
+// multiplies by the producer tile's scale when it loads.
+//
+// Tiles (producer -> scale array):
+//   rows forward  (row block, coil)           -> s_rows[coil][row block]
+//   dim-2 forward (column tile, slice block, plane) -> s_mid[plane][slice block][column tile]   (3D)
+//   Λ pass        (column tile, coil)         -> s_lam[coil][tile]
+//   dim-2 inverse (column tile, slice block, plane) -> s_mid2[...]                             (3D)
+#include <algorithm>
+
+#include "fft4.cuh"
+#include "passes.cuh"
+
+namespace mrsr {
+
+constexpr float kHalfTarget = 30000.f;  // largest stored magnitude (< 65504)
+
+__device__ __forceinline__ float2 ld_h(const __half2* p, int64_t i, float s) {
+  const float2 v = __half22float2(p[i]);
+  return make_float2(v.x * s, v.y * s);
+}
+
+__device__ __forceinline__ float amax2(float2 v) { return fmaxf(fabsf(v.x), fabsf(v.y)); }
+
+// block-wide max of per-thread maxima; every thread of the block calls it.
+// Non-negative floats order like their bit patterns read as unsigned.
+__device__ __forceinline__ void block_max_commit(float* m, float local) {
+  const unsigned u = __reduce_max_sync(0xffffffffu, __float_as_uint(local));
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned*>(m), u);
+}
+
+__device__ __forceinline__ float scale_of(float mx) { return mx > 0.f ? mx / kHalfTarget : 1.f; }
+
+struct HalfTiles {
+  int rpc;           // rows per CTA of the row passes
+  int64_t nrowblk;   // row blocks per plane group
+  int TCm, NOo;      // dim-2 pass tiling (3D)
+  int64_t nslab, nmtile;
+  float* s_rows;     // [coil][row block]
+  float* s_mid;      // [plane][slab][column tile]
+  float* s_lam;      // [coil][tile]
+  float* s_mid2;     // [plane][slab][column tile]
+};
+
+struct HalfArgs {
+  FftPlan pl;
+  // geometry
+  int d, K, n1;
+  int64_t nrows;     // n2 * n3
+  int64_t g1, g2, n2, n3;
+  int c0, ncg;
+  // Λ pass
+  int TC, P, lam_mode, FC, NCH;
+  int64_t inner, ntiles;
+  int nlast, glast;
+  const void* lam;   // half / half2 chunked layout
+  const float* lam_scale;  // [tile]
+  // data
+  const float2* x;
+  const float2* cmaps;
+  float2* y;
+  float2 alpha, beta;
+  int first;
+  __half2* st1;      // rows output / Λ-pass (2D) stack
+  __half2* st2;      // 3D dim-2 stack
+  HalfTiles t;
+};
+
+// ------------------------------------------------------------ rows forward ---
+template <class SP>
+__global__ void __launch_bounds__(512) kh_rows_fwd(HalfArgs a, Slots sl) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* sm = smem + L;
+  __shared__ float smax;
+  load_twiddles(tw, a.pl);
+  if (threadIdx.x == 0) smax = 0.f;
+  const int cl = blockIdx.y, c = a.c0 + cl;
+  const int64_t rb = blockIdx.x;
+  const int64_t row0 = rb * a.t.rpc;
+  const int nr = (int)min((int64_t)a.t.rpc, a.nrows - row0);
+  const int NO = a.t.rpc * a.K;
+  const int nload = (a.n1 * 2 == L) ? R1 / 2 : R1;
+  __syncthreads();
+  step_a<SP, -1>(sm, sl, NO, tw, nload, [&](int lo, int, int n) -> float2 {
+    const int rl = lo / a.K, k = lo - rl * a.K;
+    if (rl >= nr || n >= a.n1) return make_float2(0.f, 0.f);
+    const int64_t r = row0 + rl;
+    float2 v = a.x[n + (int64_t)a.n1 * (r + a.nrows * k)];
+    if (a.cmaps) v = cmul(a.cmaps[n + (int64_t)a.n1 * (r + a.nrows * c)], v);
+    return v;
+  });
+  __syncthreads();
+  float lmax = 0.f;
+  step_b<SP, -1>(sm, sl, NO, R2, [&](int lo, int li, int f1, int f2, float2 v) {
+    sm[sl.at(lo, f1, f2, li, R1)] = v;
+    lmax = fmaxf(lmax, amax2(v));
+  });
+  block_max_commit(&smax, lmax);
+  __syncthreads();
+  const float s = scale_of(smax), inv = 1.f / s;
+  if (threadIdx.x == 0) a.t.s_rows[(int64_t)cl * a.t.nrowblk + rb] = s;
+  for (int e = threadIdx.x; e < nr * a.K * L; e += blockDim.x) {
+    const int lo = e / L, f = e - lo * L;
+    const int rl = lo / a.K, k = lo - rl * a.K;
+    const float2 v = sm[sl.at(lo, f % R1, f / R1, 0, R1)];
+    a.st1[(((int64_t)cl * a.K + k) * a.nrows + row0 + rl) * L + f] = __floats2half2_rn(v.x * inv, v.y * inv);
+  }
+}
+
+// ---------------------------------------------------------- dim-2 passes ---
+// forward: st1 (g1, n2, n3) -> st2 (g1, g2, n3);  inverse: st2 -> st1
+template <class SP, int S>
+__global__ void __launch_bounds__(512) kh_mid(HalfArgs a, Slots sl) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* sm = smem + L;
+  __shared__ float smax;
+  load_twiddles(tw, a.pl);
+  if (threadIdx.x == 0) smax = 0.f;
+  const int TC = a.t.TCm;
+  const int64_t ct = blockIdx.x, ob = blockIdx.y, p = blockIdx.z;  // column tile, slab, plane (cl K + k)
+  const int64_t col0 = ct * TC, o0 = ob * a.t.NOo;
+  const int no = (int)min((int64_t)a.t.NOo, a.n3 - o0);
+  const int cl = (int)(p / a.K), k = (int)(p - (int64_t)cl * a.K);
+  const int nin = S < 0 ? (int)a.n2 : L, nout = S < 0 ? L : (int)a.n2;
+  const __half2* ib = (S < 0 ? a.st1 : a.st2) + (p * a.n3 + o0) * nin * a.g1 + col0;
+  __half2* ob_ = (S < 0 ? a.st2 : a.st1) + (p * a.n3 + o0) * nout * a.g1 + col0;
+  const int nload = (nin * 2 == L) ? R1 / 2 : R1;
+  const int nkeep = (nout * 2 == L) ? R2 / 2 : R2;
+  __syncthreads();
+  step_a<SP, S>(sm, sl, a.t.NOo, tw, nload, [&](int o, int li, int n) -> float2 {
+    if (o >= no || n >= nin) return make_float2(0.f, 0.f);
+    float s;
+    if (S < 0) {  // producer: rows forward, row r = n + n2 (o0 + o)
+      const int64_t r = n + a.n2 * (o0 + o);
+      s = a.t.s_rows[(int64_t)cl * a.t.nrowblk + r / a.t.rpc];
+    } else {      // producer: Λ pass, inner = (col0 + li) + g1 * n
+      const int64_t inner = col0 + li + a.g1 * n;
+      s = a.t.s_lam[(int64_t)cl * a.ntiles + inner / a.TC];
+    }
+    return ld_h(ib, ((int64_t)o * nin + n) * a.g1 + li, s);
+  });
+  __syncthreads();
+  float lmax = 0.f;
+  step_b<SP, S>(sm, sl, a.t.NOo, nkeep, [&](int o, int li, int f1, int f2, float2 v) {
+    sm[sl.at(o, f1, f2, li, R1)] = v;
+    if (o < no) lmax = fmaxf(lmax, amax2(v));
+  });
+  block_max_commit(&smax, lmax);
+  __syncthreads();
+  const float s = scale_of(smax), inv = 1.f / s;
+  float* sarr = S < 0 ? a.t.s_mid : a.t.s_mid2;
+  if (threadIdx.x == 0) sarr[(p * a.t.nslab + ob) * a.t.nmtile + ct] = s;
+  for (int e = threadIdx.x; e < no * nout * TC; e += blockDim.x) {
+    const int li = e % TC;
+    const int t = e / TC;
+    const int n = t % nout, o = t / nout;
+    const float2 v = sm[sl.at(o, n % R1, n / R1, li, R1)];
+    ob_[((int64_t)o * nout + n) * a.g1 + li] = __floats2half2_rn(v.x * inv, v.y * inv);
+  }
+  (void)k;
+}
+
+// ------------------------------------------------------------- Λ pass ---
+template <int KM>
+__device__ __forceinline__ void lam_apply_half(int mode, int K, const void* lamv, int64_t lbase, int64_t pstride,
+                                               float ls, const float2* X, float2* Y) {
+#pragma unroll
+  for (int j = 0; j < KM; ++j) Y[j] = make_float2(0.f, 0.f);
+  if (mode == LAM_PACKED_REAL) {
+    const __half* lam = reinterpret_cast<const __half*>(lamv) + lbase;
+    int p = 0;
+#pragma unroll
+    for (int k2 = 0; k2 < KM; ++k2) {
+#pragma unroll
+      for (int k1 = 0; k1 <= k2; ++k1) {
+        if (k2 < K) {
+          const float l = __half2float(lam[p * pstride]) * ls;
+          Y[k1].x += l * X[k2].x;
+          Y[k1].y += l * X[k2].y;
+          if (k1 != k2) {
+            Y[k2].x += l * X[k1].x;
+            Y[k2].y += l * X[k1].y;
+          }
+        }
+        ++p;
+      }
+    }
+  } else if (mode == LAM_PACKED_CPLX) {
+    const __half2* lam = reinterpret_cast<const __half2*>(lamv) + lbase;
+    int p = 0;
+#pragma unroll
+    for (int k2 = 0; k2 < KM; ++k2) {
+#pragma unroll
+      for (int k1 = 0; k1 <= k2; ++k1) {
+        if (k2 < K) {
+          const float2 l = cscale(__half22float2(lam[p * pstride]), ls);
+          Y[k1] = cadd(Y[k1], cmul(l, X[k2]));
+          if (k1 != k2) Y[k2] = cadd(Y[k2], cmul(cconj(l), X[k1]));
+        }
+        ++p;
+      }
+    }
+  } else {
+    const __half2* lam = reinterpret_cast<const __half2*>(lamv) + lbase;
+#pragma unroll
+    for (int k2 = 0; k2 < KM; ++k2) {
+#pragma unroll
+      for (int k1 = 0; k1 < KM; ++k1) {
+        if (k1 < K && k2 < K) {
+          const float2 l = cscale(__half22float2(lam[(k1 + K * k2) * pstride]), ls);
+          Y[k1] = cadd(Y[k1], cmul(l, X[k2]));
+        }
+      }
+    }
+  }
+}
+
+template <class SP>
+__global__ void __launch_bounds__(256, 2) kh_lambda(HalfArgs a, Slots sl) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* sm = smem + L;
+  __shared__ float smax;
+  load_twiddles(tw, a.pl);
+  if (threadIdx.x == 0) smax = 0.f;
+  const int cl = blockIdx.y;
+  const int64_t tile = blockIdx.x;
+  const int64_t plane = (int64_t)a.nlast * a.inner;
+  __half2* stack = a.d == 2 ? a.st1 : a.st2;
+  __half2* base = stack + (int64_t)cl * a.K * plane + tile * a.TC;
+  const int nload = (a.nlast * 2 == L) ? R1 / 2 : R1;
+  const int nkeep = (a.nlast * 2 == L) ? R1 / 2 : R1;
+  __syncthreads();
+  step_a<SP, -1>(sm, sl, a.K, tw, nload, [&](int k, int li, int n) -> float2 {
+    if (n >= a.nlast) return make_float2(0.f, 0.f);
+    float s;
+    if (a.d == 2) {  // producer: rows forward, row n
+      s = a.t.s_rows[(int64_t)cl * a.t.nrowblk + n / a.t.rpc];
+    } else {         // producer: dim-2 forward, plane (cl,k), slab n / NOo, column tile f1 / TCm
+      const int64_t f1 = (tile * a.TC + li) % a.g1;
+      s = a.t.s_mid[(((int64_t)cl * a.K + k) * a.t.nslab + n / a.t.NOo) * a.t.nmtile + f1 / a.t.TCm];
+    }
+    return ld_h(base, k * plane + (int64_t)n * a.inner + li, s);
+  });
+  __syncthreads();
+  step_b<SP, -1>(sm, sl, a.K, R2, [&](int lo, int li, int f1, int f2, float2 v) { sm[sl.at(lo, f1, f2, li, R1)] = v; });
+  __syncthreads();
+  const float ls = a.lam_scale[tile];
+  for (int t = threadIdx.x; t < (L << sl.tcs); t += blockDim.x) {
+    const int li = t & (a.TC - 1);
+    const int r = t >> sl.tcs;
+    const int f1 = r % R1, f2 = r / R1;
+    const int f = f1 + R1 * f2;
+    float2 X[KMAX], Y[KMAX];
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) X[k] = (k < a.K) ? sm[sl.at(k, f1, f2, li, R1)] : make_float2(0.f, 0.f);
+    const int64_t lbase = lam_elem(tile, f, li, 0, a.TC, a.P, a.FC, a.NCH);
+    lam_apply_half<KMAX>(a.lam_mode, a.K, a.lam, lbase, (int64_t)a.FC * a.TC, ls, X, Y);
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k)
+      if (k < a.K) sm[sl.at(k, f1, f2, li, R1)] = Y[k];
+  }
+  __syncthreads();
+  inv_step_a_slots<SP>(sm, sl, a.K, tw);
+  __syncthreads();
+  float lmax = 0.f;
+  inv_step_b_slots<SP>(sm, sl, a.K, nkeep, [&](int k, int li, int n, float2 v) {
+    // output n = g1 + R2 g2 goes back into the task's own column g1 (slot row g2): no other task reads it
+    sm[sl.at(k, n / R2, n % R2, li, R1)] = v;
+    if (n < a.nlast) lmax = fmaxf(lmax, amax2(v));
+  });
+  block_max_commit(&smax, lmax);
+  __syncthreads();
+  const float s = scale_of(smax), inv = 1.f / s;
+  if (threadIdx.x == 0) a.t.s_lam[(int64_t)cl * a.ntiles + tile] = s;
+  for (int e = threadIdx.x; e < a.K * a.nlast * a.TC; e += blockDim.x) {
+    const int li = e % a.TC;
+    const int t = e / a.TC;
+    const int n = t % a.nlast, k = t / a.nlast;
+    const float2 v = sm[sl.at(k, n / R2, n % R2, li, R1)];
+    base[k * plane + (int64_t)n * a.inner + li] = __floats2half2_rn(v.x * inv, v.y * inv);
+  }
+}
+
+// ------------------------------------------------------------ rows inverse ---
+template <class SP>
+__global__ void __launch_bounds__(512) kh_rows_inv(HalfArgs a, Slots sl) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* sm = smem + L;
+  load_twiddles(tw, a.pl);
+  const int k = blockIdx.y;
+  const int64_t row0 = (int64_t)blockIdx.x * a.t.rpc;
+  const int nr = (int)min((int64_t)a.t.rpc, a.nrows - row0);
+  const int NO = a.t.rpc * a.ncg;
+  const int nkeep = (a.n1 * 2 == L) ? R2 / 2 : R2;
+  __syncthreads();
+  step_a<SP, +1>(sm, sl, NO, tw, R1, [&](int lo, int, int m) -> float2 {
+    const int rl = lo / a.ncg, cl = lo - rl * a.ncg;
+    if (rl >= nr) return make_float2(0.f, 0.f);
+    const int64_t r = row0 + rl;
+    float s;
+    if (a.d == 2) {  // producer: Λ pass, column m
+      s = a.t.s_lam[(int64_t)cl * a.ntiles + m / a.TC];
+    } else {         // producer: dim-2 inverse, plane (cl,k), slab i3 / NOo, column tile m / TCm
+      const int64_t i3 = r / a.n2;
+      s = a.t.s_mid2[(((int64_t)cl * a.K + k) * a.t.nslab + i3 / a.t.NOo) * a.t.nmtile + m / a.t.TCm];
+    }
+    return ld_h(a.st1, (((int64_t)cl * a.K + k) * a.nrows + r) * L + m, s);
+  });
+  __syncthreads();
+  step_b<SP, +1>(sm, sl, NO, nkeep, [&](int lo, int li, int f1, int f2, float2 v) { sm[sl.at(lo, f1, f2, li, R1)] = v; });
+  __syncthreads();
+  for (int e = threadIdx.x; e < nr * a.n1; e += blockDim.x) {
+    const int rl = e / a.n1, i1 = e - rl * a.n1;
+    const int f1 = i1 % R1, f2 = i1 / R1;
+    const int64_t r = row0 + rl;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int cl = 0; cl < a.ncg; ++cl) {
+      const float2 v = sm[sl.at(rl * a.ncg + cl, f1, f2, 0, R1)];
+      if (a.cmaps)
+        acc = cadd(acc, cmulc(v, a.cmaps[i1 + (int64_t)a.n1 * (r + a.nrows * (a.c0 + cl))]));
+      else
+        acc = cadd(acc, v);
+    }
+    const int64_t yi = i1 + (int64_t)a.n1 * (r + a.nrows * k);
+    float2 yv;
+    if (a.first)
+      yv = (a.beta.x == 0.f && a.beta.y == 0.f) ? make_float2(0.f, 0.f) : cmul(a.beta, a.y[yi]);
+    else
+      yv = a.y[yi];
+    a.y[yi] = cadd(yv, cmul(a.alpha, acc));
+  }
+}
+
+// ----------------------------------------------------- Λ to fp16 tiles ---
+// max |entry| over each tile of the float32 chunked Λ, then half storage
+__global__ void k_lam_tile_max(const float* lamf, int64_t per_tile, int64_t ntiles, float* scale) {
+  __shared__ float red[32];
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    float m = 0.f;
+    for (int64_t i = threadIdx.x; i < per_tile; i += blockDim.x) m = fmaxf(m, fabsf(lamf[t * per_tile + i]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float mm = 0.f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = fmaxf(mm, red[w]);
+      scale[t] = scale_of(mm);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_lam_to_half(const float* lamf, int64_t per_tile, int64_t n, const float* scale, __half* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = __float2half_rn(lamf[i] / scale[i / per_tile]);
+}
+
+// ----------------------------------------------------------- dispatch ---
+template <class F>
+static int with_split_h(int L, F f) {
+  switch (L) {
+    case 64: return f(Split<8, 8>());
+    case 128: return f(Split<8, 16>());
+    case 256: return f(Split<16, 16>());
+    case 384: return f(Split<12, 32>());
+    case 512: return f(Split<16, 32>());
+    case 768: return f(Split<24, 32>());
+    case 1024: return f(Split<32, 32>());
+    default: return MRSR_ERR_UNSUPPORTED;
+  }
+}
+
+static Slots slots_for(int R2, int TC) {
+  Slots s;
+  s.TC = TC;
+  s.tcs = 0;
+  while ((1 << s.tcs) < TC) ++s.tcs;
+  s.W = slots_width(R2, TC);
+  return s;
+}
+
+template <class K>
+static int launch_h(K k, dim3 grid, int threads, size_t smem, cudaStream_t st, const HalfArgs& a, const Slots& sl) {
+  MRSR_REQUIRE(smem <= 227 * 1024, MRSR_ERR_UNSUPPORTED, "shared memory request %zu too large", smem);
+  if (smem > 48 * 1024) MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+  k<<<grid, threads, smem, st>>>(a, sl);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+static int rthreads(int tasks) {
+  int t = ((tasks + 31) / 32) * 32;
+  return t < 128 ? 128 : (t > 512 ? 512 : t);
+}
+
+bool half_supported(const mrsr_normalop* op) {
+  for (int i = 0; i < op->geo.ndims; ++i)
+    if (!fast_length((int)op->geo.g[i])) return false;
+  return op->TC >= 1;
+}
+
+int half_lambda_convert(mrsr_normalop* op, cudaStream_t st) {
+  const int64_t per_tile = (int64_t)op->P * op->geo.glast() * op->TC * (op->lam_mode == LAM_PACKED_REAL ? 1 : 2);
+  const int64_t ntiles = op->geo.inner() / op->TC;
+  MRSR_TRY(op->lam_scale.alloc(sizeof(float) * ntiles));
+  MRSR_TRY(op->lam_half.alloc(sizeof(__half) * per_tile * ntiles));
+  const unsigned b = (unsigned)std::min<int64_t>(ntiles, 65535);
+  k_lam_tile_max<<<b, 256, 0, st>>>(op->lam.as<float>(), per_tile, ntiles, op->lam_scale.as<float>());
+  MRSR_LAUNCH_CHECK();
+  const int64_t n = per_tile * ntiles;
+  k_lam_to_half<<<(unsigned)std::min<int64_t>(cdiv(n, 256), 65535), 256, 0, st>>>(op->lam.as<float>(), per_tile, n,
+                                                                                  op->lam_scale.as<float>(),
+                                                                                  op->lam_half.as<__half>());
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+// scale-array sizes of the fp16 tiles (same formulas as the launches below)
+static HalfTiles tiles_of(const mrsr_normalop* op) {
+  const OpGeom& g = op->geo;
+  HalfTiles t{};
+  const int L1 = (int)g.g[0];
+  const int64_t nrows = g.n[1] * g.n[2];
+  t.rpc = (int)std::max<int64_t>(1, std::min<int64_t>(4096 / ((int64_t)std::max(g.K, op->Cg) * L1), nrows));
+  t.nrowblk = cdiv(nrows, t.rpc);
+  t.TCm = 8;
+  while (t.TCm > 1 && g.g[0] % t.TCm) t.TCm >>= 1;
+  t.NOo = (int)std::max<int64_t>(1, std::min<int64_t>(4096 / ((int64_t)t.TCm * g.g[1]), g.n[2]));
+  t.nslab = cdiv(g.n[2], t.NOo);
+  t.nmtile = g.g[0] / t.TCm;
+  return t;
+}
+
+int half_alloc_scales(mrsr_normalop* op) {
+  const HalfTiles t = tiles_of(op);
+  const int64_t n_rows = (int64_t)op->Cg * t.nrowblk;
+  const int64_t n_mid = op->geo.ndims == 3 ? (int64_t)op->Cg * op->geo.K * t.nslab * t.nmtile : 1;
+  const int64_t n_lam = (int64_t)op->Cg * (op->geo.inner() / op->TC);
+  MRSR_TRY(op->scale1.alloc(sizeof(float) * (n_rows + n_lam)));
+  MRSR_TRY(op->scale2.alloc(sizeof(float) * 2 * n_mid));
+  return MRSR_OK;
+}
+
+int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
+                    void (*record)(void*), void* rec_ctx) {
+  const OpGeom& g = op->geo;
+  const int K = g.K;
+  const float inv = 1.0f / (float)g.ngrid();
+  HalfArgs a{};
+  a.d = g.ndims;
+  a.K = K;
+  a.n1 = (int)g.n[0];
+  a.nrows = g.n[1] * g.n[2];
+  a.g1 = g.g[0];
+  a.g2 = g.g[1];
+  a.n2 = g.n[1];
+  a.n3 = g.n[2];
+  a.TC = op->TC;
+  a.P = op->P;
+  a.lam_mode = op->lam_mode;
+  a.FC = op->FC;
+  a.NCH = (int)(g.glast() / op->FC);
+  a.inner = g.inner();
+  a.ntiles = g.inner() / op->TC;
+  a.nlast = (int)g.nlast();
+  a.glast = (int)g.glast();
+  a.lam = op->lam_half.p;
+  a.lam_scale = op->lam_scale.as<float>();
+  a.x = x;
+  a.cmaps = op->cmaps.p ? op->cmaps.as<float2>() : nullptr;
+  a.y = y;
+  a.alpha = make_float2(alpha.x * inv, alpha.y * inv);
+  a.beta = beta;
+  a.st1 = op->stack1.as<__half2>();
+  a.st2 = op->stack2.as<__half2>();
+  a.t = tiles_of(op);
+  a.t.s_rows = op->scale1.as<float>();
+  a.t.s_lam = op->scale1.as<float>() + (int64_t)op->Cg * a.t.nrowblk;
+  const int64_t n_mid = g.ndims == 3 ? (int64_t)op->Cg * K * a.t.nslab * a.t.nmtile : 1;
+  a.t.s_mid = op->scale2.as<float>();
+  a.t.s_mid2 = op->scale2.as<float>() + n_mid;
+  const int ngroups = (int)cdiv(g.ncoils, op->Cg);
+  for (int grp = 0; grp < ngroups; ++grp) {
+    a.c0 = grp * op->Cg;
+    a.ncg = std::min(op->Cg, g.ncoils - a.c0);
+    a.first = grp == 0 ? 1 : 0;
+    // rows forward
+    a.pl = op->plan[0].plan;
+    MRSR_TRY(with_split_h(a.pl.L, [&](auto sp) -> int {
+      using SP = decltype(sp);
+      const Slots sl = slots_for(SP::R2, 1);
+      const int NO = a.t.rpc * K;
+      const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)NO * SP::R1 * sl.W);
+      return launch_h(kh_rows_fwd<SP>, dim3((unsigned)a.t.nrowblk, a.ncg), rthreads(NO * SP::R1), smem, st, a, sl);
+    }));
+    if (record) record(rec_ctx);
+    if (g.ndims == 3) {
+      a.pl = op->plan[1].plan;
+      MRSR_TRY(with_split_h(a.pl.L, [&](auto sp) -> int {
+        using SP = decltype(sp);
+        const Slots sl = slots_for(SP::R2, a.t.TCm);
+        const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)a.t.NOo * SP::R1 * sl.W);
+        dim3 grid((unsigned)a.t.nmtile, (unsigned)a.t.nslab, (unsigned)(a.ncg * K));
+        return launch_h(kh_mid<SP, -1>, grid, rthreads(a.t.NOo * a.t.TCm * SP::R1), smem, st, a, sl);
+      }));
+      if (record) record(rec_ctx);
+    }
+    a.pl = op->plan[g.ndims - 1].plan;
+    MRSR_TRY(with_split_h(a.pl.L, [&](auto sp) -> int {
+      using SP = decltype(sp);
+      const Slots sl = slots_for(SP::R2, a.TC);
+      const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)K * SP::R1 * sl.W);
+      return launch_h(kh_lambda<SP>, dim3((unsigned)a.ntiles, a.ncg), 256, smem, st, a, sl);
+    }));
+    if (record) record(rec_ctx);
+    if (g.ndims == 3) {
+      a.pl = op->plan[1].plan;
+      MRSR_TRY(with_split_h(a.pl.L, [&](auto sp) -> int {
+        using SP = decltype(sp);
+        const Slots sl = slots_for(SP::R2, a.t.TCm);
+        const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)a.t.NOo * SP::R1 * sl.W);
+        dim3 grid((unsigned)a.t.nmtile, (unsigned)a.t.nslab, (unsigned)(a.ncg * K));
+        return launch_h(kh_mid<SP, +1>, grid, rthreads(a.t.NOo * a.t.TCm * SP::R1), smem, st, a, sl);
+      }));
+      if (record) record(rec_ctx);
+    }
+    a.pl = op->plan[0].plan;
+    MRSR_TRY(with_split_h(a.pl.L, [&](auto sp) -> int {
+      using SP = decltype(sp);
+      const Slots sl = slots_for(SP::R2, 1);
+      const int NO = a.t.rpc * a.ncg;
+      const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)NO * SP::R1 * sl.W);
+      return launch_h(kh_rows_inv<SP>, dim3((unsigned)a.t.nrowblk, K), rthreads(NO * SP::R1), smem, st, a, sl);
+    }));
+    if (record) record(rec_ctx);
+  }
+  return MRSR_OK;
+}
+
+}  // namespace mrsr

@@ -432,8 +432,12 @@ static int mid_tc(const mrsr_normalop* op) {
   return TC;
 }
 
+static void record_cb(void* ctx) { static_cast<Recorder*>(ctx)->record(); }
+
 static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
                       Recorder rec) {
+  if (op->precision == MRSR_PREC_FP16)
+    return apply_half_impl(op, x, y, alpha, beta, st, rec.ev ? record_cb : nullptr, &rec);
   const OpGeom& g = op->geo;
   const int K = g.K;
   const float inv = 1.0f / (float)g.ngrid();
@@ -537,7 +541,8 @@ int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_
   MRSR_REQUIRE(img_shape != nullptr, MRSR_ERR_ARG, "img_shape is NULL");
   MRSR_REQUIRE(K >= 1 && K <= KMAX, MRSR_ERR_UNSUPPORTED, "rank K=%d outside 1..%d", K, KMAX);
   MRSR_REQUIRE(ncoils >= 1, MRSR_ERR_ARG, "ncoils must be >= 1");
-  MRSR_REQUIRE(precision == MRSR_PREC_FP32, MRSR_ERR_UNSUPPORTED, "precision %d not available", precision);
+  MRSR_REQUIRE(precision == MRSR_PREC_FP32 || precision == MRSR_PREC_FP16, MRSR_ERR_ARG, "unknown precision %d",
+               precision);
   op->kind = kind;
   op->precision = precision;
   OpGeom& g = op->geo;
@@ -580,8 +585,12 @@ int op_set_cmaps(mrsr_normalop* op, const float* cmaps, cudaStream_t st) {
 
 int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   const OpGeom& g = op->geo;
+  const bool half = op->precision == MRSR_PREC_FP16;
+  MRSR_REQUIRE(!half || half_supported(op), MRSR_ERR_UNSUPPORTED,
+               "fp16 storage needs grid lengths with a register four-step split (64, 128, 256, 384, 512, 768, 1024)");
+  const int64_t esz = half ? 4 : (int64_t)sizeof(float2);
   // coils per group: keep one group's stack near 48 MB so it can stay in L2 between passes
-  const int64_t per_coil = (int64_t)g.K * g.g[0] * g.n[1] * g.n[2] * (int64_t)sizeof(float2);
+  const int64_t per_coil = (int64_t)g.K * g.g[0] * g.n[1] * g.n[2] * esz;
   int64_t cg = env_int("MRSR_COIL_GROUP", 0);
   if (cg <= 0) {
     if (g.ndims == 2)
@@ -595,10 +604,15 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   op->Cg = (int)cg;
   MRSR_TRY(op->stack1.alloc((size_t)(per_coil * cg)));
   if (g.ndims == 3) {
-    const int64_t per_coil2 = (int64_t)g.K * g.g[0] * g.g[1] * g.n[2] * (int64_t)sizeof(float2);
+    const int64_t per_coil2 = (int64_t)g.K * g.g[0] * g.g[1] * g.n[2] * esz;
     MRSR_TRY(op->stack2.alloc((size_t)(per_coil2 * cg)));
   }
   op->launches = (int)ngroups * (g.ndims == 2 ? 3 : 5);
+  if (half) {
+    MRSR_TRY(half_lambda_convert(op, st));
+    MRSR_TRY(half_alloc_scales(op));
+    MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  }
   (void)st;
   return MRSR_OK;
 }

@@ -42,6 +42,7 @@ struct mrsr_normalop {
   mrsr::DevBuf kmask;      // int64 nk, 1-based column-major grid indices
   mrsr::DevBuf lam;        // [tile][chunk][P][FC][TC] of float / float2 (chunked along f_last)
   mrsr::DevBuf lam_scale;  // fp16: one float per tile
+  mrsr::DevBuf lam_half;   // fp16: the chunked kernel in half precision
   mrsr::DevBuf cmaps;      // (img..., ncoils) complex; empty = unit coil
   mrsr::DevBuf stack1, stack2;  // intermediates of one coil group
   mrsr::DevBuf scale1, scale2;  // fp16 per-line scales

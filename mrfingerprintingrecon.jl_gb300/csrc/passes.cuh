@@ -138,4 +138,11 @@ int fast_lambda(const LamPassArgs& a, int ncg, int planes_total, int* errword, c
 int fast_mid(const MidArgs& a, int nplanes, cudaStream_t st);
 int fast_rows_inv(const RowsInvArgs& a, int64_t nrows, cudaStream_t st);
 
+// fp16-storage operator (apply_half.cu)
+bool half_supported(const mrsr_normalop* op);
+int half_lambda_convert(mrsr_normalop* op, cudaStream_t st);
+int half_alloc_scales(mrsr_normalop* op);
+int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
+                    void (*record)(void*), void* rec_ctx);
+
 }  // namespace mrsr
