@@ -35,6 +35,7 @@ WORKLOADS = {
     "radial2d_64_nt200_nc4_k4": dict(img=(64, 64), Nr=128, Ncyc=1, Nt=200, Nc=4, K=4),
 }
 DEFAULT_WORKLOAD = "radial2d_256_nt1000_nc20_k5"
+SERVED = "served_mixed_500"
 L2_FLUSH_BYTES = 256 << 20   # > 129 MB L2
 
 
@@ -44,7 +45,12 @@ def parse_args():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SERVED])
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "refined"],
+                   help="operator storage: fp32, fp16 (per-tile scaled half stacks and kernel); "
+                        "refined (served workload only: fp16 inner CG + float32 residual steps)")
+    p.add_argument("--rate", type=float, default=40.0, help="served workload: Poisson arrival rate (requests/s)")
+    p.add_argument("--requests", type=int, default=500, help="served workload: requests in the timed stream")
     return p.parse_args()
 
 
@@ -200,6 +206,10 @@ def cpu_apply_sample(w, trj, cm, Lam=None, kmask=None, coils=2, reps=2, seed=0):
 def reference_arm(args, world, rank):
     if rank != 0:
         return
+    if args.workload == SERVED:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference package has no request server; "
+                          "its per-reconstruction CPU path is timed by the apply workloads"}), flush=True)
+        return
     w = WORKLOADS[args.workload]
     # inputs from the oracle's own restatements only (no package code on this arm)
     from oracle import normalop as onormal
@@ -239,7 +249,9 @@ def gb300_arm(args, world, rank, local):
     # operator: Toeplitz kernel precompute on the device (timed once, reported beside the headline)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    A = mr.NFFTNormalOp(w["img"], trj, U, cmaps=cm)
+    prec = "fp32" if args.precision == "fp32" else "fp16"
+    A = mr.NFFTNormalOp(w["img"], trj, U, cmaps=cm, precision=prec)
+    esz, lsz = (8, 4) if prec == "fp32" else (4, 2)   # bytes per stack element / per real kernel entry
     torch.cuda.synchronize()
     t_lambda = time.perf_counter() - t0
     x = mr.to_jl(x_h, torch.complex64)
@@ -315,11 +327,12 @@ def gb300_arm(args, world, rank, local):
     P = K * (K + 1) // 2
     cg = -(-Nc // ngroups)
     nk = A.nk
-    lam_bytes = 2.0 * cg * K * N2 * G1 * 8 + nk * P * 4          # stack in + out, Λ once
+    lam_bytes = 2.0 * cg * K * N2 * G1 * esz + nk * P * lsz      # stack in + out, Λ once
     achieved = lam_bytes / (lam_avg * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = profile_traffic("k4_lambda")
-    apply_bytes = N1 * N2 * K * 16 + 2 * Nc * N1 * N2 * 8 + 4 * Nc * (G1 * N2 * K) * 8 + nk * P * 4
+    lam_kernel = "k4_lambda" if prec == "fp32" else "kh_lambda"
+    traffic = profile_traffic(lam_kernel)
+    apply_bytes = N1 * N2 * K * 16 + 2 * Nc * N1 * N2 * 8 + 4 * Nc * (G1 * N2 * K) * esz + nk * P * lsz
     if rank != 0:
         return
     value = world * 1000.0 / ms
@@ -327,13 +340,16 @@ def gb300_arm(args, world, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded phantom, dictionary basis, coil maps)",
+        "vs_baseline": None, "dtype": "c64" if prec == "fp32" else "c64 (f16 storage)",
+        "data": "synthetic (seeded phantom, dictionary basis, coil maps)",
         "config": {"workload": args.workload, "img": list(w["img"]), "Nr": w["Nr"], "Ncyc": w["Ncyc"], "Nt": w["Nt"],
-                   "Nc": Nc, "K": K, "operator": "NFFTNormalOp float32 (real basis, packed real kernel)",
+                   "Nc": Nc, "K": K, "precision": prec,
+                   "operator": "NFFTNormalOp " + ("float32" if prec == "fp32" else "fp16 storage, float32 arithmetic")
+                   + " (real basis, packed real kernel)",
                    "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) before every timed step"},
         "e2e": {"value": world * 1000.0 / ms_e2e, "unit": "applies/s", "h2d_bytes_per_step": int(xh.numel() * 8),
                 "d2h_bytes_per_step": int(yh.numel() * 8)},
-        "roofline": {"bound": "hbm", "kernel": "Λ pass (k4_lambda: last-axis FFT + K x K kernel + inverse FFT)",
+        "roofline": {"bound": "hbm", "kernel": f"Λ pass ({lam_kernel}: last-axis FFT + K x K kernel + inverse FFT)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": f"{peak_kind} MEASURED_PEAKS hbm_gbs" if peak_kind == "measured" else "fallback",
                      "traffic": traffic, "bytes_per_launch": lam_bytes, "ms_per_launch": lam_avg},
@@ -348,11 +364,95 @@ def gb300_arm(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------- served stream ---
+def served_arm(args, world, rank, local):
+    """Mixed request stream through the continuous-batching server (one process per GPU, replicas).
+
+    8 protocols (seeded: matrix 128/192/256/384, K 3-6, Nt 300-1500, golden-angle
+    radial with 2N readout samples, rotated per seed); one 32-coil synthetic scan
+    per protocol (forward model + 1% noise) in pinned host memory; each request
+    draws a protocol and 8-32 coils and arrives by a Poisson process.  A request
+    = host-to-device copy of its data, backprojection, 20 CG iterations (graph-
+    captured, batched with queued same-protocol requests), all inside its latency.
+    """
+    import importlib
+    import torch
+    import __graft_entry__ as ge
+    mr = ge.package()
+    sv = importlib.import_module(mr.__name__ + ".serving")
+    protos = sv.make_protocols(mr, 8, seed=42 + rank)
+    scans = []
+    for i, p in enumerate(protos):
+        data, cm, _ = sv.make_scans(mr, p, 32, seed=100 + i)
+        host = torch.empty(tuple(data.shape)[::-1], dtype=torch.complex64, pin_memory=True)
+        host.copy_(data.permute(*reversed(range(data.dim()))))
+        scans.append((host.permute(*reversed(range(data.dim()))), cm))
+        del data
+    torch.cuda.synchronize()
+    budget = 64 << 30
+    iters = 20
+
+    def stream(n, rate, seed):
+        return sv.make_request_stream(protos, scans, n, rate, coil_range=(8, 32), seed=seed)
+
+    def server():
+        ex = sv.GpuExecutor(mr, iters=iters, precision=args.precision, outer=2, keep_results=False)
+        return sv.ReconServer(ex, budget, slots=4, max_batch=4)
+
+    # warm-up: every protocol once (code paths, graph instantiation), then a fresh server (cold kernel cache)
+    warm = [sv.Request(rid=i, protocol=p, data=scans[i][0][..., :8], cmaps=scans[i][1][..., :8])
+            for i, p in enumerate(protos)]
+    w = server()
+    w.run(warm)
+    w.close()
+    torch.cuda.synchronize()
+    reqs = stream(args.requests, args.rate, seed=7 + rank)
+    clocks = ClockSampler(local) if rank == 0 else None
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    barrier(world)
+    srv = server()
+    w0 = time.time()
+    st = srv.run(reqs)
+    torch.cuda.synchronize()
+    w1 = time.time()
+    barrier(world)
+    clk = clocks.summary(w0, w1) if clocks else None
+    if clocks:
+        clocks.stop()
+    srv.close()
+    wall = max_over_ranks(st.wall_s, world)
+    if rank != 0:
+        return
+    value = world * st.completed / wall
+    h2d = int(sum(r.data.numel() * 8 for r in reqs) / len(reqs))
+    line = {
+        "metric": METRIC, "value": value, "unit": "recons/s", "n_gpus": world, "steps": st.completed,
+        "warmup": len(warm), "ms_per_step": 1000.0 * wall / st.completed, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64" if args.precision == "fp32" else "c64/f16",
+        "data": "synthetic (8 seeded protocols, one 32-coil scan each, forward model + 1% noise)",
+        "config": {"workload": SERVED, "requests": st.completed, "rate_hz": args.rate, "precision": args.precision,
+                   "cg_iters": iters, "outer_steps": 2 if args.precision == "refined" else None, "slots": 4,
+                   "max_batch": 4, "hbm_budget_gb": budget / 2 ** 30,
+                   "protocols": [p.name for p in protos], "coils": [8, 32],
+                   "parallelism": f"replicas x{world}", "l2": "inputs (per-request data 7-295 MB) stream through"},
+        "latency_ms": {"p50": st.p50_ms, "p99": st.p99_ms, "mean": st.mean_ms},
+        "e2e": {"value": value, "unit": "recons/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 0,
+                "note": "request latency includes the host-to-device copy of its data"},
+        "serving": st.as_dict(),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":
         reference_arm(args, world, rank)
+    elif args.workload == SERVED:
+        served_arm(args, world, rank, local)
     else:
         gb300_arm(args, world, rank, local)
     if world > 1:

@@ -228,6 +228,41 @@ int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int maxiter, do
 int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const float* b, float* x, int inner_iters,
                     int max_outer, double tol, int* outer_out, double* relres_out, mrsr_stream_t stream);
 
+/* ---------------------------------------------------------------------
+ * Serving support (no counterpart in the reference).
+ *
+ * mrsr_normalop_share: a new operator on src's Toeplitz kernel and kmask,
+ * which it shares by reference count (not copied), with its own coil maps
+ * (cmaps (img..., ncoils) or NULL) and work stacks.  precision may differ
+ * from src's (the fp16 copy of the kernel is made once and shared too).
+ * Destroying src first is allowed.
+ */
+int mrsr_normalop_share(const mrsr_normalop* src, const float* cmaps, int ncoils, int precision,
+                        mrsr_stream_t stream, mrsr_normalop** out);
+
+/* A batch of independent fixed-iteration solves recorded once into one CUDA
+ * graph, one graph branch per entry, so that the entries overlap on the
+ * device and a launch costs one cudaGraphLaunch.
+ *   ops_hi == NULL or ops_hi[i] == NULL: entry i is cg(A, b; maxiter =
+ *     inner_iters, reltol = 0) with x0 = 0 on ops_lo[i] (the kernels of
+ *     mrsr_cg, without its tolerance test).
+ *   ops_hi[i] != NULL: mixed-precision refinement with a fixed schedule,
+ *     x = 0, r = b; outer_steps times { d = cg(ops_lo[i], r; inner_iters);
+ *     x += d; r = b - ops_hi[i] x } (ops_hi[i] float32, ops_lo[i] fp16).
+ * Pointers b[i], x[i] are baked into the graph: each launch solves again with
+ * the current contents of b[i]; x[i] is overwritten.  No operator may appear
+ * in two entries.  Relaunching before the previous launch finished is
+ * ordered only by the stream the caller passes.
+ * mrsr_cg_batch_result (synchronises): plain entries give the iterations run
+ * and the final ||r||; refined entries give outer_steps and ||r|| / ||b||. */
+typedef struct mrsr_cg_batch mrsr_cg_batch; /* opaque handle */
+int mrsr_cg_batch_create(mrsr_normalop* const* ops_lo, mrsr_normalop* const* ops_hi, const float* const* b,
+                         float* const* x, int n, int inner_iters, int outer_steps, mrsr_stream_t stream,
+                         mrsr_cg_batch** out);
+int mrsr_cg_batch_launch(mrsr_cg_batch* batch, mrsr_stream_t stream);
+int mrsr_cg_batch_result(mrsr_cg_batch* batch, int i, int* iters_out, double* resnorm_out);
+void mrsr_cg_batch_destroy(mrsr_cg_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

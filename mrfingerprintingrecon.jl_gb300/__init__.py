@@ -7,13 +7,13 @@ no CPU implementation: every call runs on the current CUDA device.
 from . import _lib
 from .normalop import NFFTNormalOp, FFTNormalOp, NormalOperator
 from .backprojection import calculate_backprojection, forward_model
-from .solvers import cg, cg_refined
+from .solvers import cg, cg_refined, CgBatch
 from .grog import grog_calib, grog_gridding, radial_grog
 from . import trajectories, synthetic
 from .arrays import jl_empty, jl_zeros, jl_reshape, to_jl, to_host
 
 __all__ = ["NFFTNormalOp", "FFTNormalOp", "NormalOperator", "calculate_backprojection", "forward_model", "cg",
-           "cg_refined", "grog_calib", "grog_gridding", "radial_grog", "trajectories", "synthetic",
+           "cg_refined", "CgBatch", "grog_calib", "grog_gridding", "radial_grog", "trajectories", "synthetic",
            "jl_empty", "jl_zeros", "jl_reshape", "to_jl", "to_host"]
 
 

@@ -207,6 +207,7 @@ extern "C" int mrsr_fft_normalop_create(int ndims, const int64_t* img_shape, int
                                         const int32_t* trj, const uint8_t* sample_mask, const void* U, int u_is_complex,
                                         int K, int nrep, const float* cmaps, int ncoils, int precision,
                                         mrsr_stream_t stream, mrsr_normalop** out) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(out, MRSR_ERR_ARG, "out is NULL");
   *out = nullptr;
   MRSR_REQUIRE(trj && U, MRSR_ERR_ARG, "trj and U must be device pointers");
@@ -239,6 +240,7 @@ extern "C" int mrsr_fft_normalop_create_from_mask(int ndims, const int64_t* img_
                                                   const void* U, int u_is_complex, int K, const float* cmaps,
                                                   int ncoils, int precision, mrsr_stream_t stream,
                                                   mrsr_normalop** out) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(out, MRSR_ERR_ARG, "out is NULL");
   *out = nullptr;
   MRSR_REQUIRE(M && U, MRSR_ERR_ARG, "M and U must be device pointers");
@@ -268,6 +270,7 @@ extern "C" int mrsr_backprojection_cartesian(int ndims, const int64_t* img_shape
                                              int ncoils, int nrep, const float* data, const int32_t* trj,
                                              const uint8_t* sample_mask, const void* U, int u_is_complex, int K,
                                              const float* cmaps, float* out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(ndims == 2 || ndims == 3, MRSR_ERR_ARG, "ndims must be 2 or 3");
   MRSR_REQUIRE(img_shape && data && trj && out, MRSR_ERR_ARG, "NULL argument");
   MRSR_REQUIRE(ncoils >= 1 && nrep >= 1, MRSR_ERR_ARG, "empty data");

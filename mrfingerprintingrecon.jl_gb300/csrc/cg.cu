@@ -166,7 +166,7 @@ int CgWork::ensure(int64_t n_) {
   MRSR_TRY(c.alloc(sizeof(float2) * n));
   MRSR_TRY(state.alloc(sizeof(CgState)));
   MRSR_TRY(partial.alloc(sizeof(double2) * kCgBlocks));
-  MRSR_CHECK_CUDA(cudaMemset(state.p, 0, sizeof(CgState)));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(state.p, 0, sizeof(CgState), call_stream()));
   return MRSR_OK;
 }
 
@@ -209,6 +209,37 @@ int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter
   return MRSR_OK;
 }
 
+int cg_fixed_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st) {
+  CgWork& w = op->cg;
+  const int64_t n = op->geo.nimg() * op->geo.K;
+  MRSR_REQUIRE(w.n == n && w.r.p, MRSR_ERR_STATE, "CG work vectors are not allocated for this operator");
+  CgState* s = w.state.as<CgState>();
+  double2* part = w.partial.as<double2>();
+  const unsigned nb = vec_blocks(n);
+  k_cg_init<<<nb, kCgThreads, 0, st>>>(b, x, w.r.as<float2>(), w.u.as<float2>(), n, 0.0, 0.0, iters, s, part);
+  MRSR_LAUNCH_CHECK();
+  for (int k = 0; k < iters; ++k) {
+    k_cg_dir<<<nb, kCgThreads, 0, st>>>(w.r.as<float2>(), w.u.as<float2>(), n, s);
+    MRSR_LAUNCH_CHECK();
+    MRSR_TRY(normalop_apply_internal(op, w.u.as<float2>(), w.c.as<float2>(), make_float2(1.f, 0.f),
+                                     make_float2(0.f, 0.f), st));
+    k_cg_alpha<<<nb, kCgThreads, 0, st>>>(w.u.as<float2>(), w.c.as<float2>(), n, s, part);
+    MRSR_LAUNCH_CHECK();
+    k_cg_update<<<nb, kCgThreads, 0, st>>>(x, w.r.as<float2>(), w.u.as<float2>(), w.c.as<float2>(), n, s, part);
+    MRSR_LAUNCH_CHECK();
+  }
+  return MRSR_OK;
+}
+
+int cg_fixed_result(mrsr_normalop* op, int* iters, double* res) {
+  MRSR_REQUIRE(op->cg.state.p, MRSR_ERR_STATE, "no CG has run on this operator");
+  CgState h;
+  MRSR_CHECK_CUDA(cudaMemcpy(&h, op->cg.state.p, sizeof(CgState), cudaMemcpyDeviceToHost));
+  if (iters) *iters = h.it;
+  if (res) *res = h.res;
+  return MRSR_OK;
+}
+
 // r = b - A x  (outer residual of the refinement, float32 operator)
 __global__ void k_copy(const float2* a, float2* b, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) b[i] = a[i];
@@ -236,19 +267,23 @@ using namespace mrsr;
 
 extern "C" int mrsr_cg(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
                        int* iters_out, double* resnorm_out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(op && b && x, MRSR_ERR_ARG, "NULL argument to mrsr_cg");
   MRSR_REQUIRE((const void*)b != (const void*)x, MRSR_ERR_ARG, "b and x must not alias");
   MRSR_REQUIRE(maxiter >= 0, MRSR_ERR_ARG, "maxiter must be >= 0");
+  OpUse use{op, reinterpret_cast<cudaStream_t>(stream)};
   return cg_run(op, op->cg, reinterpret_cast<const float2*>(b), reinterpret_cast<float2*>(x), maxiter, reltol, abstol,
                 reinterpret_cast<cudaStream_t>(stream), iters_out, resnorm_out);
 }
 
 extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const float* b, float* x, int inner_iters,
                                int max_outer, double tol, int* outer_out, double* relres_out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(op_lo && op_hi && b && x, MRSR_ERR_ARG, "NULL argument to mrsr_cg_refined");
   MRSR_REQUIRE(op_lo->geo.nimg() == op_hi->geo.nimg() && op_lo->geo.K == op_hi->geo.K, MRSR_ERR_ARG,
                "operators of different sizes");
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  OpUse use_lo{op_lo, st}, use_hi{op_hi, st};
   const int64_t n = op_hi->geo.nimg() * op_hi->geo.K;
   const float2* bb = reinterpret_cast<const float2*>(b);
   float2* xx = reinterpret_cast<float2*>(x);
@@ -334,6 +369,7 @@ static int noalloc_scratch(unsigned char** out) {
 
 extern "C" int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
                                int* iters_out, double* resnorm_out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   using namespace mrsr;
   MRSR_REQUIRE(op && b && x, MRSR_ERR_ARG, "NULL argument to mrsr_cg_noalloc");
   MRSR_REQUIRE((const void*)b != (const void*)x, MRSR_ERR_ARG, "b and x must not alias");
@@ -350,6 +386,7 @@ extern "C" int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int 
   unsigned char* base = nullptr;
   MRSR_TRY(noalloc_scratch(&base));
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  OpUse use{op, st};
   CgState* s = reinterpret_cast<CgState*>(base);
   double2* part = reinterpret_cast<double2*>(base + off_part);
   float2* r = reinterpret_cast<float2*>(base + off_r);

@@ -20,4 +20,11 @@ int normalop_apply_internal(mrsr_normalop* op, const float2* x, float2* y, float
 int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter, double reltol, double abstol,
            cudaStream_t st, int* iters, double* res);
 
+// `iters` CG iterations with no tolerance test and no host synchronisation,
+// so the sequence can be recorded into a CUDA graph; op->cg must already be
+// sized (CgWork::ensure).  cg_fixed_result reads the iteration count and
+// residual norm after the stream has finished.
+int cg_fixed_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st);
+int cg_fixed_result(mrsr_normalop* op, int* iters, double* res);
+
 }  // namespace mrsr

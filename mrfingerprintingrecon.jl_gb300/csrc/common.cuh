@@ -45,8 +45,32 @@ struct Status {
 // Launch-error check right after a <<<>>> launch.
 #define MRSR_LAUNCH_CHECK() MRSR_CHECK_CUDA(cudaGetLastError())
 
+// ------------------------------------------------------ stream scopes ---
+// Every entry point that takes a stream opens a CallScope on it.  Device
+// memory comes from the stream-ordered pool (cudaMallocAsync) on the call's
+// stream, so the library never calls cudaMalloc / cudaFree, which would
+// synchronise the whole device and stall other streams' work.  A buffer is
+// freed on the library's private stream after that stream has waited for the
+// work that may still use it: the running call's stream (temporaries) or the
+// owning operator's last use (see mrsr_normalop).
+cudaStream_t lib_stream();          // private non-blocking stream of the current device
+cudaStream_t call_stream();         // stream of the running entry point, else lib_stream()
+bool in_call();
+// lib_stream() waits for the work enqueued so far on `s`
+int fence_lib_after(cudaStream_t s);
+// host -> device copy ordered on call_stream() (pageable source may be freed on return)
+int copy_h2d(void* dst, const void* src, size_t bytes);
+
+struct CallScope {
+  cudaStream_t prev;
+  bool prev_in;
+  explicit CallScope(cudaStream_t st);
+  ~CallScope();
+};
+#define MRSR_CALL_SCOPE(st) ::mrsr::CallScope _mrsr_call_scope(st)
+
 // ------------------------------------------------------- device buffers ---
-// Small RAII owner for cudaMalloc'd workspaces held by operator handles.
+// RAII owner of a device workspace from the stream-ordered pool.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -54,23 +78,8 @@ struct DevBuf {
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-  int alloc(size_t n) {
-    release();
-    if (n == 0) return MRSR_OK;
-    cudaError_t e = cudaMalloc(&p, n);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      set_error("cudaMalloc(%zu bytes) failed: %s", n, cudaGetErrorString(e));
-      return MRSR_ERR_ALLOC;
-    }
-    bytes = n;
-    return MRSR_OK;
-  }
+  void release();
+  int alloc(size_t n);
   template <class T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 

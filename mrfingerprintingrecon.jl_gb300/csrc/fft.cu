@@ -62,7 +62,7 @@ int FftPlanHost::init(int L) {
     h[p] = make_float2((float)std::cos(ang), (float)std::sin(ang));
   }
   MRSR_TRY(tw.alloc(sizeof(float2) * L));
-  MRSR_CHECK_CUDA(cudaMemcpy(tw.p, h.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
+  MRSR_TRY(copy_h2d(tw.p, h.data(), sizeof(float2) * L));
   plan.tw = tw.as<float2>();
   return MRSR_OK;
 }

@@ -431,6 +431,7 @@ using namespace mrsr;
 
 extern "C" int mrsr_grog_calib(int ndims, int64_t nr, int64_t ns_per_frame, int64_t nt, int ncoils, int nrep,
                                const float* data, const float* trj, float* lnG_out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(ndims == 2 || ndims == 3, MRSR_ERR_ARG, "ndims must be 2 or 3");
   MRSR_REQUIRE(data && trj && lnG_out, MRSR_ERR_ARG, "NULL argument to mrsr_grog_calib");
   MRSR_REQUIRE(nr >= 2 && ns_per_frame % nr == 0, MRSR_ERR_ARG, "samples per frame must be a multiple of Nr >= 2");
@@ -451,8 +452,8 @@ extern "C" int mrsr_grog_calib(int ndims, int64_t nr, int64_t ns_per_frame, int6
   gauss_legendre01(kLogGL, t, w);
   MRSR_TRY(glt.alloc(sizeof(double) * kLogGL));
   MRSR_TRY(glw.alloc(sizeof(double) * kLogGL));
-  MRSR_CHECK_CUDA(cudaMemcpy(glt.p, t.data(), sizeof(double) * kLogGL, cudaMemcpyHostToDevice));
-  MRSR_CHECK_CUDA(cudaMemcpy(glw.p, w.data(), sizeof(double) * kLogGL, cudaMemcpyHostToDevice));
+  MRSR_TRY(copy_h2d(glt.p, t.data(), sizeof(double) * kLogGL));
+  MRSR_TRY(copy_h2d(glw.p, w.data(), sizeof(double) * kLogGL));
   MRSR_TRY(err.alloc(sizeof(int)));
   MRSR_CHECK_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
   const size_t smem_g = sizeof(float2) * nr * ncoils;
@@ -483,6 +484,7 @@ extern "C" int mrsr_grog_calib(int ndims, int64_t nr, int64_t ns_per_frame, int6
 extern "C" int mrsr_grog_gridding(int ndims, const int64_t* img_shape, int64_t nr, int64_t ns_per_frame, int64_t nt,
                                   int ncoils, int nrep, float* data, const float* trj, const float* lnG,
                                   int32_t* trj_cart_out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(ndims == 2 || ndims == 3, MRSR_ERR_ARG, "ndims must be 2 or 3");
   MRSR_REQUIRE(img_shape && data && trj && lnG && trj_cart_out, MRSR_ERR_ARG, "NULL argument to mrsr_grog_gridding");
   MRSR_REQUIRE(ncoils >= 1 && ncoils <= kGrogMaxCoils, MRSR_ERR_UNSUPPORTED, "GROG supports 1..%d coils",

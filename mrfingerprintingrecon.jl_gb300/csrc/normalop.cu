@@ -609,11 +609,11 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   }
   op->launches = (int)ngroups * (g.ndims == 2 ? 3 : 5);
   if (half) {
-    MRSR_TRY(half_lambda_convert(op, st));
+    if (!op->lam_half.p) MRSR_TRY(half_lambda_convert(op, st));  // a shared kernel may already have it
     MRSR_TRY(half_alloc_scales(op));
-    MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
   }
-  (void)st;
+  // the operator's buffers came from the pool on `st`: make them usable on any stream
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
   return MRSR_OK;
 }
 
@@ -719,6 +719,7 @@ extern "C" int mrsr_nfft_normalop_from_lambda(int ndims, const int64_t* img_shap
                                               int lambda_is_complex, const int64_t* kmask_indcs, int64_t nk,
                                               const float* cmaps, int ncoils, int precision, mrsr_stream_t stream,
                                               mrsr_normalop** out) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(out, MRSR_ERR_ARG, "out is NULL");
   *out = nullptr;
   cudaStream_t st = as_stream(stream);
@@ -738,6 +739,7 @@ extern "C" int mrsr_nfft_normalop_from_lambda(int ndims, const int64_t* img_shap
 extern "C" int mrsr_fft_normalop_from_lambda(int ndims, const int64_t* img_shape, int K, const float* lambda_full,
                                              const float* cmaps, int ncoils, int precision, mrsr_stream_t stream,
                                              mrsr_normalop** out) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(out, MRSR_ERR_ARG, "out is NULL");
   *out = nullptr;
   MRSR_REQUIRE(lambda_full, MRSR_ERR_ARG, "Λ is NULL");
@@ -757,8 +759,10 @@ extern "C" int mrsr_fft_normalop_from_lambda(int ndims, const int64_t* img_shape
 
 extern "C" int mrsr_normalop_apply(mrsr_normalop* op, const float* x, float* y, float alpha_re, float alpha_im,
                                    float beta_re, float beta_im, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(op && x && y, MRSR_ERR_ARG, "NULL argument to mrsr_normalop_apply");
   MRSR_REQUIRE((const void*)x != (const void*)y, MRSR_ERR_ARG, "x and y must not alias");
+  OpUse use{op, as_stream(stream)};
   return apply_impl(op, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(y),
                     make_float2(alpha_re, alpha_im), make_float2(beta_re, beta_im), as_stream(stream), Recorder{});
 }
@@ -773,7 +777,9 @@ extern "C" int mrsr_normalop_info(const mrsr_normalop* op, int64_t* info) {
 }
 
 extern "C" int mrsr_normalop_get_kmask(const mrsr_normalop* op, int64_t* out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(op && out, MRSR_ERR_ARG, "NULL argument");
+  OpUse use{op, as_stream(stream)};
   MRSR_CHECK_CUDA(cudaMemcpyAsync(out, op->kmask.p, sizeof(int64_t) * op->nk, cudaMemcpyDeviceToDevice,
                                   as_stream(stream)));
   return MRSR_OK;
@@ -796,8 +802,10 @@ __global__ void k_unpack_full(const void* packed, int real, int K, int64_t nk, f
 }
 
 extern "C" int mrsr_normalop_get_lambda(const mrsr_normalop* op, void* out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(op && out, MRSR_ERR_ARG, "NULL argument");
   cudaStream_t st = as_stream(stream);
+  OpUse use{op, st};
   LamLayout l = lam_layout(op);
   const unsigned blocks = (unsigned)std::min<int64_t>(cdiv(op->nk, 256), 65535);
   if (op->kind == MRSR_KIND_FFT && op->lam_mode != LAM_FULL_CPLX) {
@@ -826,8 +834,10 @@ extern "C" int mrsr_normalop_get_lambda(const mrsr_normalop* op, void* out, mrsr
 
 extern "C" int mrsr_normalop_profile(mrsr_normalop* op, const float* x, float* y, int iters, float* ms_per_pass,
                                      mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(op && x && y && ms_per_pass && iters > 0, MRSR_ERR_ARG, "bad argument to mrsr_normalop_profile");
   cudaStream_t st = as_stream(stream);
+  OpUse use{op, st};
   std::vector<double> acc(op->launches, 0.0);
   for (int it = 0; it < iters; ++it) {
     std::vector<cudaEvent_t> ev;
@@ -851,3 +861,20 @@ extern "C" int mrsr_normalop_profile(mrsr_normalop* op, const float* x, float* y
 }
 
 extern "C" void mrsr_normalop_destroy(mrsr_normalop* op) { delete op; }
+
+mrsr_normalop::~mrsr_normalop() {
+  if (last_use) {
+    // members are freed on the library stream after the last enqueued use
+    cudaStreamWaitEvent(mrsr::lib_stream(), last_use, 0);
+    cudaEventDestroy(last_use);
+  }
+}
+
+namespace mrsr {
+int mark_use(const mrsr_normalop* cop, cudaStream_t st) {
+  mrsr_normalop* op = const_cast<mrsr_normalop*>(cop);
+  if (!op->last_use) MRSR_CHECK_CUDA(cudaEventCreateWithFlags(&op->last_use, cudaEventDisableTiming));
+  MRSR_CHECK_CUDA(cudaEventRecord(op->last_use, st));
+  return MRSR_OK;
+}
+}  // namespace mrsr

@@ -1,5 +1,7 @@
 // Internal state of a subspace Toeplitz normal operator handle.
 #pragma once
+#include <memory>
+
 #include "cg.cuh"
 #include "fft.cuh"
 
@@ -26,9 +28,25 @@ struct OpGeom {
   int64_t nlast() const { return n[ndims - 1]; }
 };
 
+// The Toeplitz kernel and its kmask, shared (read-only) by every operator
+// made from it with mrsr_normalop_share.
+struct LamStore {
+  DevBuf kmask;      // int64 nk, 1-based column-major grid indices
+  DevBuf lam;        // [tile][chunk][P][FC][TC] of float / float2 (chunked along f_last)
+  DevBuf lam_scale;  // fp16: one float per tile
+  DevBuf lam_half;   // fp16: the chunked kernel in half precision
+};
+
 }  // namespace mrsr
 
 struct mrsr_normalop {
+  mrsr_normalop() : mrsr_normalop(std::make_shared<mrsr::LamStore>()) {}
+  explicit mrsr_normalop(std::shared_ptr<mrsr::LamStore> s)
+      : store(std::move(s)), kmask(store->kmask), lam(store->lam), lam_scale(store->lam_scale),
+        lam_half(store->lam_half) {}
+  mrsr_normalop(const mrsr_normalop&) = delete;
+  mrsr_normalop& operator=(const mrsr_normalop&) = delete;
+
   int kind = MRSR_KIND_NFFT;
   int precision = MRSR_PREC_FP32;
   mrsr::OpGeom geo;
@@ -39,16 +57,21 @@ struct mrsr_normalop {
   int FC = 1;     // Λ chunk length along the last dim
   int Cg = 1;     // coils per group
   int launches = 0;
-  mrsr::DevBuf kmask;      // int64 nk, 1-based column-major grid indices
-  mrsr::DevBuf lam;        // [tile][chunk][P][FC][TC] of float / float2 (chunked along f_last)
-  mrsr::DevBuf lam_scale;  // fp16: one float per tile
-  mrsr::DevBuf lam_half;   // fp16: the chunked kernel in half precision
+  std::shared_ptr<mrsr::LamStore> store;
+  mrsr::DevBuf& kmask;
+  mrsr::DevBuf& lam;
+  mrsr::DevBuf& lam_scale;
+  mrsr::DevBuf& lam_half;
   mrsr::DevBuf cmaps;      // (img..., ncoils) complex; empty = unit coil
   mrsr::DevBuf stack1, stack2;  // intermediates of one coil group
   mrsr::DevBuf scale1, scale2;  // fp16 per-line scales
   mrsr::DevBuf errflag;         // device int
   mrsr::FftPlanHost plan[3];
   mrsr::CgWork cg;              // CG vectors, allocated on first solve
+  // recorded after every call that enqueues work on the operator; the
+  // destructor frees the buffers only after it (stream-ordered, no device sync)
+  cudaEvent_t last_use = nullptr;
+  ~mrsr_normalop();
 };
 
 namespace mrsr {
@@ -62,6 +85,16 @@ int op_set_lambda_packed(mrsr_normalop* op, const void* lam_packed, int is_compl
                          int64_t nk, cudaStream_t st);
 // Λ of an FFT operator from the reference's full (K, K, grid...) complex array; kmask = Λ[1,1,:] .!= 0.
 int op_set_lambda_full(mrsr_normalop* op, const float2* lam_full, cudaStream_t st);
+// record op->last_use on `st` (the work enqueued so far on st may use op)
+int mark_use(const mrsr_normalop* op, cudaStream_t st);
+// marks the operator's use when the entry point returns
+struct OpUse {
+  const mrsr_normalop* op;
+  cudaStream_t st;
+  ~OpUse() {
+    if (op) mark_use(op, st);
+  }
+};
 // Stream compaction: 1-based indices of nonzero flags, sorted.
 int compact_nonzero(const uint8_t* flags, int64_t n, DevBuf& out, int64_t* count, cudaStream_t st);
 }  // namespace mrsr

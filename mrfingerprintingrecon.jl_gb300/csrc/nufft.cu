@@ -88,7 +88,7 @@ int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, DevBuf& out) {
     h[i] = (float)(1.0 / (hw * s));
   }
   MRSR_TRY(out.alloc(sizeof(float) * count));
-  MRSR_CHECK_CUDA(cudaMemcpy(out.p, h.data(), sizeof(float) * count, cudaMemcpyHostToDevice));
+  MRSR_TRY(copy_h2d(out.p, h.data(), sizeof(float) * count));
   return MRSR_OK;
 }
 
@@ -554,6 +554,7 @@ extern "C" int mrsr_nfft_normalop_create(int ndims, const int64_t* img_shape, in
                                          const float* trj, const uint8_t* sample_mask, const void* U, int u_is_complex,
                                          int K, const float* cmaps, int ncoils, int precision, mrsr_stream_t stream,
                                          mrsr_normalop** out) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(out, MRSR_ERR_ARG, "out is NULL");
   *out = nullptr;
   MRSR_REQUIRE(trj && U, MRSR_ERR_ARG, "trj and U must be device pointers");
@@ -582,6 +583,7 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
                                    const float* data, const float* trj, const uint8_t* sample_mask, const void* U,
                                    int u_is_complex, int K, const float* cmaps, int dcf_kind, const float* dcf_array,
                                    float* out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(ndims == 2 || ndims == 3, MRSR_ERR_ARG, "ndims must be 2 or 3");
   MRSR_REQUIRE(img_shape && data && trj && out, MRSR_ERR_ARG, "NULL argument to mrsr_backprojection");
   MRSR_REQUIRE(ncoils >= 1 && ns_per_frame >= 1 && nt >= 1, MRSR_ERR_ARG, "empty data");
@@ -639,13 +641,13 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
     k_bp_fold<<<grid1d(nimg * K), 256, 0, st>>>(fa);
     MRSR_LAUNCH_CHECK();
   }
-  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
-  return MRSR_OK;
+  return MRSR_OK;  // asynchronous on `st`; the temporaries are freed in stream order
 }
 
 extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t ns_per_frame, int64_t nt, int ncoils,
                                   const float* x, const float* trj, const void* U, int u_is_complex, int K,
                                   const float* cmaps, float* data_out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(ndims == 2 || ndims == 3, MRSR_ERR_ARG, "ndims must be 2 or 3");
   MRSR_REQUIRE(img_shape && x && trj && U && data_out, MRSR_ERR_ARG, "NULL argument to mrsr_forward_model");
   MRSR_REQUIRE(K >= 1 && K <= 8, MRSR_ERR_UNSUPPORTED, "forward model supports 1 <= K <= 8");
@@ -691,6 +693,5 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
     k_interp<<<spread_blocks(sl.set.n), 256, 0, st>>>(ia);
     MRSR_LAUNCH_CHECK();
   }
-  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
-  return MRSR_OK;
+  return MRSR_OK;  // asynchronous on `st`
 }

@@ -126,6 +126,16 @@ class NormalOperator:
 
     Lambda = Λ
 
+    def share(self, cmaps=None, precision=None, stream=None):
+        """A new operator on this operator's Toeplitz kernel and kmask (shared, not copied)
+        with its own coil maps; ``precision`` defaults to this operator's."""
+        S = stack_cmaps(cmaps)
+        nc = 1 if S is None else int(S.shape[-1])
+        prec = self.precision if precision is None else _prec(precision)
+        op = _new_handle(_lib.load().mrsr_normalop_share, self._h, ptr(S), nc, prec, stream_handle(stream))
+        op._cmaps_ref = S
+        return op
+
     def profile(self, x, y, iters=10, stream=None):
         """Per-pass device milliseconds of one apply (CUDA events between launches)."""
         xi, yi = self._as_image(x), self._as_image(y)

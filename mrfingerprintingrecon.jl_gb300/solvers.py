@@ -55,3 +55,58 @@ def cg_refined(A_lo, A_hi, b, inner_iters=20, max_outer=10, tol=1e-4, log=False,
     if log:
         return CgResult(x, outer.value, rel.value)
     return x
+
+
+class CgBatch:
+    """Fixed-iteration solves of independent systems recorded into one CUDA graph.
+
+    Entry i solves ``ops[i] x[i] = b[i]`` with ``cg(A, b; maxiter=iters,
+    reltol=0)`` from x0 = 0, or, when ``ops_hi`` is given, by mixed-precision
+    refinement with ``outer`` fixed steps (inner CG on ``ops[i]``, residual with
+    ``ops_hi[i]``).  Each entry is a branch of the graph, so the solves overlap
+    on the device; :meth:`launch` re-solves with the current contents of the
+    ``b`` tensors (their storage is baked into the graph).
+    """
+
+    def __init__(self, ops, bs, xs, iters, ops_hi=None, outer=1, stream=None):
+        lib = _lib.load()
+        n = len(ops)
+        if not (len(bs) == len(xs) == n) or n == 0:
+            raise ValueError("ops, bs and xs must have the same nonzero length")
+        self._ops, self._ops_hi = list(ops), (list(ops_hi) if ops_hi is not None else None)
+        self._b = [ops[i]._as_image(bs[i]) for i in range(n)]
+        self._x = [ops[i]._as_image(xs[i]) for i in range(n)]
+        for i in range(n):
+            if self._b[i].data_ptr() != bs[i].data_ptr() or self._x[i].data_ptr() != xs[i].data_ptr():
+                raise ValueError("b and x must be column-major complex64 CUDA tensors of the operator's size")
+        P = C.c_void_p * n
+        lo = P(*[o.handle.value for o in ops])
+        hi = P(*[o.handle.value for o in ops_hi]) if ops_hi is not None else None
+        bp = P(*[t.data_ptr() for t in self._b])
+        xp = P(*[t.data_ptr() for t in self._x])
+        h = C.c_void_p()
+        _lib.check(lib.mrsr_cg_batch_create(lo, hi, bp, xp, n, int(iters), int(outer), stream_handle(stream),
+                                            C.byref(h)))
+        self._h = h
+        self.n = n
+
+    def launch(self, stream=None):
+        _lib.check(_lib.load().mrsr_cg_batch_launch(self._h, stream_handle(stream)))
+
+    def result(self, i):
+        """(iterations or outer steps, residual norm) of entry i; waits for the last launch."""
+        it = C.c_int(0)
+        rn = C.c_double(0.0)
+        _lib.check(_lib.load().mrsr_cg_batch_result(self._h, int(i), C.byref(it), C.byref(rn)))
+        return it.value, rn.value
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().mrsr_cg_batch_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
