@@ -15,7 +15,10 @@ namespace mrsr {
 
 // ---------------------------------------------------------- kernels ---
 
-template <class SP>
+// PR: the NFFT operator's zero-padded half (inputs n < L/2 only; outputs kept
+// for n < L/2 after inverse transforms).  A compile-time flag, so the register
+// DFTs fold the known zeros and drop the unused outputs.
+template <class SP, bool PR>
 __global__ void __launch_bounds__(512) k4_rows_fwd(RowsFwdArgs a, Slots sl) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   extern __shared__ float2 smem[];
@@ -27,11 +30,11 @@ __global__ void __launch_bounds__(512) k4_rows_fwd(RowsFwdArgs a, Slots sl) {
   const int64_t row0 = (int64_t)blockIdx.x * a.rpc;
   const int nr = (int)min((int64_t)a.rpc, a.nrows - row0);
   const int NO = a.rpc * a.K;
-  const int nload = (a.n1 * 2 == L) ? R1 / 2 : R1;
+  constexpr int nload = PR ? R1 / 2 : R1;
   __syncthreads();
   step_a<SP, -1>(sm, sl, NO, tw, nload, [&](int lo, int, int n) -> float2 {
     const int rl = lo / a.K, k = lo - rl * a.K;
-    if (rl >= nr || n >= a.n1) return make_float2(0.f, 0.f);
+    if (rl >= nr || (!PR && n >= a.n1)) return make_float2(0.f, 0.f);
     const int64_t r = row0 + rl;
     float2 v = a.x[n + (int64_t)a.n1 * (r + a.nrows * k)];
     if (a.cmaps) v = cmul(a.cmaps[n + (int64_t)a.n1 * (r + a.nrows * c)], v);
@@ -44,7 +47,7 @@ __global__ void __launch_bounds__(512) k4_rows_fwd(RowsFwdArgs a, Slots sl) {
   });
 }
 
-template <class SP>
+template <class SP, bool PR>
 __global__ void __launch_bounds__(512) k4_rows_inv(RowsInvArgs a, Slots sl) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   extern __shared__ float2 smem[];
@@ -55,7 +58,7 @@ __global__ void __launch_bounds__(512) k4_rows_inv(RowsInvArgs a, Slots sl) {
   const int64_t row0 = (int64_t)blockIdx.x * a.rpc;
   const int nr = (int)min((int64_t)a.rpc, a.nrows - row0);
   const int NO = a.rpc * a.ncg;
-  const int nkeep = (a.n1 * 2 == L) ? R2 / 2 : R2;
+  constexpr int nkeep = PR ? R2 / 2 : R2;
   __syncthreads();
   step_a<SP, +1>(sm, sl, NO, tw, R1, [&](int lo, int, int m) -> float2 {
     const int rl = lo / a.ncg, cl = lo - rl * a.ncg;
@@ -87,50 +90,68 @@ __global__ void __launch_bounds__(512) k4_rows_inv(RowsInvArgs a, Slots sl) {
   }
 }
 
-template <class SP>
+// per-voxel K x K product at every frequency f of the tile, rank KK known at compile time
+template <class SP, int KK>
+__device__ __forceinline__ void lam_voxels(const LamPassArgs& a, float2* sm, const Slots& sl, int64_t tile) {
+  constexpr int R1 = SP::R1, L = SP::L;
+  const int64_t pstride = (int64_t)a.FC * a.TC;
+  for (int t = threadIdx.x; t < (L << sl.tcs); t += blockDim.x) {
+    const int li = t & (a.TC - 1);
+    const int f = t >> sl.tcs;          // f = f1 + R1 f2
+    const int f1 = f % R1, f2 = f / R1;
+    float2 X[KK], Y[KK];
+#pragma unroll
+    for (int k = 0; k < KK; ++k) X[k] = sm[sl.at(k, f1, f2, li, R1)];
+    const int ch = (int)a.fcd.div((uint32_t)f), fc = f - ch * a.FC;
+    const int64_t lbase = (((tile * a.NCH + ch) * a.P) * (int64_t)a.FC + fc) * a.TC + li;
+    lam_apply_ptr<KK>(a.lam_mode, KK, a.lam, lbase, pstride, X, Y);
+#pragma unroll
+    for (int k = 0; k < KK; ++k) sm[sl.at(k, f1, f2, li, R1)] = Y[k];
+  }
+}
+
+template <class SP, bool PR>
 __global__ void __launch_bounds__(256, 2) k4_lambda(LamPassArgs a, Slots sl) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* sm = smem + L;
   load_twiddles(tw, a.pl);
-  const int cl = blockIdx.y;
-  const int64_t tile = blockIdx.x;
+  // coil fastest: the CTAs of one column tile run together and share its Λ tile in L2
+  const int cl = (int)(blockIdx.x % (unsigned)a.ncg);
+  const int64_t tile = blockIdx.x / (unsigned)a.ncg;
   const int64_t plane = (int64_t)a.nrow * a.inner;
   float2* base = a.stack + (int64_t)cl * a.K * plane + tile * a.TC;
-  const int nload = (a.nin * 2 == L) ? R1 / 2 : R1;
-  const int nkeep = (a.nout * 2 == L) ? R1 / 2 : R1;
+  constexpr int nload = PR ? R1 / 2 : R1;
+  constexpr int nkeep = PR ? R1 / 2 : R1;
   __syncthreads();
   step_a<SP, -1>(sm, sl, a.K, tw, nload, [&](int k, int li, int n) -> float2 {
-    return (n < a.nin) ? base[k * plane + (int64_t)n * a.inner + li] : make_float2(0.f, 0.f);
+    return (PR || n < a.nin) ? base[k * plane + (int64_t)n * a.inner + li] : make_float2(0.f, 0.f);
   });
   __syncthreads();
   step_b<SP, -1>(sm, sl, a.K, R2, [&](int lo, int li, int f1, int f2, float2 v) { sm[sl.at(lo, f1, f2, li, R1)] = v; });
   __syncthreads();
-  // per-voxel K x K product at every frequency f = f1 + R1 f2 of the tile
-  for (int t = threadIdx.x; t < (L << sl.tcs); t += blockDim.x) {
-    const int li = t & (a.TC - 1);
-    const int r = t >> sl.tcs;
-    const int f1 = r % R1, f2 = r / R1;
-    const int f = f1 + R1 * f2;
-    float2 X[KMAX], Y[KMAX];
-#pragma unroll
-    for (int k = 0; k < KMAX; ++k) X[k] = (k < a.K) ? sm[sl.at(k, f1, f2, li, R1)] : make_float2(0.f, 0.f);
-    const int64_t lbase = lam_elem(tile, f, li, 0, a.TC, a.P, a.FC, a.NCH);
-    lam_apply<KMAX>(a, lbase, (int64_t)a.FC * a.TC, X, Y);
-#pragma unroll
-    for (int k = 0; k < KMAX; ++k)
-      if (k < a.K) sm[sl.at(k, f1, f2, li, R1)] = Y[k];
+  switch (a.K) {
+    case 1: lam_voxels<SP, 1>(a, sm, sl, tile); break;
+    case 2: lam_voxels<SP, 2>(a, sm, sl, tile); break;
+    case 3: lam_voxels<SP, 3>(a, sm, sl, tile); break;
+    case 4: lam_voxels<SP, 4>(a, sm, sl, tile); break;
+    case 5: lam_voxels<SP, 5>(a, sm, sl, tile); break;
+    case 6: lam_voxels<SP, 6>(a, sm, sl, tile); break;
+    case 7: lam_voxels<SP, 7>(a, sm, sl, tile); break;
+    default: lam_voxels<SP, 8>(a, sm, sl, tile); break;
   }
   __syncthreads();
   inv_step_a_slots<SP>(sm, sl, a.K, tw);
   __syncthreads();
   inv_step_b_slots<SP>(sm, sl, a.K, nkeep, [&](int k, int li, int n, float2 v) {
-    if (n < a.nout) base[k * plane + (int64_t)n * a.inner + li] = v;
+    if (PR || n < a.nout) base[k * plane + (int64_t)n * a.inner + li] = v;
   });
 }
 
-template <class SP, int S>
+// S = -1: forward, input rows n < nin (PR: nin = L/2), all L outputs kept;
+// S = +1: inverse, all L inputs, outputs kept for n < nout (PR: nout = L/2).
+template <class SP, int S, bool PR>
 __global__ void __launch_bounds__(512) k4_mid(MidArgs a, Slots sl) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   extern __shared__ float2 smem[];
@@ -143,16 +164,17 @@ __global__ void __launch_bounds__(512) k4_mid(MidArgs a, Slots sl) {
   const int64_t p = blockIdx.z;
   const float2* ib = a.in + (p * a.n3 + o0) * a.nin * a.width + col0;
   float2* ob = a.out + (p * a.n3 + o0) * a.nout * a.width + col0;
-  const int nload = (a.nin * 2 == L) ? R1 / 2 : R1;
-  const int nkeep = (a.nout * 2 == L) ? R2 / 2 : R2;
+  constexpr int nload = (PR && S < 0) ? R1 / 2 : R1;
+  constexpr int nkeep = (PR && S > 0) ? R2 / 2 : R2;
   __syncthreads();
   step_a<SP, S>(sm, sl, a.NOo, tw, nload, [&](int o, int li, int n) -> float2 {
-    return (o < no && n < a.nin) ? ib[((int64_t)o * a.nin + n) * a.width + li] : make_float2(0.f, 0.f);
+    return (o < no && ((PR && S < 0) || n < a.nin)) ? ib[((int64_t)o * a.nin + n) * a.width + li]
+                                                    : make_float2(0.f, 0.f);
   });
   __syncthreads();
   step_b<SP, S>(sm, sl, a.NOo, nkeep, [&](int o, int li, int f1, int f2, float2 v) {
     const int n = f1 + R1 * f2;
-    if (o < no && n < a.nout) ob[((int64_t)o * a.nout + n) * a.width + li] = v;
+    if (o < no && ((PR && S > 0) || n < a.nout)) ob[((int64_t)o * a.nout + n) * a.width + li] = v;
   });
 }
 
@@ -339,7 +361,8 @@ int fast_rows_fwd(const RowsFwdArgs& a, int64_t nrows, int ncg, cudaStream_t st)
     const int NO = a.rpc * a.K;
     const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)NO * SP::R1 * sl.W);
     dim3 grid((unsigned)cdiv(nrows, a.rpc), ncg);
-    return launch(k4_rows_fwd<SP>, grid, round_threads(NO * SP::R1), smem, st, a, sl);
+    if (a.n1 * 2 == SP::L) return launch(k4_rows_fwd<SP, true>, grid, round_threads(NO * SP::R1), smem, st, a, sl);
+    return launch(k4_rows_fwd<SP, false>, grid, round_threads(NO * SP::R1), smem, st, a, sl);
   });
 }
 
@@ -350,7 +373,8 @@ int fast_rows_inv(const RowsInvArgs& a, int64_t nrows, cudaStream_t st) {
     const int NO = a.rpc * a.ncg;
     const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)NO * SP::R1 * sl.W);
     dim3 grid((unsigned)cdiv(nrows, a.rpc), a.K);
-    return launch(k4_rows_inv<SP>, grid, round_threads(NO * SP::R1), smem, st, a, sl);
+    if (a.n1 * 2 == SP::L) return launch(k4_rows_inv<SP, true>, grid, round_threads(NO * SP::R1), smem, st, a, sl);
+    return launch(k4_rows_inv<SP, false>, grid, round_threads(NO * SP::R1), smem, st, a, sl);
   });
 }
 
@@ -410,8 +434,12 @@ int fast_lambda(const LamPassArgs& a, int ncg, int planes_total, int* errword, c
       return MRSR_OK;
     }
     const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)a.K * SP::R1 * sl.W);
-    dim3 grid((unsigned)(a.inner / a.TC), ncg);
-    return launch(k4_lambda<SP>, grid, 256, smem, st, a, sl);
+    LamPassArgs b = a;
+    b.ncg = ncg;
+    b.fcd = FastDiv((uint32_t)a.FC);
+    dim3 grid((unsigned)((a.inner / a.TC) * ncg));
+    if (a.nin * 2 == SP::L && a.nout * 2 == SP::L) return launch(k4_lambda<SP, true>, grid, 256, smem, st, b, sl);
+    return launch(k4_lambda<SP, false>, grid, 256, smem, st, b, sl);
   });
 }
 
@@ -422,8 +450,11 @@ int fast_mid(const MidArgs& a, int nplanes, cudaStream_t st) {
     const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)a.NOo * SP::R1 * sl.W);
     dim3 grid((unsigned)(a.width / a.TC), (unsigned)cdiv(a.n3, a.NOo), (unsigned)nplanes);
     const int thr = round_threads(a.NOo * a.TC * SP::R1);
-    if (a.sgn < 0) return launch(k4_mid<SP, -1>, grid, thr, smem, st, a, sl);
-    return launch(k4_mid<SP, +1>, grid, thr, smem, st, a, sl);
+    const bool pr = a.sgn < 0 ? a.nin * 2 == SP::L : a.nout * 2 == SP::L;
+    if (a.sgn < 0) return pr ? launch(k4_mid<SP, -1, true>, grid, thr, smem, st, a, sl)
+                             : launch(k4_mid<SP, -1, false>, grid, thr, smem, st, a, sl);
+    return pr ? launch(k4_mid<SP, +1, true>, grid, thr, smem, st, a, sl)
+              : launch(k4_mid<SP, +1, false>, grid, thr, smem, st, a, sl);
   });
 }
 

@@ -233,8 +233,8 @@ __global__ void __launch_bounds__(256, 2) kh_lambda(HalfArgs a, Slots sl) {
   __shared__ float smax;
   load_twiddles(tw, a.pl);
   if (threadIdx.x == 0) smax = 0.f;
-  const int cl = blockIdx.y;
-  const int64_t tile = blockIdx.x;
+  const int cl = (int)(blockIdx.x % (unsigned)a.ncg);  // coil fastest (Λ tile shared in L2)
+  const int64_t tile = blockIdx.x / (unsigned)a.ncg;
   const int64_t plane = (int64_t)a.nlast * a.inner;
   __half2* stack = a.d == 2 ? a.st1 : a.st2;
   __half2* base = stack + (int64_t)cl * a.K * plane + tile * a.TC;
@@ -524,7 +524,7 @@ int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha,
       using SP = decltype(sp);
       const Slots sl = slots_for(SP::R2, a.TC);
       const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)K * SP::R1 * sl.W);
-      return launch_h(kh_lambda<SP>, dim3((unsigned)a.ntiles, a.ncg), 256, smem, st, a, sl);
+      return launch_h(kh_lambda<SP>, dim3((unsigned)(a.ntiles * a.ncg)), 256, smem, st, a, sl);
     }));
     if (record) record(rec_ctx);
     if (g.ndims == 3) {

@@ -83,6 +83,21 @@ struct DevBuf {
   template <class T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 
+// ------------------------------------------------------- fast division ---
+// Division by a runtime constant d (0 <= n < 2^31): q = (umulhi(n, m) + n) >> s
+// with s = ceil(log2 d), m = floor(2^32 (2^s - d) / d) + 1 (Granlund and
+// Montgomery's round-up method, the 33-bit magic's top bit folded as "+ n").
+struct FastDiv {
+  uint32_t d = 1, m = 1, s = 0;
+  FastDiv() = default;
+  explicit FastDiv(uint32_t d_) : d(d_) {
+    s = 0;
+    while ((1ull << s) < d) ++s;
+    m = (uint32_t)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(n, m) + n) >> s; }
+};
+
 // ------------------------------------------------------ complex helpers ---
 __host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }

@@ -593,11 +593,17 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   const int64_t per_coil = (int64_t)g.K * g.g[0] * g.n[1] * g.n[2] * esz;
   int64_t cg = env_int("MRSR_COIL_GROUP", 0);
   if (cg <= 0) {
-    if (g.ndims == 2)
+    if (g.ndims == 2) {
       cg = std::max<int64_t>(1, (48ll << 20) / std::max<int64_t>(per_coil, 1));
-    else
-      cg = 1;
+    } else {
+      // 3D stacks are far larger than L2; group as many coils as a 12 GB stack budget
+      // allows, so one Λ pass streams the kernel once for all of them
+      const int64_t per_coil3 = per_coil + (int64_t)g.K * g.g[0] * g.g[1] * g.n[2] * esz;
+      cg = std::max<int64_t>(1, (env_int("MRSR_STACK_BUDGET_MB", 12288) << 20) / std::max<int64_t>(per_coil3, 1));
+    }
   }
+  // rows inverse holds one row of every coil of the group in shared memory (<= ~200 KB)
+  cg = std::min<int64_t>(cg, std::max<int64_t>(1, (200ll << 10) / (9 * g.g[0])));
   cg = std::min<int64_t>(cg, g.ncoils);
   const int64_t ngroups = cdiv(g.ncoils, cg);
   cg = cdiv(g.ncoils, ngroups);

@@ -31,6 +31,8 @@ struct LamPassArgs {
   const void* lam;     // [tile][chunk][P][FC][TC]
   float2* stack;       // planes [cl][k][row][inner], in place
   int FC, NCH;         // Λ chunk: frequencies per chunk, chunks per tile (L = FC * NCH)
+  int ncg = 1;         // coils of the launch (four-step kernel: block = tile * ncg + coil)
+  FastDiv fcd;         // division by FC
 };
 
 // Element (tile, frequency f, column li, entry p) of the chunked Λ layout;
