@@ -415,10 +415,19 @@ struct RowTiling {
   size_t smem;
 };
 
+static int64_t env_int(const char* name, int64_t dflt);
+
+// line elements per CTA of the four-step row passes (one exchange buffer)
+static int64_t fast_row_elems() {
+  static const int64_t v = env_int("MRSR_ROW_ELEMS", 4096);
+  return v;
+}
+
 static RowTiling rows_tiling(int L, int lines_per_row, int64_t nrows) {
   RowTiling t;
   t.lstride = L;
-  int rpc = (int)std::max<int64_t>(1, kRowElems / ((int64_t)lines_per_row * L));
+  const int64_t elems = fast_length(L) ? fast_row_elems() : kRowElems;
+  int rpc = (int)std::max<int64_t>(1, elems / ((int64_t)lines_per_row * L));
   rpc = (int)std::min<int64_t>(rpc, nrows);
   t.rpc = rpc;
   t.threads = 256;
