@@ -49,8 +49,11 @@ enum {
 /* Storage precision of the oversampled K-stack and the Toeplitz kernel. */
 enum {
   MRSR_PREC_FP32 = 0, /* float32 everywhere (the reference's precision)   */
-  MRSR_PREC_FP16 = 1  /* fp16 storage with per-line / per-tile scales,
-                         fp32 arithmetic                                   */
+  MRSR_PREC_FP16 = 1, /* fp16 storage with per-tile scales, fp32 arithmetic */
+  MRSR_PREC_FP16_ARITH = 2 /* fp16 storage and fp16 (half2) FFT / kernel
+                              arithmetic on line pairs, fp32 coil sums; 2D
+                              four-step grids with an even Λ tile width,
+                              else as MRSR_PREC_FP16                       */
 };
 
 /* Density compensation of calculate_backprojection (src/BackProjection.jl:169-181). */

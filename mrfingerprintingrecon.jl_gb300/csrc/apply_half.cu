@@ -14,6 +14,7 @@
 #include <algorithm>
 
 #include "fft4.cuh"
+#include "half.cuh"
 #include "passes.cuh"
 
 namespace mrsr {
@@ -25,27 +26,8 @@ __device__ __forceinline__ float2 ld_h(const __half2* p, int64_t i, float s) {
   return make_float2(v.x * s, v.y * s);
 }
 
-__device__ __forceinline__ float amax2(float2 v) { return fmaxf(fabsf(v.x), fabsf(v.y)); }
-
-// block-wide max of per-thread maxima; every thread of the block calls it.
-// Non-negative floats order like their bit patterns read as unsigned.
-__device__ __forceinline__ void block_max_commit(float* m, float local) {
-  const unsigned u = __reduce_max_sync(0xffffffffu, __float_as_uint(local));
-  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned*>(m), u);
-}
 
 __device__ __forceinline__ float scale_of(float mx) { return mx > 0.f ? mx / kHalfTarget : 1.f; }
-
-struct HalfTiles {
-  int rpc;           // rows per CTA of the row passes
-  int64_t nrowblk;   // row blocks per plane group
-  int TCm, NOo;      // dim-2 pass tiling (3D)
-  int64_t nslab, nmtile;
-  float* s_rows;     // [coil][row block]
-  float* s_mid;      // [plane][slab][column tile]
-  float* s_lam;      // [coil][tile]
-  float* s_mid2;     // [plane][slab][column tile]
-};
 
 struct HalfArgs {
   FftPlan pl;
@@ -346,7 +328,7 @@ __global__ void __launch_bounds__(512) kh_rows_inv(HalfArgs a, Slots sl) {
 
 // ----------------------------------------------------- Λ to fp16 tiles ---
 // max |entry| over each tile of the float32 chunked Λ, then half storage
-__global__ void k_lam_tile_max(const float* lamf, int64_t per_tile, int64_t ntiles, float* scale) {
+__global__ void k_lam_tile_max(const float* lamf, int64_t per_tile, int64_t ntiles, float target, float* scale) {
   __shared__ float red[32];
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     float m = 0.f;
@@ -357,7 +339,7 @@ __global__ void k_lam_tile_max(const float* lamf, int64_t per_tile, int64_t ntil
     if (threadIdx.x == 0) {
       float mm = 0.f;
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mm = fmaxf(mm, red[w]);
-      scale[t] = scale_of(mm);
+      scale[t] = mm > 0.f ? mm / target : 1.f;
     }
     __syncthreads();
   }
@@ -369,29 +351,6 @@ __global__ void k_lam_to_half(const float* lamf, int64_t per_tile, int64_t n, co
 }
 
 // ----------------------------------------------------------- dispatch ---
-template <class F>
-static int with_split_h(int L, F f) {
-  switch (L) {
-    case 64: return f(Split<8, 8>());
-    case 128: return f(Split<8, 16>());
-    case 256: return f(Split<16, 16>());
-    case 384: return f(Split<12, 32>());
-    case 512: return f(Split<16, 32>());
-    case 768: return f(Split<24, 32>());
-    case 1024: return f(Split<32, 32>());
-    default: return MRSR_ERR_UNSUPPORTED;
-  }
-}
-
-static Slots slots_for(int R2, int TC) {
-  Slots s;
-  s.TC = TC;
-  s.tcs = 0;
-  while ((1 << s.tcs) < TC) ++s.tcs;
-  s.W = slots_width(R2, TC);
-  return s;
-}
-
 template <class K>
 static int launch_h(K k, dim3 grid, int threads, size_t smem, cudaStream_t st, const HalfArgs& a, const Slots& sl) {
   MRSR_REQUIRE(smem <= 227 * 1024, MRSR_ERR_UNSUPPORTED, "shared memory request %zu too large", smem);
@@ -400,11 +359,6 @@ static int launch_h(K k, dim3 grid, int threads, size_t smem, cudaStream_t st, c
   k<<<grid, threads, smem, st>>>(a, sl);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
-}
-
-static int rthreads(int tasks) {
-  int t = ((tasks + 31) / 32) * 32;
-  return t < 128 ? 128 : (t > 512 ? 512 : t);
 }
 
 bool half_supported(const mrsr_normalop* op) {
@@ -419,7 +373,10 @@ int half_lambda_convert(mrsr_normalop* op, cudaStream_t st) {
   MRSR_TRY(op->lam_scale.alloc(sizeof(float) * ntiles));
   MRSR_TRY(op->lam_half.alloc(sizeof(__half) * per_tile * ntiles));
   const unsigned b = (unsigned)std::min<int64_t>(ntiles, 65535);
-  k_lam_tile_max<<<b, 256, 0, st>>>(op->lam.as<float>(), per_tile, ntiles, op->lam_scale.as<float>());
+  // tile max scaled to 1: the fp16-arithmetic (pair) kernels need |Λ| <= 1, the float32-arithmetic
+  // ones take any scale, and operators of both kinds may share this copy
+  const float target = 1.f;
+  k_lam_tile_max<<<b, 256, 0, st>>>(op->lam.as<float>(), per_tile, ntiles, target, op->lam_scale.as<float>());
   MRSR_LAUNCH_CHECK();
   const int64_t n = per_tile * ntiles;
   k_lam_to_half<<<(unsigned)std::min<int64_t>(cdiv(n, 256), 65535), 256, 0, st>>>(op->lam.as<float>(), per_tile, n,
@@ -427,22 +384,6 @@ int half_lambda_convert(mrsr_normalop* op, cudaStream_t st) {
                                                                                   op->lam_half.as<__half>());
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
-}
-
-// scale-array sizes of the fp16 tiles (same formulas as the launches below)
-static HalfTiles tiles_of(const mrsr_normalop* op) {
-  const OpGeom& g = op->geo;
-  HalfTiles t{};
-  const int L1 = (int)g.g[0];
-  const int64_t nrows = g.n[1] * g.n[2];
-  t.rpc = (int)std::max<int64_t>(1, std::min<int64_t>(4096 / ((int64_t)std::max(g.K, op->Cg) * L1), nrows));
-  t.nrowblk = cdiv(nrows, t.rpc);
-  t.TCm = 8;
-  while (t.TCm > 1 && g.g[0] % t.TCm) t.TCm >>= 1;
-  t.NOo = (int)std::max<int64_t>(1, std::min<int64_t>(4096 / ((int64_t)t.TCm * g.g[1]), g.n[2]));
-  t.nslab = cdiv(g.n[2], t.NOo);
-  t.nmtile = g.g[0] / t.TCm;
-  return t;
 }
 
 int half_alloc_scales(mrsr_normalop* op) {

@@ -445,8 +445,10 @@ static void record_cb(void* ctx) { static_cast<Recorder*>(ctx)->record(); }
 
 static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
                       Recorder rec) {
-  if (op->precision == MRSR_PREC_FP16)
+  if (op->precision != MRSR_PREC_FP32) {
+    if (pair_supported(op)) return apply_pair_impl(op, x, y, alpha, beta, st, rec.ev ? record_cb : nullptr, &rec);
     return apply_half_impl(op, x, y, alpha, beta, st, rec.ev ? record_cb : nullptr, &rec);
+  }
   const OpGeom& g = op->geo;
   const int K = g.K;
   const float inv = 1.0f / (float)g.ngrid();
@@ -550,8 +552,8 @@ int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_
   MRSR_REQUIRE(img_shape != nullptr, MRSR_ERR_ARG, "img_shape is NULL");
   MRSR_REQUIRE(K >= 1 && K <= KMAX, MRSR_ERR_UNSUPPORTED, "rank K=%d outside 1..%d", K, KMAX);
   MRSR_REQUIRE(ncoils >= 1, MRSR_ERR_ARG, "ncoils must be >= 1");
-  MRSR_REQUIRE(precision == MRSR_PREC_FP32 || precision == MRSR_PREC_FP16, MRSR_ERR_ARG, "unknown precision %d",
-               precision);
+  MRSR_REQUIRE(precision == MRSR_PREC_FP32 || precision == MRSR_PREC_FP16 || precision == MRSR_PREC_FP16_ARITH,
+               MRSR_ERR_ARG, "unknown precision %d", precision);
   op->kind = kind;
   op->precision = precision;
   OpGeom& g = op->geo;
@@ -594,7 +596,7 @@ int op_set_cmaps(mrsr_normalop* op, const float* cmaps, cudaStream_t st) {
 
 int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   const OpGeom& g = op->geo;
-  const bool half = op->precision == MRSR_PREC_FP16;
+  const bool half = op->precision != MRSR_PREC_FP32;
   MRSR_REQUIRE(!half || half_supported(op), MRSR_ERR_UNSUPPORTED,
                "fp16 storage needs grid lengths with a register four-step split (64, 128, 256, 384, 512, 768, 1024)");
   const int64_t esz = half ? 4 : (int64_t)sizeof(float2);
@@ -625,7 +627,10 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   op->launches = (int)ngroups * (g.ndims == 2 ? 3 : 5);
   if (half) {
     if (!op->lam_half.p) MRSR_TRY(half_lambda_convert(op, st));  // a shared kernel may already have it
-    MRSR_TRY(half_alloc_scales(op));
+    if (pair_supported(op))
+      MRSR_TRY(pair_alloc(op, st));
+    else
+      MRSR_TRY(half_alloc_scales(op));
   }
   // the operator's buffers came from the pool on `st`: make them usable on any stream
   MRSR_CHECK_CUDA(cudaStreamSynchronize(st));

@@ -146,5 +146,10 @@ int half_lambda_convert(mrsr_normalop* op, cudaStream_t st);
 int half_alloc_scales(mrsr_normalop* op);
 int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
                     void (*record)(void*), void* rec_ctx);
+// fp16-arithmetic operator on line pairs (apply_pair.cu), 2D four-step grids with an even Λ tile width
+bool pair_supported(const mrsr_normalop* op);
+int pair_alloc(mrsr_normalop* op, cudaStream_t st);
+int apply_pair_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
+                    void (*record)(void*), void* rec_ctx);
 
 }  // namespace mrsr
