@@ -92,30 +92,6 @@ int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, DevBuf& out) {
   return MRSR_OK;
 }
 
-// Tap weights of one sample: lane i < w*d computes the weight of tap (i % w)
-// of dimension i / w; the first tap index per dimension is l0[d].
-// u = k * M is formed in float64 so the kernel argument (l - u) / (w/2) is exact
-// before rounding to float (float32 k times a non-power-of-two M is not exact).
-__device__ __forceinline__ void es_lane_weight(const float* kd, const int64_t* M, int d, int lane, float* wt_out,
-                                               int64_t* l0) {
-  const int hw = kEsWidth / 2;
-  float wt = 0.f;
-#pragma unroll
-  for (int dd = 0; dd < 3; ++dd) {
-    if (dd < d) {
-      const double u = (double)kd[dd] * (double)M[dd];
-      const int64_t l = (int64_t)ceil(u - hw);
-      l0[dd] = l;
-      if (lane / kEsWidth == dd) {
-        const int t = lane % kEsWidth;
-        const float z = (float)(((double)(l + t) - u) / hw);
-        wt = (fabsf(z) < 1.f) ? expf(kEsBeta * (sqrtf(1.f - z * z) - 1.f)) : 0.f;
-      }
-    }
-  }
-  *wt_out = wt;
-}
-
 __device__ __forceinline__ int64_t wrap(int64_t l, int64_t M) {
   l %= M;
   return l < 0 ? l + M : l;
@@ -227,6 +203,7 @@ static unsigned spread_blocks(int64_t n) { return (unsigned)std::min<int64_t>(st
 
 int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
+  if (tiles_applicable(a.S, a.S.d, a.U) && a.K <= 8) return spread_lambda_tiled(a, st);
   k_spread_lambda<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
@@ -234,6 +211,7 @@ int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
 
 int spread_data(const SpreadDataArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
+  if (tiles_applicable(a.S, a.S.d, a.U)) return spread_data_tiled(a, st);
   k_spread_data<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;

@@ -32,6 +32,38 @@ struct SampleList {
   int init(int d, const float* trj, int64_t ns_pf, int64_t nt, const uint8_t* mask, cudaStream_t st);
 };
 
+// Tap weights of one sample: lane i < w*d computes the weight of tap (i % w)
+// of dimension i / w; the first tap index per dimension is l0[d].
+// u = k M (float32 k, integer M < 2^24) is carried exactly as uh + ul with
+// ul = fma(k, M, -uh), so the first tap l = ceil(u - w/2) is exact and the
+// kernel argument z = (l + t - u) / (w/2) is rounded once, all in float32
+// arithmetic (float64 is a small fraction of float32 throughput on this GPU):
+// with f = floor(uh) and r = (uh - f) + ul, u = f + r, r in (-1, 1), so
+// l = f - w/2 + [r > 0] and z = ([r > 0] - w/2 + t - r) / (w/2).
+__device__ __forceinline__ void es_lane_weight(const float* kd, const int64_t* M, int d, int lane, float* wt_out,
+                                               int64_t* l0) {
+  const int hw = kEsWidth / 2;
+  float wt = 0.f;
+#pragma unroll
+  for (int dd = 0; dd < 3; ++dd) {
+    if (dd < d) {
+      const float m = (float)M[dd];
+      const float uh = kd[dd] * m;
+      const float ul = fmaf(kd[dd], m, -uh);
+      const float f = floorf(uh);
+      const float r = (uh - f) + ul;
+      const int c = r > 0.f ? 1 : 0;
+      l0[dd] = (int64_t)f - hw + c;
+      if (lane / kEsWidth == dd) {
+        const int t = lane % kEsWidth;
+        const float z = ((float)(c - hw + t) - r) * (1.f / hw);
+        wt = (fabsf(z) < 1.f) ? expf(kEsBeta * (sqrtf(1.f - z * z) - 1.f)) : 0.f;
+      }
+    }
+  }
+  *wt_out = wt;
+}
+
 // Deconvolution factors 1/psi_hat(j) for j = jmin .. jmin + count - 1 on an upsampled grid of size M.
 int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, DevBuf& out);
 
@@ -60,5 +92,11 @@ struct SpreadDataArgs {
   float2* grid;         // [(c - c0) * K + k][cells]
 };
 int spread_data(const SpreadDataArgs& a, cudaStream_t st);
+
+// Tile-sorted shared-memory spreading of 2D grids (spread_tiles.cu); used by
+// spread_data / spread_lambda when tiles_applicable().
+bool tiles_applicable(const SampleSet& S, int d, const void* U);
+int spread_data_tiled(const SpreadDataArgs& a, cudaStream_t st);
+int spread_lambda_tiled(const SpreadLambdaArgs& a, cudaStream_t st);
 
 }  // namespace mrsr

@@ -117,7 +117,7 @@ def request_bytes(img, K, nc, precision="fp32", refine=False):
     vec = nimg * K * 8
     esz = 4 if precision == "fp16" else 8
     per_coil = K * 2 * img[0] * _prod(img[1:]) * esz
-    cg = min(nc, max(1, (48 << 20) // per_coil)) if len(img) == 2 else 1
+    cg = min(nc, max(1, (112 << 20) // per_coil)) if len(img) == 2 else 1
     stacks = per_coil * cg
     if len(img) == 3:
         stacks += K * 4 * img[0] * img[1] * img[2] * esz * cg
