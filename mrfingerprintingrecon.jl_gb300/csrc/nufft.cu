@@ -199,11 +199,146 @@ __global__ void __launch_bounds__(256) k_spread_data(SpreadDataArgs a) {
   }
 }
 
+// Channel-last spreading: the grid is [cell][channel] with an even channel
+// count, one warp per sample, and each lane adds two consecutive channels with
+// one float4 atomic, so a warp's atomic instruction covers 64 consecutive
+// channels of one cell (whole cache lines) instead of 32 scattered cells.
+// kCl channel values per lane are kept in registers for all taps.
+constexpr int kClPairs = 4;  // up to 2 * 32 * kClPairs = 256 channels
+template <class VAL>
+__device__ __forceinline__ void spread_cl_sample(const SampleSet& S, const int64_t* M, int64_t li, int nch,
+                                                 float extra_w, VAL val, float2* gcl) {
+  const int lane = threadIdx.x & 31;
+  const int d = S.d;
+  const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
+  float kd[3] = {0.f, 0.f, 0.f};
+  for (int dd = 0; dd < d; ++dd) kd[dd] = S.trj[dd + (int64_t)d * li];
+  float wt;
+  int64_t l0[3] = {0, 0, 0};
+  es_lane_weight(kd, M, d, lane, &wt, l0);
+  float4 v[kClPairs];
+#pragma unroll
+  for (int b = 0; b < kClPairs; ++b) {
+    const int ch = 2 * (lane + 32 * b);
+    float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+    if (ch < nch) a0 = val(ch);
+    if (ch + 1 < nch) a1 = val(ch + 1);
+    v[b] = make_float4(a0.x * extra_w, a0.y * extra_w, a1.x * extra_w, a1.y * extra_w);
+  }
+  for (int tt = 0; tt < ntap; ++tt) {
+    const int t1 = tt % kEsWidth, t2 = (tt / kEsWidth) % kEsWidth, t3 = tt / (kEsWidth * kEsWidth);
+    float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
+    if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
+    if (w == 0.f) continue;
+    int64_t cell = wrap(l0[0] + t1, M[0]) + M[0] * wrap(l0[1] + t2, M[1]);
+    if (d == 3) cell += M[0] * M[1] * wrap(l0[2] + t3, M[2]);
+    float2* row = gcl + cell * nch;
+#pragma unroll
+    for (int b = 0; b < kClPairs; ++b) {
+      const int ch = 2 * (lane + 32 * b);
+      if (ch < nch)
+        atomicAdd(reinterpret_cast<float4*>(row + ch), make_float4(v[b].x * w, v[b].y * w, v[b].z * w, v[b].w * w));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_spread_data_cl(SpreadDataArgs a, int nch, float2* gcl) {
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t ns_tot = a.S.ns_pf * a.S.nt;
+  for (int64_t n = warp; n < a.S.n; n += nwarps) {
+    const int64_t li = sample_lin(a.S, n);
+    const int64_t t = li / a.S.ns_pf;
+    float dcf = 1.f;
+    if (a.dcf_kind == MRSR_DCF_RADIAL_3D || a.dcf_kind == MRSR_DCF_RADIAL_2D) {
+      float s2 = 0.f;
+      for (int dd = 0; dd < a.S.d; ++dd) {
+        const float k = a.S.trj[dd + (int64_t)a.S.d * li];
+        s2 = __fadd_rn(s2, __fmul_rn(k, k));
+      }
+      dcf = a.dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
+    } else if (a.dcf_kind == MRSR_DCF_ARRAY) {
+      dcf = a.dcf[n];
+    }
+    spread_cl_sample(a.S, a.M, li, nch, dcf, [&](int ch) -> float2 {
+      if (ch >= a.nc * a.K) return make_float2(0.f, 0.f);  // row padding
+      const int c = ch / a.K, k = ch - c * a.K;
+      const float2 y = a.data[li + ns_tot * (a.c0 + c)];
+      if (a.u_complex) return cmulc(y, reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k]);
+      const float uu = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
+      return make_float2(y.x * uu, y.y * uu);
+    }, gcl);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_spread_lambda_cl(SpreadLambdaArgs a, int nch, float2* gcl) {
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t n = warp; n < a.S.n; n += nwarps) {
+    const int64_t li = sample_lin(a.S, n);
+    const int64_t t = li / a.S.ns_pf;
+    spread_cl_sample(a.S, a.M, li, nch, 1.f, [&](int ch) -> float2 {
+      if (ch >= a.np) return make_float2(0.f, 0.f);  // row padding
+      // packed pair p0 + ch -> (k1, k2), k1 <= k2
+      int p = a.p0 + ch, k2 = 0;
+      while (p > k2) {
+        p -= k2 + 1;
+        ++k2;
+      }
+      const int k1 = p;
+      float2 u1, u2;
+      if (a.u_complex) {
+        u1 = reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k1];
+        u2 = reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k2];
+      } else {
+        u1 = make_float2(reinterpret_cast<const float*>(a.U)[t + a.S.nt * k1], 0.f);
+        u2 = make_float2(reinterpret_cast<const float*>(a.U)[t + a.S.nt * k2], 0.f);
+      }
+      return cmulc(u2, u1);  // conj(U[t,k1]) * U[t,k2]
+    }, gcl);
+  }
+}
+
+// [cell][nch] -> [ch][cell] through 32 x 32 shared-memory tiles
+__global__ void k_cl_to_planes(const float2* gcl, int nch, int nout, int64_t cells, float2* out) {
+  __shared__ float2 tile[32][33];
+  const int64_t c0 = (int64_t)blockIdx.x * 32;
+  const int h0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int64_t cell = c0 + r;
+    const int ch = h0 + threadIdx.x;
+    if (cell < cells && ch < nch) tile[r][threadIdx.x] = gcl[cell * nch + ch];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int ch = h0 + r;
+    const int64_t cell = c0 + threadIdx.x;
+    if (cell < cells && ch < nout) out[(int64_t)ch * cells + cell] = tile[threadIdx.x][r];
+  }
+}
+
 static unsigned spread_blocks(int64_t n) { return (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(n * 32, 256), 1), 152 * 64); }
+
+// channel-last spreading into a scratch [cell][channel] grid, then transposed to a.grid
+static int spread_cl_finish(float2* gcl, int nch, int nout, int64_t cells, float2* grid, cudaStream_t st) {
+  const dim3 g((unsigned)cdiv(cells, 32), (unsigned)cdiv(nout, 32));
+  k_cl_to_planes<<<g, dim3(32, 8), 0, st>>>(gcl, nch, nout, cells, grid);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
 
 int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
   if (tiles_applicable(a.S, a.S.d, a.U) && a.K <= 8) return spread_lambda_tiled(a, st);
+  if (a.np >= 160 && a.np <= 64 * kClPairs) {  // see spread_data
+    const int nchp = a.np + (a.np & 1);
+    DevBuf gcl;
+    MRSR_TRY(gcl.alloc(sizeof(float2) * a.cells * nchp));
+    MRSR_CHECK_CUDA(cudaMemsetAsync(gcl.p, 0, gcl.bytes, st));
+    k_spread_lambda_cl<<<spread_blocks(a.S.n), 256, 0, st>>>(a, nchp, gcl.as<float2>());
+    MRSR_LAUNCH_CHECK();
+    return spread_cl_finish(gcl.as<float2>(), nchp, a.np, a.cells, a.grid, st);
+  }
   k_spread_lambda<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
@@ -212,6 +347,18 @@ int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
 int spread_data(const SpreadDataArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
   if (tiles_applicable(a.S, a.S.d, a.U)) return spread_data_tiled(a, st);
+  // channel-last pays off for many channels (GB300, 2D radial: 100 channels 8.6 ms vs
+  // 5.7 ms for the scattered kernel, 192 channels 20.5 ms vs 31 ms)
+  const int nch = a.nc * a.K;
+  if (a.U && nch >= 160 && nch <= 64 * kClPairs) {
+    const int nchp = nch + (nch & 1);  // float4 atomics need an even row length
+    DevBuf gcl;
+    MRSR_TRY(gcl.alloc(sizeof(float2) * a.cells * nchp));
+    MRSR_CHECK_CUDA(cudaMemsetAsync(gcl.p, 0, gcl.bytes, st));
+    k_spread_data_cl<<<spread_blocks(a.S.n), 256, 0, st>>>(a, nchp, gcl.as<float2>());
+    MRSR_LAUNCH_CHECK();
+    return spread_cl_finish(gcl.as<float2>(), nchp, nch, a.cells, a.grid, st);
+  }
   k_spread_data<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
