@@ -36,6 +36,8 @@ WORKLOADS = {
 }
 DEFAULT_WORKLOAD = "radial2d_256_nt1000_nc20_k5"
 SERVED = "served_mixed_500"
+PIPE3D = "radial3d_128_nt800_nc16_k5"
+PIPEGROG = "grog_cart256_nt500_nc32_k6"
 L2_FLUSH_BYTES = 256 << 20   # > 129 MB L2
 
 
@@ -45,7 +47,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SERVED])
+    p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SERVED, PIPE3D, PIPEGROG])
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "refined"],
                    help="operator storage: fp32, fp16 (per-tile scaled half stacks and kernel); "
                         "refined (served workload only: fp16 inner CG + float32 residual steps)")
@@ -209,6 +211,10 @@ def reference_arm(args, world, rank):
     if args.workload == SERVED:
         print(json.dumps({"impl": "reference", "unavailable": "the reference package has no request server; "
                           "its per-reconstruction CPU path is timed by the apply workloads"}), flush=True)
+        return
+    if args.workload in (PIPE3D, PIPEGROG):
+        print(json.dumps({"impl": "reference", "unavailable": "stage timings of the GPU pipeline only; the CPU "
+                          "restatement is timed on the 2D apply workloads"}), flush=True)
         return
     w = WORKLOADS[args.workload]
     # inputs from the oracle's own restatements only (no package code on this arm)
@@ -446,6 +452,129 @@ def served_arm(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------ pipeline workloads ---
+def _events_ms(fn, reps, stream):
+    """Mean device milliseconds of fn() over reps calls (CUDA events on `stream`)."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _wall_ms(fn, reps):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        fn()
+    torch.cuda.synchronize()
+    return 1e3 * (time.perf_counter() - t0) / reps
+
+
+def pipeline_arm(args, world, rank, local):
+    """The other benchmark configurations, stage by stage (one process per GPU, replicas).
+
+    radial3d_128_nt800_nc16_k5: 128^3 koosh-ball golden means, Nt=800 x 24 spokes x 256
+      samples, 16 coils, K=5.  Stages: Λ/kmask precompute, forward model, backprojection,
+      apply (float32 and fp16 storage), 20 CG iterations, refinement.  `value` = float32
+      applies/s; the fp16 operator's applies/s and its difference from the float32 apply
+      on the phantom are reported beside it.
+    grog_cart256_nt500_nc32_k6: 256^2 radial, Nt=500 x 2 spokes x 512 samples, 32 coils,
+      K=6.  Stages: grog_calib, grog_gridding!, FFTNormalOp from the gridded trajectory,
+      Cartesian backprojection, 20 CG iterations.  `value` = FFTNormalOp applies/s.
+    Inputs are seeded synthetic data (forward model + 1% noise).  Stage times are CUDA
+    events on the launching stream after one untimed run of every stage (L2 not flushed:
+    every stage streams far more than the 129 MB L2).
+    """
+    import torch
+    import __graft_entry__ as ge
+    mr = ge.package()
+    stream = torch.cuda.current_stream()
+    syn, tr = mr.synthetic, mr.trajectories
+    reps = max(1, args.steps)
+    st = {}
+    if args.workload == PIPE3D:
+        N, Nr, Ncyc, Nt, Nc, K = 128, 256, 24, 800, 16, 5
+        img = (N, N, N)
+        trj = mr.to_jl(tr.traj_kooshball_goldenratio(Nr, Ncyc, Nt), torch.float32)
+        D = syn.dictionary(Nt, seed=42 + rank)
+        U = mr.to_jl(syn.basis(D, K), torch.float32)
+        cm = mr.to_jl(syn.coil_maps(img, Nc, seed=42 + rank), torch.complex64)
+        x = mr.to_jl(syn.phantom(img, D, mr.to_host(U), seed=42 + rank), torch.complex64)
+        A = mr.NFFTNormalOp(img, trj, U, cmaps=cm)                      # untimed first call
+        st["lambda_kmask"] = _wall_ms(lambda: mr.NFFTNormalOp(img, trj, U, cmaps=cm).close(), 1)
+        data = mr.forward_model(x, trj, U, cmaps=cm)
+        st["forward_model"] = _events_ms(lambda: mr.forward_model(x, trj, U, cmaps=cm), 1, stream)
+        data = syn.add_noise(data, 0.01)
+        b = mr.calculate_backprojection(data, trj, cm, U=U)
+        st["backprojection"] = _events_ms(lambda: mr.calculate_backprojection(data, trj, cm, U=U), 1, stream)
+        A16 = A.share(cmaps=cm, precision="fp16")
+        y32 = mr.jl_empty(x.shape, torch.complex64)
+        y16 = mr.jl_empty(x.shape, torch.complex64)
+        for _ in range(max(args.warmup, 3)):
+            A.mul(y32, x)
+            A16.mul(y16, x)
+        ms32 = _events_ms(lambda: A.mul(y32, x), reps, stream)
+        ms16 = _events_ms(lambda: A16.mul(y16, x), reps, stream)
+        st["apply_fp32"], st["apply_fp16"] = ms32, ms16
+        diff = float(torch.linalg.vector_norm(y16 - y32) / torch.linalg.vector_norm(y32))
+        st["cg20_fp32"] = _events_ms(lambda: mr.cg(A, b, maxiter=20, reltol=0.0), 1, stream)
+        res = mr.cg_refined(A16, A, b, inner_iters=20, max_outer=2, tol=0.0, log=True)
+        st["refined_2x20_fp16"] = _events_ms(lambda: mr.cg_refined(A16, A, b, inner_iters=20, max_outer=2, tol=0.0),
+                                             1, stream)
+        value, unit = 1000.0 / ms32, "applies/s"
+        extra = {"fp16_applies_s": 1000.0 / ms16, "fp16_vs_fp32_apply_rel_l2": diff,
+                 "refined_relres_after_2x20": res.resnorm}
+        cfg = {"workload": PIPE3D, "img": list(img), "Nr": Nr, "Ncyc": Ncyc, "Nt": Nt, "Nc": Nc, "K": K,
+               "trajectory": "koosh-ball golden means", "samples": Nr * Ncyc * Nt}
+    else:
+        N, Nr, Ncyc, Nt, Nc, K = 256, 512, 2, 500, 32, 6
+        img = (N, N)
+        trj = mr.to_jl(tr.traj_2d_radial_goldenratio(Nr, Ncyc, Nt), torch.float32)
+        D = syn.dictionary(Nt, seed=42 + rank)
+        U = mr.to_jl(syn.basis(D, K), torch.float32)
+        cm = mr.to_jl(syn.coil_maps(img, Nc, seed=42 + rank), torch.complex64)
+        x = mr.to_jl(syn.phantom(img, D, mr.to_host(U), seed=42 + rank), torch.complex64)
+        data0 = syn.add_noise(mr.forward_model(x, trj, U, cmaps=cm), 0.01)
+        import warnings
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")  # 1000 spokes < 32^2: the reference warns that calibration is ill posed
+            lnG = mr.grog_calib(data0, trj, Nr)
+            st["grog_calib"] = _events_ms(lambda: mr.grog_calib(data0, trj, Nr), 1, stream)
+            data = data0.clone()
+            trj_c = mr.grog_gridding(data, trj, lnG, Nr, img)
+            work = data0.clone()
+            st["grog_gridding"] = _events_ms(lambda: mr.grog_gridding(work, trj, lnG, Nr, img), 1, stream)
+        A = mr.FFTNormalOp(img, trj_c, U, cmaps=cm)
+        st["fft_normalop_create"] = _wall_ms(lambda: mr.FFTNormalOp(img, trj_c, U, cmaps=cm).close(), 1)
+        b = mr.calculate_backprojection(data, trj_c, cm, U=U)
+        st["backprojection_cartesian"] = _events_ms(lambda: mr.calculate_backprojection(data, trj_c, cm, U=U), 1,
+                                                   stream)
+        y = mr.jl_empty(x.shape, torch.complex64)
+        for _ in range(max(args.warmup, 3)):
+            A.mul(y, x)
+        ms = _events_ms(lambda: A.mul(y, x), reps, stream)
+        st["apply"] = ms
+        st["cg20"] = _events_ms(lambda: mr.cg(A, b, maxiter=20, reltol=0.0), 1, stream)
+        value, unit = 1000.0 / ms, "applies/s"
+        extra = {}
+        cfg = {"workload": PIPEGROG, "img": list(img), "Nr": Nr, "Ncyc": Ncyc, "Nt": Nt, "Nc": Nc, "K": K,
+               "operator": "FFTNormalOp after GROG gridding"}
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": world * value, "unit": unit, "n_gpus": world, "steps": reps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded phantom, dictionary basis, coil maps, 1% noise)",
+            "config": {**cfg, "parallelism": f"replicas x{world}", "l2": "not flushed; every stage streams > 129 MB"},
+            "stages_ms": {k: round(v, 4) for k, v in st.items()}, **extra}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args.gpus)
@@ -453,6 +582,8 @@ def main():
         reference_arm(args, world, rank)
     elif args.workload == SERVED:
         served_arm(args, world, rank, local)
+    elif args.workload in (PIPE3D, PIPEGROG):
+        pipeline_arm(args, world, rank, local)
     else:
         gb300_arm(args, world, rank, local)
     if world > 1:

@@ -203,20 +203,35 @@ __global__ void __launch_bounds__(1024) k_grog_solve_log(LogArgs a) {
     Y[e] = T1[j + n * i];
   }
   __syncthreads();
-  // inverse scaling: square roots (Denman-Beavers) until ||Y - I||_F <= 0.25
+  // inverse scaling: square roots until ||Y - I||_F <= 0.25, each by the product form of
+  // the Denman-Beavers iteration (Cheng, Higham, Kenney and Laub, SIAM J. Matrix Anal.
+  // Appl. 22, 2001): M0 = Y0 = A, Y <- Y (I + M^{-1}) / 2, M <- I/2 + (M + M^{-1}) / 4;
+  // Y -> A^{1/2} and M -> I quadratically.  One inversion per step, and the stopping
+  // test ||M - I||_F^2 <= 1e-26 n is scale free (M tends to I whatever the size of A).
   int s = 0;
   while (s < 40 && dist_eye2(Y, n, red) > 0.0625) {
-    mat_eye(Z, n);
+    mat_copy(Z, Y, n);  // M
     for (int it = 0; it < 60; ++it) {
-      mat_inv(T1, Y, M, n, &piv);   // Y^{-1}
-      mat_inv(T2, Z, M, n, &piv);   // Z^{-1}
+      mat_inv(T1, Z, M, n, &piv);  // M^{-1}
+      for (int e = threadIdx.x; e < nn; e += blockDim.x) {  // T2 = Y (I + M^{-1})
+        const int i = e % n, j = e / n;
+        double2 acc = Y[i + n * j];
+        for (int l = 0; l < n; ++l) {
+          const double2 u = Y[i + n * l], v = T1[l + n * j];
+          acc.x += u.x * v.x - u.y * v.y;
+          acc.y += u.x * v.y + u.y * v.x;
+        }
+        T2[e] = acc;
+      }
+      __syncthreads();
       double dacc = 0.0;
       for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-        const double2 yn = make_double2(0.5 * (Y[e].x + T2[e].x), 0.5 * (Y[e].y + T2[e].y));
-        const double2 zn = make_double2(0.5 * (Z[e].x + T1[e].x), 0.5 * (Z[e].y + T1[e].y));
-        dacc += zabs2(zsub(yn, Y[e]));
-        Y[e] = yn;
-        Z[e] = zn;
+        const bool diag = (e % n) == (e / n);
+        Y[e] = make_double2(0.5 * T2[e].x, 0.5 * T2[e].y);
+        double2 m = make_double2(0.25 * (Z[e].x + T1[e].x) + (diag ? 0.5 : 0.0), 0.25 * (Z[e].y + T1[e].y));
+        Z[e] = m;
+        if (diag) m.x -= 1.0;
+        dacc += zabs2(m);
       }
       for (int o = 16; o > 0; o >>= 1) dacc += __shfl_down_sync(0xffffffffu, dacc, o);
       if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dacc;
@@ -224,7 +239,7 @@ __global__ void __launch_bounds__(1024) k_grog_solve_log(LogArgs a) {
       double tot = 0.0;
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
       __syncthreads();
-      if (tot < 1e-28 * n) break;
+      if (tot < 1e-26 * n) break;
     }
     ++s;
   }
