@@ -51,10 +51,12 @@ struct HalfArgs {
   __half2* st1;      // rows output / Λ-pass (2D) stack
   __half2* st2;      // 3D dim-2 stack
   HalfTiles t;
+  // divisions of the per-element scale lookups (all operands < 2^31)
+  FastDiv fd_rpc, fd_noo, fd_tcm, fd_tc, fd_n2, fd_fc;
 };
 
 // ------------------------------------------------------------ rows forward ---
-template <class SP>
+template <class SP, bool PR>
 __global__ void __launch_bounds__(512) kh_rows_fwd(HalfArgs a, Slots sl) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   extern __shared__ float2 smem[];
@@ -68,11 +70,11 @@ __global__ void __launch_bounds__(512) kh_rows_fwd(HalfArgs a, Slots sl) {
   const int64_t row0 = rb * a.t.rpc;
   const int nr = (int)min((int64_t)a.t.rpc, a.nrows - row0);
   const int NO = a.t.rpc * a.K;
-  const int nload = (a.n1 * 2 == L) ? R1 / 2 : R1;
+  constexpr int nload = PR ? R1 / 2 : R1;
   __syncthreads();
   step_a<SP, -1>(sm, sl, NO, tw, nload, [&](int lo, int, int n) -> float2 {
     const int rl = lo / a.K, k = lo - rl * a.K;
-    if (rl >= nr || n >= a.n1) return make_float2(0.f, 0.f);
+    if (rl >= nr || (!PR && n >= a.n1)) return make_float2(0.f, 0.f);
     const int64_t r = row0 + rl;
     float2 v = a.x[n + (int64_t)a.n1 * (r + a.nrows * k)];
     if (a.cmaps) v = cmul(a.cmaps[n + (int64_t)a.n1 * (r + a.nrows * c)], v);
@@ -98,7 +100,7 @@ __global__ void __launch_bounds__(512) kh_rows_fwd(HalfArgs a, Slots sl) {
 
 // ---------------------------------------------------------- dim-2 passes ---
 // forward: st1 (g1, n2, n3) -> st2 (g1, g2, n3);  inverse: st2 -> st1
-template <class SP, int S>
+template <class SP, int S, bool PR>
 __global__ void __launch_bounds__(512) kh_mid(HalfArgs a, Slots sl) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   extern __shared__ float2 smem[];
@@ -115,18 +117,18 @@ __global__ void __launch_bounds__(512) kh_mid(HalfArgs a, Slots sl) {
   const int nin = S < 0 ? (int)a.n2 : L, nout = S < 0 ? L : (int)a.n2;
   const __half2* ib = (S < 0 ? a.st1 : a.st2) + (p * a.n3 + o0) * nin * a.g1 + col0;
   __half2* ob_ = (S < 0 ? a.st2 : a.st1) + (p * a.n3 + o0) * nout * a.g1 + col0;
-  const int nload = (nin * 2 == L) ? R1 / 2 : R1;
-  const int nkeep = (nout * 2 == L) ? R2 / 2 : R2;
+  constexpr int nload = (PR && S < 0) ? R1 / 2 : R1;
+  constexpr int nkeep = (PR && S > 0) ? R2 / 2 : R2;
   __syncthreads();
   step_a<SP, S>(sm, sl, a.t.NOo, tw, nload, [&](int o, int li, int n) -> float2 {
-    if (o >= no || n >= nin) return make_float2(0.f, 0.f);
+    if (o >= no || (!(PR && S < 0) && n >= nin)) return make_float2(0.f, 0.f);
     float s;
     if (S < 0) {  // producer: rows forward, row r = n + n2 (o0 + o)
-      const int64_t r = n + a.n2 * (o0 + o);
-      s = a.t.s_rows[(int64_t)cl * a.t.nrowblk + r / a.t.rpc];
+      const uint32_t r = (uint32_t)(n + a.n2 * (o0 + o));
+      s = a.t.s_rows[(int64_t)cl * a.t.nrowblk + a.fd_rpc.div(r)];
     } else {      // producer: Λ pass, inner = (col0 + li) + g1 * n
-      const int64_t inner = col0 + li + a.g1 * n;
-      s = a.t.s_lam[(int64_t)cl * a.ntiles + inner / a.TC];
+      const uint32_t inner = (uint32_t)(col0 + li + a.g1 * n);
+      s = a.t.s_lam[(int64_t)cl * a.ntiles + a.fd_tc.div(inner)];
     }
     return ld_h(ib, ((int64_t)o * nin + n) * a.g1 + li, s);
   });
@@ -206,7 +208,26 @@ __device__ __forceinline__ void lam_apply_half(int mode, int K, const void* lamv
   }
 }
 
-template <class SP>
+template <class SP, int KK>
+__device__ __forceinline__ void lam_voxels_half(const HalfArgs& a, float2* sm, const Slots& sl, int64_t tile, float ls) {
+  constexpr int R1 = SP::R1, L = SP::L;
+  const int64_t pstride = (int64_t)a.FC * a.TC;
+  for (int t = threadIdx.x; t < (L << sl.tcs); t += blockDim.x) {
+    const int li = t & (a.TC - 1);
+    const int f = t >> sl.tcs;  // f = f1 + R1 f2
+    const int f1 = f % R1, f2 = f / R1;
+    float2 X[KK], Y[KK];
+#pragma unroll
+    for (int k = 0; k < KK; ++k) X[k] = sm[sl.at(k, f1, f2, li, R1)];
+    const int ch = (int)a.fd_fc.div((uint32_t)f), fc = f - ch * a.FC;
+    const int64_t lbase = (((tile * a.NCH + ch) * a.P) * (int64_t)a.FC + fc) * a.TC + li;
+    lam_apply_half<KK>(a.lam_mode, KK, a.lam, lbase, pstride, ls, X, Y);
+#pragma unroll
+    for (int k = 0; k < KK; ++k) sm[sl.at(k, f1, f2, li, R1)] = Y[k];
+  }
+}
+
+template <class SP, bool PR>
 __global__ void __launch_bounds__(256, 2) kh_lambda(HalfArgs a, Slots sl) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   extern __shared__ float2 smem[];
@@ -220,17 +241,18 @@ __global__ void __launch_bounds__(256, 2) kh_lambda(HalfArgs a, Slots sl) {
   const int64_t plane = (int64_t)a.nlast * a.inner;
   __half2* stack = a.d == 2 ? a.st1 : a.st2;
   __half2* base = stack + (int64_t)cl * a.K * plane + tile * a.TC;
-  const int nload = (a.nlast * 2 == L) ? R1 / 2 : R1;
-  const int nkeep = (a.nlast * 2 == L) ? R1 / 2 : R1;
+  constexpr int nload = PR ? R1 / 2 : R1;
+  constexpr int nkeep = PR ? R1 / 2 : R1;
+  // 3D: the tile's TC columns lie in one dim-2 column tile (TC and TCm are powers of two dividing g1)
+  const int mt = a.d == 3 ? (int)(((tile * a.TC) % a.g1) / a.t.TCm) : 0;
   __syncthreads();
   step_a<SP, -1>(sm, sl, a.K, tw, nload, [&](int k, int li, int n) -> float2 {
-    if (n >= a.nlast) return make_float2(0.f, 0.f);
+    if (!PR && n >= a.nlast) return make_float2(0.f, 0.f);
     float s;
     if (a.d == 2) {  // producer: rows forward, row n
-      s = a.t.s_rows[(int64_t)cl * a.t.nrowblk + n / a.t.rpc];
-    } else {         // producer: dim-2 forward, plane (cl,k), slab n / NOo, column tile f1 / TCm
-      const int64_t f1 = (tile * a.TC + li) % a.g1;
-      s = a.t.s_mid[(((int64_t)cl * a.K + k) * a.t.nslab + n / a.t.NOo) * a.t.nmtile + f1 / a.t.TCm];
+      s = a.t.s_rows[(int64_t)cl * a.t.nrowblk + a.fd_rpc.div((uint32_t)n)];
+    } else {         // producer: dim-2 forward, plane (cl,k), slab n / NOo, column tile mt
+      s = a.t.s_mid[(((int64_t)cl * a.K + k) * a.t.nslab + a.fd_noo.div((uint32_t)n)) * a.t.nmtile + mt];
     }
     return ld_h(base, k * plane + (int64_t)n * a.inner + li, s);
   });
@@ -238,19 +260,15 @@ __global__ void __launch_bounds__(256, 2) kh_lambda(HalfArgs a, Slots sl) {
   step_b<SP, -1>(sm, sl, a.K, R2, [&](int lo, int li, int f1, int f2, float2 v) { sm[sl.at(lo, f1, f2, li, R1)] = v; });
   __syncthreads();
   const float ls = a.lam_scale[tile];
-  for (int t = threadIdx.x; t < (L << sl.tcs); t += blockDim.x) {
-    const int li = t & (a.TC - 1);
-    const int r = t >> sl.tcs;
-    const int f1 = r % R1, f2 = r / R1;
-    const int f = f1 + R1 * f2;
-    float2 X[KMAX], Y[KMAX];
-#pragma unroll
-    for (int k = 0; k < KMAX; ++k) X[k] = (k < a.K) ? sm[sl.at(k, f1, f2, li, R1)] : make_float2(0.f, 0.f);
-    const int64_t lbase = lam_elem(tile, f, li, 0, a.TC, a.P, a.FC, a.NCH);
-    lam_apply_half<KMAX>(a.lam_mode, a.K, a.lam, lbase, (int64_t)a.FC * a.TC, ls, X, Y);
-#pragma unroll
-    for (int k = 0; k < KMAX; ++k)
-      if (k < a.K) sm[sl.at(k, f1, f2, li, R1)] = Y[k];
+  switch (a.K) {
+    case 1: lam_voxels_half<SP, 1>(a, sm, sl, tile, ls); break;
+    case 2: lam_voxels_half<SP, 2>(a, sm, sl, tile, ls); break;
+    case 3: lam_voxels_half<SP, 3>(a, sm, sl, tile, ls); break;
+    case 4: lam_voxels_half<SP, 4>(a, sm, sl, tile, ls); break;
+    case 5: lam_voxels_half<SP, 5>(a, sm, sl, tile, ls); break;
+    case 6: lam_voxels_half<SP, 6>(a, sm, sl, tile, ls); break;
+    case 7: lam_voxels_half<SP, 7>(a, sm, sl, tile, ls); break;
+    default: lam_voxels_half<SP, 8>(a, sm, sl, tile, ls); break;
   }
   __syncthreads();
   inv_step_a_slots<SP>(sm, sl, a.K, tw);
@@ -259,7 +277,7 @@ __global__ void __launch_bounds__(256, 2) kh_lambda(HalfArgs a, Slots sl) {
   inv_step_b_slots<SP>(sm, sl, a.K, nkeep, [&](int k, int li, int n, float2 v) {
     // output n = g1 + R2 g2 goes back into the task's own column g1 (slot row g2): no other task reads it
     sm[sl.at(k, n / R2, n % R2, li, R1)] = v;
-    if (n < a.nlast) lmax = fmaxf(lmax, amax2(v));
+    if (PR || n < a.nlast) lmax = fmaxf(lmax, amax2(v));
   });
   block_max_commit(&smax, lmax);
   __syncthreads();
@@ -275,7 +293,7 @@ __global__ void __launch_bounds__(256, 2) kh_lambda(HalfArgs a, Slots sl) {
 }
 
 // ------------------------------------------------------------ rows inverse ---
-template <class SP>
+template <class SP, bool PR>
 __global__ void __launch_bounds__(512) kh_rows_inv(HalfArgs a, Slots sl) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   extern __shared__ float2 smem[];
@@ -286,7 +304,7 @@ __global__ void __launch_bounds__(512) kh_rows_inv(HalfArgs a, Slots sl) {
   const int64_t row0 = (int64_t)blockIdx.x * a.t.rpc;
   const int nr = (int)min((int64_t)a.t.rpc, a.nrows - row0);
   const int NO = a.t.rpc * a.ncg;
-  const int nkeep = (a.n1 * 2 == L) ? R2 / 2 : R2;
+  constexpr int nkeep = PR ? R2 / 2 : R2;
   __syncthreads();
   step_a<SP, +1>(sm, sl, NO, tw, R1, [&](int lo, int, int m) -> float2 {
     const int rl = lo / a.ncg, cl = lo - rl * a.ncg;
@@ -294,10 +312,10 @@ __global__ void __launch_bounds__(512) kh_rows_inv(HalfArgs a, Slots sl) {
     const int64_t r = row0 + rl;
     float s;
     if (a.d == 2) {  // producer: Λ pass, column m
-      s = a.t.s_lam[(int64_t)cl * a.ntiles + m / a.TC];
+      s = a.t.s_lam[(int64_t)cl * a.ntiles + a.fd_tc.div((uint32_t)m)];
     } else {         // producer: dim-2 inverse, plane (cl,k), slab i3 / NOo, column tile m / TCm
-      const int64_t i3 = r / a.n2;
-      s = a.t.s_mid2[(((int64_t)cl * a.K + k) * a.t.nslab + i3 / a.t.NOo) * a.t.nmtile + m / a.t.TCm];
+      const uint32_t i3 = a.fd_n2.div((uint32_t)r);
+      s = a.t.s_mid2[(((int64_t)cl * a.K + k) * a.t.nslab + a.fd_noo.div(i3)) * a.t.nmtile + a.fd_tcm.div((uint32_t)m)];
     }
     return ld_h(a.st1, (((int64_t)cl * a.K + k) * a.nrows + r) * L + m, s);
   });
@@ -429,6 +447,12 @@ int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha,
   a.st1 = op->stack1.as<__half2>();
   a.st2 = op->stack2.as<__half2>();
   a.t = tiles_of(op);
+  a.fd_rpc = FastDiv((uint32_t)a.t.rpc);
+  a.fd_noo = FastDiv((uint32_t)a.t.NOo);
+  a.fd_tcm = FastDiv((uint32_t)a.t.TCm);
+  a.fd_tc = FastDiv((uint32_t)op->TC);
+  a.fd_n2 = FastDiv((uint32_t)g.n[1]);
+  a.fd_fc = FastDiv((uint32_t)op->FC);
   a.t.s_rows = op->scale1.as<float>();
   a.t.s_lam = op->scale1.as<float>() + (int64_t)op->Cg * a.t.nrowblk;
   const int64_t n_mid = g.ndims == 3 ? (int64_t)op->Cg * K * a.t.nslab * a.t.nmtile : 1;
@@ -446,7 +470,10 @@ int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha,
       const Slots sl = slots_for(SP::R2, 1);
       const int NO = a.t.rpc * K;
       const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)NO * SP::R1 * sl.W);
-      return launch_h(kh_rows_fwd<SP>, dim3((unsigned)a.t.nrowblk, a.ncg), rthreads(NO * SP::R1), smem, st, a, sl);
+      const dim3 grid((unsigned)a.t.nrowblk, a.ncg);
+      const int thr = std::min(256, rthreads(NO * SP::R1));
+      return a.n1 * 2 == SP::L ? launch_h(kh_rows_fwd<SP, true>, grid, thr, smem, st, a, sl)
+                               : launch_h(kh_rows_fwd<SP, false>, grid, thr, smem, st, a, sl);
     }));
     if (record) record(rec_ctx);
     if (g.ndims == 3) {
@@ -456,7 +483,9 @@ int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha,
         const Slots sl = slots_for(SP::R2, a.t.TCm);
         const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)a.t.NOo * SP::R1 * sl.W);
         dim3 grid((unsigned)a.t.nmtile, (unsigned)a.t.nslab, (unsigned)(a.ncg * K));
-        return launch_h(kh_mid<SP, -1>, grid, rthreads(a.t.NOo * a.t.TCm * SP::R1), smem, st, a, sl);
+        const int thr = rthreads(a.t.NOo * a.t.TCm * SP::R1);
+        return a.n2 * 2 == SP::L ? launch_h(kh_mid<SP, -1, true>, grid, thr, smem, st, a, sl)
+                                 : launch_h(kh_mid<SP, -1, false>, grid, thr, smem, st, a, sl);
       }));
       if (record) record(rec_ctx);
     }
@@ -465,7 +494,9 @@ int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha,
       using SP = decltype(sp);
       const Slots sl = slots_for(SP::R2, a.TC);
       const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)K * SP::R1 * sl.W);
-      return launch_h(kh_lambda<SP>, dim3((unsigned)(a.ntiles * a.ncg)), 256, smem, st, a, sl);
+      const dim3 grid((unsigned)(a.ntiles * a.ncg));
+      return a.nlast * 2 == SP::L ? launch_h(kh_lambda<SP, true>, grid, 256, smem, st, a, sl)
+                                  : launch_h(kh_lambda<SP, false>, grid, 256, smem, st, a, sl);
     }));
     if (record) record(rec_ctx);
     if (g.ndims == 3) {
@@ -475,7 +506,9 @@ int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha,
         const Slots sl = slots_for(SP::R2, a.t.TCm);
         const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)a.t.NOo * SP::R1 * sl.W);
         dim3 grid((unsigned)a.t.nmtile, (unsigned)a.t.nslab, (unsigned)(a.ncg * K));
-        return launch_h(kh_mid<SP, +1>, grid, rthreads(a.t.NOo * a.t.TCm * SP::R1), smem, st, a, sl);
+        const int thr = rthreads(a.t.NOo * a.t.TCm * SP::R1);
+        return a.n2 * 2 == SP::L ? launch_h(kh_mid<SP, +1, true>, grid, thr, smem, st, a, sl)
+                                 : launch_h(kh_mid<SP, +1, false>, grid, thr, smem, st, a, sl);
       }));
       if (record) record(rec_ctx);
     }
@@ -485,7 +518,10 @@ int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha,
       const Slots sl = slots_for(SP::R2, 1);
       const int NO = a.t.rpc * a.ncg;
       const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)NO * SP::R1 * sl.W);
-      return launch_h(kh_rows_inv<SP>, dim3((unsigned)a.t.nrowblk, K), rthreads(NO * SP::R1), smem, st, a, sl);
+      const dim3 grid((unsigned)a.t.nrowblk, K);
+      const int thr = std::min(256, rthreads(NO * SP::R1));
+      return a.n1 * 2 == SP::L ? launch_h(kh_rows_inv<SP, true>, grid, thr, smem, st, a, sl)
+                               : launch_h(kh_rows_inv<SP, false>, grid, thr, smem, st, a, sl);
     }));
     if (record) record(rec_ctx);
   }
