@@ -5,18 +5,22 @@
 // then lnG[:, i, j] = nm \ v[:, i, j] over all spokes, nm = Nr * (k_2 - k_1).
 // The least squares run in float64 through the normal equations (Gram
 // matrices accumulated in float64, Gauss-Jordan with partial pivoting); the
-// principal matrix logarithm uses inverse scaling and squaring: Denman-Beavers
-// square roots until ||Y - I||_F <= 1/4, then log(I + X) by the m-point
-// Gauss-Legendre quadrature of int_0^1 X (I + t X)^{-1} dt (the diagonal Pade
-// approximant), times 2^s (Higham, Functions of Matrices, SIAM 2008, ch. 11).
+// principal matrix logarithm runs in float32, the precision the reference
+// computes log(G) in, by inverse scaling and squaring: Denman-Beavers square
+// roots until ||Y - I||_F <= 1/4, then log(I + X) by the m-point Gauss-Legendre
+// quadrature of int_0^1 X (I + t X)^{-1} dt (the diagonal Pade approximant),
+// times 2^s (Higham, Functions of Matrices, SIAM 2008, ch. 11).
 //
 // grog_gridding! (src/GROG.jl:73-102): per sample and dimension the grid index
 // follows the reference's float32/float64 promotion bit for bit, and
-// data <- exp(shift lnG_d) data is applied as a Horner-evaluated Taylor series
-// of the action on the Nc x Nrep block (the reference forms the Higham-2005
-// Pade exponential of the float32 matrix and multiplies).
+// data <- exp(shift lnG_d) data is applied as exp(s_j lnG_d) exp((shift - s_j) lnG_d)
+// on the Nc x Nrep block: the first factor from a per-call table over a grid of
+// s_j, the second as a Horner-evaluated Taylor series of its action (the
+// reference forms the Higham-2005 Pade exponential of each float32 matrix and
+// multiplies).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "common.cuh"
@@ -26,22 +30,30 @@ namespace mrsr {
 constexpr int kGrogMaxCoils = 32;
 constexpr int kLogGL = 12;  // Gauss-Legendre nodes of the log quadrature
 
-__device__ __forceinline__ double2 zadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 zsub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ double2 zmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ double2 zconjmul(double2 a, double2 b) {  // conj(a) * b
-  return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ double2 zdiv(double2 a, double2 b) {
-  const double d = b.x * b.x + b.y * b.y;
-  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
-}
-__device__ __forceinline__ double zabs2(double2 a) { return a.x * a.x + a.y * a.y; }
-
 // ------------------------------------------------------- spoke Grams ---
-// A = D1^H D1, B = D1^H D2 for spoke `blockIdx.x`; one thread per (i, j).
+// A = D1^H D1, B = D1^H D2 for spoke `blockIdx.x`; one thread per (i, j).  The sums run on
+// the float32 cores in float-float form: each product is split exactly into p + e (one
+// FMA) and added to a (hi, lo) pair by Knuth's TwoSum, the compensated dot product of
+// Ogita, Rump and Oishi (SIAM J. Sci. Comput. 26, 2005): the result is as accurate as a
+// float64 sum up to a relative n^2 u^2 of sum |d_i d_j| (u = 2^-24), which float64
+// itself only meets to n u_64.  The rounded intrinsics keep the compiler from fusing the
+// product into the following addition, which would lose the exact split.
+struct FF {
+  float hi = 0.f, lo = 0.f;
+};
+__device__ __forceinline__ void ff_madd(FF& s, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  const float e = fmaf(a, b, -p);  // a b = p + e exactly
+  const float t = __fadd_rn(s.hi, p);
+  const float z = __fsub_rn(t, s.hi);
+  const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, z)), __fsub_rn(p, z));  // s.hi + p = t + err
+  s.hi = t;
+  s.lo = __fadd_rn(s.lo, __fadd_rn(err, e));
+}
+__device__ __forceinline__ double ff_value(const FF& s) { return (double)s.hi + (double)s.lo; }
+
+constexpr int kGramRows = 128;  // samples of a spoke staged in shared memory at a time
+
 struct GramArgs {
   const float2* data;   // (ns_pf, nt, nc, nrep)
   int64_t ns_pf, nt;
@@ -49,124 +61,180 @@ struct GramArgs {
   double2* AB;          // [spoke][2][nc][nc] (column-major i + nc j)
 };
 
-__global__ void __launch_bounds__(1024) k_grog_gram(GramArgs a) {
-  extern __shared__ float2 sd[];  // [c][r] spoke samples
+__global__ void __launch_bounds__(1024, 2) k_grog_gram(GramArgs a) {
+  extern __shared__ float2 sd[];  // [row][coil], row stride nc + 1 (conflict-free staging)
+  const int n = a.nc, ld = n + 1;
   const int64_t ip = blockIdx.x;
   const int64_t rep = ip / ((int64_t)a.spf * a.nt);
   const int64_t rem = ip - rep * a.spf * a.nt;
   const int64_t t = rem / a.spf;
   const int64_t sif = rem - t * a.spf;
   const int64_t ns_tot = a.ns_pf * a.nt;
-  for (int e = threadIdx.x; e < a.nr * a.nc; e += blockDim.x) {
-    const int r = e % a.nr, c = e / a.nr;
-    sd[c * a.nr + r] = a.data[(sif * a.nr + r) + a.ns_pf * t + ns_tot * (c + (int64_t)a.nc * rep)];
-  }
-  __syncthreads();
+  const float2* src = a.data + sif * a.nr + a.ns_pf * t + ns_tot * a.nc * rep;  // coil stride ns_tot
   const int i = threadIdx.x % kGrogMaxCoils, j = threadIdx.x / kGrogMaxCoils;
-  if (i < a.nc && j < a.nc) {
-    double2 s1 = make_double2(0, 0), s2 = make_double2(0, 0);
-    for (int r = 0; r + 1 < a.nr; ++r) {
-      const float2 di = sd[i * a.nr + r];
-      const float2 dj = sd[j * a.nr + r];
-      const float2 dj1 = sd[j * a.nr + r + 1];
-      const double2 ci = make_double2(di.x, di.y);
-      s1 = zadd(s1, zconjmul(ci, make_double2(dj.x, dj.y)));
-      s2 = zadd(s2, zconjmul(ci, make_double2(dj1.x, dj1.y)));
+  const bool act = i < n && j < n;
+  FF are, aim, bre, bim;
+  for (int r0 = 0; r0 + 1 < a.nr; r0 += kGramRows) {
+    const int rows = min(kGramRows + 1, a.nr - r0);  // one extra row: B reads sample r + 1
+    __syncthreads();
+    for (int e = threadIdx.x; e < rows * n; e += blockDim.x) {
+      const int r = e % rows, c = e / rows;
+      sd[r * ld + c] = src[r0 + r + ns_tot * c];
     }
+    __syncthreads();
+    if (act) {
+      const int last = min(kGramRows, a.nr - 1 - r0);
+      for (int r = 0; r < last; ++r) {
+        const float2 di = sd[r * ld + i], dj = sd[r * ld + j], dk = sd[(r + 1) * ld + j];
+        // conj(di) dj and conj(di) dk
+        ff_madd(are, di.x, dj.x);
+        ff_madd(are, di.y, dj.y);
+        ff_madd(aim, di.x, dj.y);
+        ff_madd(aim, -di.y, dj.x);
+        ff_madd(bre, di.x, dk.x);
+        ff_madd(bre, di.y, dk.y);
+        ff_madd(bim, di.x, dk.y);
+        ff_madd(bim, -di.y, dk.x);
+      }
+    }
+  }
+  if (act) {
     double2* out = a.AB + ip * 2 * a.nc * a.nc;
-    out[i + a.nc * j] = s1;
-    out[a.nc * a.nc + i + a.nc * j] = s2;
+    out[i + a.nc * j] = make_double2(ff_value(are), ff_value(aim));
+    out[a.nc * a.nc + i + a.nc * j] = make_double2(ff_value(bre), ff_value(bim));
   }
 }
 
 // ------------------------------------------ small dense linear algebra ---
-// All routines: one CTA of 1024 threads, n <= 32, column-major n x n in shared memory.
+// All routines: one CTA, n <= 32, column-major n x n complex matrices in shared
+// memory, templated on the complex type (double2 for the least squares solve,
+// float2 for the logarithm).
 
-// Solve M X = R in place (M destroyed, R <- X), partial pivoting; M, R n x n.
-__device__ void gj_solve(double2* M, double2* R, int n, int* piv_s) {
+template <class C> struct Cx;
+template <> struct Cx<double2> {
+  using R = double;
+  static constexpr double kTiny = 1e-280;  // |pivot|^2 below this: the column is singular
+  static __device__ __forceinline__ double2 mk(double x, double y) { return make_double2(x, y); }
+};
+template <> struct Cx<float2> {
+  using R = float;
+  static constexpr float kTiny = 1e-36f;
+  static __device__ __forceinline__ float2 mk(float x, float y) { return make_float2(x, y); }
+};
+template <class C> __device__ __forceinline__ C cx_zero() { return Cx<C>::mk(0, 0); }
+template <class C> __device__ __forceinline__ C cx_sub(C a, C b) { return Cx<C>::mk(a.x - b.x, a.y - b.y); }
+template <class C> __device__ __forceinline__ C cx_mul(C a, C b) {
+  return Cx<C>::mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <class C> __device__ __forceinline__ typename Cx<C>::R cx_abs2(C a) { return a.x * a.x + a.y * a.y; }
+template <class C> __device__ __forceinline__ C cx_shfl(C v, int src) {
+  return Cx<C>::mk(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// Pivot bookkeeping of one Gauss-Jordan step, double-buffered by step parity.
+template <class C> struct GjStep {
+  C f[2][kGrogMaxCoils];  // column k after the row swap: the elimination multipliers
+  C rinv[2];              // 1 / pivot
+  int p[2];               // pivot row
+  int sing[2];            // |pivot|^2 < kTiny: basic solution with x_k = 0
+};
+
+// Warp-wide pivot choice for column k, lane r holding row r: the first row r >= k of
+// largest modulus (partial pivoting); writes the step record `b`.
+template <class C>
+__device__ __forceinline__ void gj_pivot(C v, int k, int n, GjStep<C>& st, int b) {
+  using R = typename Cx<C>::R;
+  const int lane = threadIdx.x & 31;
+  R best = (lane >= k && lane < n) ? cx_abs2(v) : R(-1);
+  int idx = lane;
+  for (int o = 16; o > 0; o >>= 1) {
+    const R ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (ob > best || (ob == best && oi < idx)) {
+      best = ob;
+      idx = oi;
+    }
+  }
+  int p = __shfl_sync(0xffffffffu, idx, 0);
+  if (p < k || p >= n) p = k;  // non-finite column: keep the row order (indices stay in range)
+  const C vk = cx_shfl(v, k), vp = cx_shfl(v, p);
+  if (lane < n) st.f[b][lane] = lane == p ? vk : v;
+  if (lane == 0) {
+    const R d = cx_abs2(vp);
+    const bool s = !(d >= Cx<C>::kTiny);
+    st.p[b] = p;
+    st.sing[b] = s;
+    st.rinv[b] = s ? cx_zero<C>() : Cx<C>::mk(vp.x / d, -vp.y / d);
+  }
+}
+
+// Solve M X = R in place (R <- X, M destroyed), partial pivoting.  One warp per column of
+// [M | R], lane r holding row r.  At step k only the columns of M right of k and all of R
+// are updated (M's columns <= k are never read again), and the warp that updates column
+// k+1 of M also picks the pivot of step k+1, so a step costs one barrier.
+template <class C>
+__device__ void gj_solve(C* M, C* R, int n, GjStep<C>& st) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (warp == 0) gj_pivot(lane < n ? M[lane] : cx_zero<C>(), 0, n, st, 0);
+  __syncthreads();
   for (int k = 0; k < n; ++k) {
-    if (threadIdx.x == 0) {
-      int p = k;
-      double best = zabs2(M[k + n * k]);
-      for (int r = k + 1; r < n; ++r) {
-        const double v = zabs2(M[r + n * k]);
-        if (v > best) {
-          best = v;
-          p = r;
-        }
+    const int b = k & 1;
+    const int p = st.p[b];
+    const bool sing = st.sing[b] != 0;
+    const C rinv = st.rinv[b];
+    const C f = lane < n ? st.f[b][lane] : cx_zero<C>();
+    for (int c = k + 1 + warp; c < 2 * n; c += nw) {
+      C* col = c < n ? M + n * c : R + n * (c - n);
+      const C vr = lane < n ? col[lane] : cx_zero<C>();
+      const C vk = cx_shfl(vr, k), vp = cx_shfl(vr, p);
+      const C own = lane == p ? vk : vr;  // row `lane` after the swap of rows k and p
+      C nv;
+      if (sing) {
+        nv = lane == k ? (c < n ? vp : cx_zero<C>()) : own;
+      } else {
+        const C rk = cx_mul(vp, rinv);
+        nv = lane == k ? rk : cx_sub(own, cx_mul(f, rk));
       }
-      *piv_s = p;
+      if (lane < n) col[lane] = nv;
+      if (c == k + 1 && c < n) gj_pivot(nv, k + 1, n, st, b ^ 1);
     }
-    __syncthreads();
-    const int p = *piv_s;
-    if (p != k) {
-      for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) {
-        double2* col = c < n ? M + n * c : R + n * (c - n);
-        const double2 tmp = col[k];
-        col[k] = col[p];
-        col[p] = tmp;
-      }
-      __syncthreads();
-    }
-    const double2 pivot = M[k + n * k];
-    __syncthreads();
-    if (zabs2(pivot) < 1e-280) {  // exactly singular column: basic solution with x_k = 0
-      for (int c = threadIdx.x; c < n; c += blockDim.x) R[k + n * c] = make_double2(0.0, 0.0);
-      __syncthreads();
-      continue;
-    }
-    // row k scaled
-    for (int c = threadIdx.x; c < 2 * n; c += blockDim.x) {
-      double2* col = c < n ? M + n * c : R + n * (c - n);
-      col[k] = zdiv(col[k], pivot);
-    }
-    __syncthreads();
-    // eliminate column k from the other rows
-    for (int e = threadIdx.x; e < n * 2 * n; e += blockDim.x) {
-      const int r = e % n, c = e / n;
-      if (r == k) continue;
-      double2* col = c < n ? M + n * c : R + n * (c - n);
-      const double2 f = M[r + n * k];
-      if (c == k) continue;
-      col[r] = zsub(col[r], zmul(f, col[k]));
-    }
-    __syncthreads();
-    for (int r = threadIdx.x; r < n; r += blockDim.x)
-      if (r != k) M[r + n * k] = make_double2(0.0, 0.0);
     __syncthreads();
   }
 }
 
-__device__ void mat_copy(double2* dst, const double2* src, int n) {
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) dst[e] = src[e];
-  __syncthreads();
-}
-__device__ void mat_eye(double2* dst, int n) {
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) dst[e] = make_double2((e % n) == (e / n) ? 1.0 : 0.0, 0.0);
-  __syncthreads();
-}
-// dst = inverse(src) (src preserved through a scratch copy)
-__device__ void mat_inv(double2* dst, const double2* src, double2* scratch, int n, int* piv_s) {
-  mat_copy(scratch, src, n);
-  mat_eye(dst, n);
-  gj_solve(scratch, dst, n, piv_s);
-}
-
-// || Y - I ||_F^2 into *out (thread 0 reduces)
-__device__ double dist_eye2(const double2* Y, int n, double* red) {
-  double acc = 0.0;
+// dst = src^{-1}; src is preserved (copied to scratch first).
+template <class C>
+__device__ void mat_inv(C* dst, const C* src, C* scratch, int n, GjStep<C>& st) {
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    double2 v = Y[e];
-    if ((e % n) == (e / n)) v.x -= 1.0;
-    acc += zabs2(v);
+    scratch[e] = src[e];
+    dst[e] = Cx<C>::mk((e % n) == (e / n) ? 1 : 0, 0);
   }
+  __syncthreads();
+  gj_solve(scratch, dst, n, st);
+}
+
+// Block sum of a per-thread value (all threads receive it).
+template <class R>
+__device__ __forceinline__ R block_sum(R acc, R* red) {
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
-  double s = 0.0;
+  R s = 0;
   for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
   __syncthreads();
   return s;
+}
+
+// || Y - I ||_F^2
+template <class C>
+__device__ typename Cx<C>::R dist_eye2(const C* Y, int n, typename Cx<C>::R* red) {
+  typename Cx<C>::R acc = 0;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    C v = Y[e];
+    if ((e % n) == (e / n)) v.x -= 1;
+    acc += cx_abs2(v);
+  }
+  return block_sum(acc, red);
 }
 
 struct LogArgs {
@@ -178,94 +246,100 @@ struct LogArgs {
   int* err;
 };
 
-// One spoke: X = A^{-1} B, G = X^T, v = log(G).
+// One spoke: X = A^{-1} B in float64 (A is a Gram matrix: its condition number is the
+// square of the data's), G = X^T, v = log(G) in float32 (the reference works in the data's
+// float32 throughout).  Shared memory: the float64 pair (A, B) occupies the first 2 n^2
+// double2 slots, and the six float32 matrices alias them; G is written to the float slot
+// that overlaps A, which is dead once the solve ends.
 __global__ void __launch_bounds__(1024) k_grog_solve_log(LogArgs a) {
-  extern __shared__ double2 sm[];
+  extern __shared__ __align__(16) unsigned char sraw[];
   const int n = a.nc, nn = n * n;
-  double2* M = sm;            // scratch / A
-  double2* Y = sm + nn;       // root iterate
-  double2* Z = sm + 2 * nn;
-  double2* T1 = sm + 3 * nn;
-  double2* T2 = sm + 4 * nn;
-  double2* L = sm + 5 * nn;   // log accumulator
-  __shared__ int piv;
-  __shared__ double red[32];
-  const double2* AB = a.AB + (int64_t)blockIdx.x * 2 * nn;
-  for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-    M[e] = AB[e];
-    T1[e] = AB[nn + e];
+  __shared__ GjStep<double2> std_;
+  __shared__ GjStep<float2> stf;
+  __shared__ float red[32];
+  {
+    double2* Ad = reinterpret_cast<double2*>(sraw);
+    double2* Bd = Ad + nn;
+    const double2* AB = a.AB + (int64_t)blockIdx.x * 2 * nn;
+    for (int e = threadIdx.x; e < 2 * nn; e += blockDim.x) Ad[e] = AB[e];
+    __syncthreads();
+    gj_solve(Ad, Bd, n, std_);  // Bd = A^{-1} B = X
+    float2* Yf = reinterpret_cast<float2*>(sraw) + nn;  // second half of Ad
+    for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      const double2 x = Bd[j + n * i];  // G = X^T
+      Yf[e] = make_float2((float)x.x, (float)x.y);
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  gj_solve(M, T1, n, &piv);  // T1 = A^{-1} B = X
-  // G = X^T
-  for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-    const int i = e % n, j = e / n;
-    Y[e] = T1[j + n * i];
-  }
-  __syncthreads();
+  float2* M = reinterpret_cast<float2*>(sraw);  // scratch
+  float2* Y = M + nn;                           // root iterate
+  float2* Z = M + 2 * nn;
+  float2* T1 = M + 3 * nn;
+  float2* T2 = M + 4 * nn;
+  float2* L = M + 5 * nn;                       // log accumulator
   // inverse scaling: square roots until ||Y - I||_F <= 0.25, each by the product form of
   // the Denman-Beavers iteration (Cheng, Higham, Kenney and Laub, SIAM J. Matrix Anal.
   // Appl. 22, 2001): M0 = Y0 = A, Y <- Y (I + M^{-1}) / 2, M <- I/2 + (M + M^{-1}) / 4;
-  // Y -> A^{1/2} and M -> I quadratically.  One inversion per step, and the stopping
-  // test ||M - I||_F^2 <= 1e-26 n is scale free (M tends to I whatever the size of A).
+  // Y -> A^{1/2} and M -> I quadratically.  With Y = A^{1/2} (I + E), M = (I + E)^2 and the
+  // step maps E to E^2 / 2: once ||M - I||_F^2 <= 1e-8 n, one more step brings E to the
+  // float32 rounding level.
   int s = 0;
-  while (s < 40 && dist_eye2(Y, n, red) > 0.0625) {
-    mat_copy(Z, Y, n);  // M
-    for (int it = 0; it < 60; ++it) {
-      mat_inv(T1, Z, M, n, &piv);  // M^{-1}
+  while (s < 40 && dist_eye2(Y, n, red) > 0.0625f) {
+    for (int e = threadIdx.x; e < nn; e += blockDim.x) Z[e] = Y[e];  // M
+    __syncthreads();
+    bool last = false;
+    for (int it = 0; it < 40; ++it) {
+      mat_inv(T1, Z, M, n, stf);  // M^{-1}
       for (int e = threadIdx.x; e < nn; e += blockDim.x) {  // T2 = Y (I + M^{-1})
         const int i = e % n, j = e / n;
-        double2 acc = Y[i + n * j];
+        float2 acc = Y[i + n * j];
         for (int l = 0; l < n; ++l) {
-          const double2 u = Y[i + n * l], v = T1[l + n * j];
-          acc.x += u.x * v.x - u.y * v.y;
-          acc.y += u.x * v.y + u.y * v.x;
+          const float2 u = Y[i + n * l], v = T1[l + n * j];
+          acc.x = fmaf(u.x, v.x, fmaf(-u.y, v.y, acc.x));
+          acc.y = fmaf(u.x, v.y, fmaf(u.y, v.x, acc.y));
         }
         T2[e] = acc;
       }
       __syncthreads();
-      double dacc = 0.0;
+      float dacc = 0.f;
       for (int e = threadIdx.x; e < nn; e += blockDim.x) {
         const bool diag = (e % n) == (e / n);
-        Y[e] = make_double2(0.5 * T2[e].x, 0.5 * T2[e].y);
-        double2 m = make_double2(0.25 * (Z[e].x + T1[e].x) + (diag ? 0.5 : 0.0), 0.25 * (Z[e].y + T1[e].y));
+        Y[e] = make_float2(0.5f * T2[e].x, 0.5f * T2[e].y);
+        float2 m = make_float2(0.25f * (Z[e].x + T1[e].x) + (diag ? 0.5f : 0.f), 0.25f * (Z[e].y + T1[e].y));
         Z[e] = m;
-        if (diag) m.x -= 1.0;
-        dacc += zabs2(m);
+        if (diag) m.x -= 1.f;
+        dacc += m.x * m.x + m.y * m.y;
       }
-      for (int o = 16; o > 0; o >>= 1) dacc += __shfl_down_sync(0xffffffffu, dacc, o);
-      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dacc;
-      __syncthreads();
-      double tot = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
-      __syncthreads();
-      if (tot < 1e-26 * n) break;
+      const float tot = block_sum(dacc, red);
+      if (last) break;
+      last = tot <= 1e-8f * n;
     }
     ++s;
   }
   if (s >= 40 && threadIdx.x == 0) atomicExch(a.err, 2);
   // log(I + X), X = Y - I:  sum_j w_j X (I + t_j X)^{-1}
   for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-    double2 v = Y[e];
-    if ((e % n) == (e / n)) v.x -= 1.0;
+    float2 v = Y[e];
+    if ((e % n) == (e / n)) v.x -= 1.f;
     Z[e] = v;  // X
-    L[e] = make_double2(0.0, 0.0);
+    L[e] = make_float2(0.f, 0.f);
   }
   __syncthreads();
   for (int q = 0; q < kLogGL; ++q) {
-    const double tq = a.gl_t[q], wq = a.gl_w[q];
+    const float tq = (float)a.gl_t[q], wq = (float)a.gl_w[q];
     // solve (I + t X) W = X  ->  W = (I + t X)^{-1} X = X (I + t X)^{-1} (they commute)
     for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-      double2 v = make_double2(tq * Z[e].x, tq * Z[e].y);
-      if ((e % n) == (e / n)) v.x += 1.0;
+      float2 v = make_float2(tq * Z[e].x, tq * Z[e].y);
+      if ((e % n) == (e / n)) v.x += 1.f;
       M[e] = v;
       T1[e] = Z[e];
     }
     __syncthreads();
-    gj_solve(M, T1, n, &piv);
+    gj_solve(M, T1, n, stf);
     for (int e = threadIdx.x; e < nn; e += blockDim.x) {
-      L[e].x += wq * T1[e].x;
-      L[e].y += wq * T1[e].y;
+      L[e].x = fmaf(wq, T1[e].x, L[e].x);
+      L[e].y = fmaf(wq, T1[e].y, L[e].y);
     }
     __syncthreads();
   }
@@ -273,7 +347,6 @@ __global__ void __launch_bounds__(1024) k_grog_solve_log(LogArgs a) {
   double2* out = a.vth + (int64_t)blockIdx.x * nn;
   for (int e = threadIdx.x; e < nn; e += blockDim.x) out[e] = make_double2(sc * L[e].x, sc * L[e].y);
 }
-
 // nm (nspk x d) and the d x d pseudo-inverse factor P = (nm^T nm)^{-1}; single CTA.
 struct NmArgs {
   const float* trj;   // (d, ns_pf, nt)
@@ -355,67 +428,157 @@ __global__ void k_grog_lng(const double* nm, const double* Pinv, const double2* 
 }
 
 // ----------------------------------------------------------- gridding ---
+// exp(shift L_d) v for every sample, factored as exp(s_j L_d) exp((shift - s_j) L_d) v with
+// s_j = j h the table point nearest the shift: the table exp(s_j L_d), j = -J..J, is built
+// once per call, and the remaining factor, ||(shift - s_j) L_d||_1 <= h ||L_d||_1 / 2 <= 1/2,
+// needs a Taylor polynomial of degree <= 8 instead of a scaled degree-24 series.
+constexpr int kGridTabMax = 8;       // J <= 8: 17 tables of n x n in shared memory
+constexpr int kExpTaylor = 12;       // table entries: ||.||_1 <= 1 after scaling, 1/13! < 2^-32
+constexpr float kGridTol = 7.4505806e-9f;  // 2^-27: Taylor truncation bound of the remainder
+
+// Table of exp(s_j L) for s_j = (blockIdx.x - J) h, one CTA per entry: scaling to
+// ||s_j L / 2^q||_1 <= 1, degree-12 Taylor polynomial by Horner, q squarings (float32,
+// the precision the reference forms its exponentials in).
+struct TabArgs {
+  const float2* lnG;  // (d, nc, nc)
+  int d, dd, n, J;
+  float h, lnorm;     // table spacing, ||L_dd||_1
+  float2* tab;        // [2J + 1][nc][nc]
+};
+
+__global__ void __launch_bounds__(1024) k_grog_exp_table(TabArgs a) {
+  __shared__ float2 Y[kGrogMaxCoils * kGrogMaxCoils], E[kGrogMaxCoils * kGrogMaxCoils],
+      T[kGrogMaxCoils * kGrogMaxCoils];
+  const int n = a.n, nn = n * n;
+  const float s = (float)((int)blockIdx.x - a.J) * a.h;
+  const float nrm = fabsf(s) * a.lnorm;
+  int q = 0;
+  while (nrm > ldexpf(1.f, q) && q < 60) ++q;
+  const float sc = ldexpf(s, -q);
+  for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+    const float2 l = a.lnG[a.dd + (int64_t)a.d * e];
+    Y[e] = make_float2(sc * l.x, sc * l.y);
+    E[e] = make_float2((e % n) == (e / n) ? 1.f : 0.f, 0.f);
+  }
+  __syncthreads();
+  auto matmul = [&](const float2* A, const float2* B) {  // T = A B
+    for (int e = threadIdx.x; e < nn; e += blockDim.x) {
+      const int i = e % n, c = e / n;
+      float2 acc = make_float2(0.f, 0.f);
+      for (int l = 0; l < n; ++l) acc = cadd(acc, cmul(A[i + n * l], B[l + n * c]));
+      T[e] = acc;
+    }
+    __syncthreads();
+  };
+  for (int k = kExpTaylor; k >= 1; --k) {  // E <- I + (Y / k) E
+    matmul(Y, E);
+    const float rk = 1.f / (float)k;
+    for (int e = threadIdx.x; e < nn; e += blockDim.x)
+      E[e] = make_float2(((e % n) == (e / n) ? 1.f : 0.f) + rk * T[e].x, rk * T[e].y);
+    __syncthreads();
+  }
+  for (int r = 0; r < q; ++r) {
+    matmul(E, E);
+    for (int e = threadIdx.x; e < nn; e += blockDim.x) E[e] = T[e];
+    __syncthreads();
+  }
+  float2* out = a.tab + (int64_t)blockIdx.x * nn;
+  for (int e = threadIdx.x; e < nn; e += blockDim.x) out[e] = E[e];
+}
+
 struct GridArgs {
   float2* data;           // (ns_pf, nt, nc, nrep), in place
   const float* trj;       // (d, ns_pf, nt)
   const float2* lnG;      // (d, nc, nc)
+  const float2* tab;      // [2J + 1][nc][nc] for dimension dd
   int32_t* trj_cart;      // (d, ns_pf, nt)
-  int d, nc, nrep;
-  int64_t ns_pf, nt, N[3], nr;
-  float lnorm[3];         // ||lnG_d||_1 (max column sum)
+  int d, dd, nc, nrep, J;
+  int64_t ns_pf, nt, Nd, nr;
+  float h, lnorm;         // table spacing, ||lnG_dd||_1 (max column sum)
 };
 
-// One warp per (sample, frame); lane i owns coil i of every repetition.
-__global__ void __launch_bounds__(256) k_grog_grid(GridArgs a) {
-  __shared__ float2 Ls[3][kGrogMaxCoils * kGrogMaxCoils];
-  const int n = a.nc;
-  for (int e = threadIdx.x; e < a.d * n * n; e += blockDim.x) {
-    const int dd = e / (n * n), ij = e - dd * n * n;
-    Ls[dd][ij] = a.lnG[dd + (int64_t)a.d * ij];  // Ls[d][i + n j] = lnG[d][i, j]
-  }
+// One pass per dimension, in the reference's order.  One warp per (sample, frame); lane i
+// owns coil i of every repetition.  The matrices sit in shared memory column-major:
+// L at [0, n^2), table j at [(j + 1) n^2, (j + 2) n^2).
+__global__ void __launch_bounds__(1024, 1) k_grog_grid(GridArgs a) {
+  extern __shared__ float2 Ls[];
+  const int n = a.nc, nn = n * n, ntab = 2 * a.J + 1;
+  for (int e = threadIdx.x; e < nn; e += blockDim.x) Ls[e] = a.lnG[a.dd + (int64_t)a.d * e];
+  for (int e = threadIdx.x; e < ntab * nn; e += blockDim.x) Ls[nn + e] = a.tab[e];
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int64_t total = a.ns_pf * a.nt;
-  for (int64_t li = warp; li < total; li += nwarps) {
-    double shift[3];
-    for (int dd = 0; dd < a.d; ++dd) {
-      const int64_t Nd = a.N[dd];
-      const float p = __fmul_rn(a.trj[dd + (int64_t)a.d * li], (float)Nd);   // Float32 * Int -> Float32
-      const double t = __dadd_rn((double)p, 0.5);                             // + 1/2 -> Float64
-      const double k = rint(t);                                              // round: ties to even
-      shift[dd] = __ddiv_rn(__dmul_rn(__dsub_rn(k, t), (double)a.nr), (double)Nd);
-      if (lane == 0) a.trj_cart[dd + (int64_t)a.d * li] = (int32_t)((int64_t)k + Nd / 2);
+  // y = M w for the n x n matrix M at `Mat` (lane i gets row i)
+  auto matvec = [&](const float2* Mat, float2 w) {
+    float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
+    for (int j = 0; j < n; j += 2) {
+      const float2 w0 = make_float2(__shfl_sync(0xffffffffu, w.x, j), __shfl_sync(0xffffffffu, w.y, j));
+      const float2 w1 = make_float2(__shfl_sync(0xffffffffu, w.x, j + 1), __shfl_sync(0xffffffffu, w.y, j + 1));
+      if (lane < n) {
+        acc0 = cadd(acc0, cmul(Mat[lane + n * j], w0));
+        if (j + 1 < n) acc1 = cadd(acc1, cmul(Mat[lane + n * (j + 1)], w1));
+      }
     }
+    return cadd(acc0, acc1);
+  };
+  for (int64_t li = warp; li < total; li += nwarps) {
+    const float p = __fmul_rn(a.trj[a.dd + (int64_t)a.d * li], (float)a.Nd);  // Float32 * Int -> Float32
+    const double t = __dadd_rn((double)p, 0.5);                                // + 1/2 -> Float64
+    const double k = rint(t);                                                  // round: ties to even
+    const double shift = __ddiv_rn(__dmul_rn(__dsub_rn(k, t), (double)a.nr), (double)a.Nd);
+    if (lane == 0) a.trj_cart[a.dd + (int64_t)a.d * li] = (int32_t)((int64_t)k + a.Nd / 2);
+    const float s = (float)shift;
+    const int j = max(-a.J, min(a.J, (int)rintf(s / a.h)));
+    const float del = s - (float)j * a.h;
+    const float nrm = fabsf(del) * a.lnorm;
+    int q = 0;  // normally 0: the remainder is within half a table step
+    while (nrm > ldexpf(1.f, q) && q < 20) ++q;
+    const float x = ldexpf(nrm, -q), sq = ldexpf(del, -q);
+    int m = 0;  // smallest degree with x^(m+1) / (m+1)! <= 2^-27
+    for (float tm = x; tm > kGridTol && m < 30;) {
+      ++m;
+      tm *= x / (float)(m + 1);
+    }
+    const float2* Ej = Ls + (int64_t)(j + a.J + 1) * nn;
     for (int rep = 0; rep < a.nrep; ++rep) {
       float2 v = make_float2(0.f, 0.f);
       const int64_t base = li + total * ((int64_t)a.nc * rep);
       if (lane < n) v = a.data[base + total * lane];
-      for (int dd = 0; dd < a.d; ++dd) {
-        const float s = (float)shift[dd];
-        const float nrm = fabsf(s) * a.lnorm[dd];
-        int q = 0;  // scaling: exp(A) = exp(A / 2^q)^(2^q) with ||A / 2^q|| <= 2
-        while (nrm > 2.0f * (float)(1 << q) && q < 20) ++q;
-        const float sq = ldexpf(s, -q);
-        for (int rr = 0; rr < (1 << q); ++rr) {
-          // Horner: w = v + (s/M) L (v + (s/(M-1)) L (... ))
-          float2 w = v;
-          for (int m = 24; m >= 1; --m) {
-            float2 lw = make_float2(0.f, 0.f);
-            for (int j = 0; j < n; ++j) {
-              const float2 wj = make_float2(__shfl_sync(0xffffffffu, w.x, j), __shfl_sync(0xffffffffu, w.y, j));
-              if (lane < n) lw = cadd(lw, cmul(Ls[dd][lane + n * j], wj));
-            }
-            const float c = sq / (float)m;
-            w = make_float2(v.x + c * lw.x, v.y + c * lw.y);
-          }
-          v = w;
+      for (int rr = 0; rr < (1 << q); ++rr) {
+        float2 w = v;  // Horner: w = v + (sq/m) L (v + (sq/(m-1)) L (... ))
+        for (int mm = m; mm >= 1; --mm) {
+          const float2 lw = matvec(Ls, w);
+          const float c = sq / (float)mm;
+          w = make_float2(v.x + c * lw.x, v.y + c * lw.y);
         }
+        v = w;
       }
+      v = matvec(Ej, v);
       if (lane < n) a.data[base + total * lane] = v;
     }
   }
+}
+
+static int grog_sms() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
+// Threads of the per-spoke logarithm CTA (a multiple of 32, 32..1024; env MRSR_GROG_THREADS).
+static unsigned grog_log_threads() {
+  static const unsigned t = [] {
+    const char* e = std::getenv("MRSR_GROG_THREADS");
+    const int v = e ? std::atoi(e) : 256;
+    return (unsigned)std::min(1024, std::max(32, v / 32 * 32));
+  }();
+  return t;
 }
 
 static void gauss_legendre01(int n, std::vector<double>& t, std::vector<double>& w) {
@@ -456,7 +619,6 @@ extern "C" int mrsr_grog_calib(int ndims, int64_t nr, int64_t ns_per_frame, int6
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int spf = (int)(ns_per_frame / nr);
   const int64_t nspk0 = (int64_t)spf * nt, nspk = nspk0 * nrep;
-  MRSR_REQUIRE((size_t)nr * ncoils * sizeof(float2) <= 200 * 1024, MRSR_ERR_UNSUPPORTED, "spoke too long for GROG");
   const int nn = ncoils * ncoils;
   DevBuf AB, vth, nm, Pinv, glt, glw, err;
   MRSR_TRY(AB.alloc(sizeof(double2) * 2 * nn * nspk));
@@ -471,17 +633,15 @@ extern "C" int mrsr_grog_calib(int ndims, int64_t nr, int64_t ns_per_frame, int6
   MRSR_TRY(copy_h2d(glw.p, w.data(), sizeof(double) * kLogGL));
   MRSR_TRY(err.alloc(sizeof(int)));
   MRSR_CHECK_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
-  const size_t smem_g = sizeof(float2) * nr * ncoils;
-  if (smem_g > 48 * 1024)
-    MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_grog_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g));
+  const size_t smem_g = sizeof(float2) * (kGramRows + 1) * (ncoils + 1);
   GramArgs ga{reinterpret_cast<const float2*>(data), ns_per_frame, nt, ncoils, nrep, (int)nr, spf, AB.as<double2>()};
   k_grog_gram<<<(unsigned)nspk, 1024, smem_g, st>>>(ga);
   MRSR_LAUNCH_CHECK();
-  const size_t smem_l = sizeof(double2) * 6 * nn;
-  if (smem_l > 48 * 1024)
-    MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_grog_solve_log, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l));
+  const size_t smem_l = std::max(sizeof(double2) * 2, sizeof(float2) * 6) * nn;
+  // opt in whatever the size: the dynamic part plus the kernel's static pivot records can pass 48 KB
+  MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_grog_solve_log, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l));
   LogArgs la{AB.as<double2>(), ncoils, vth.as<double2>(), glt.as<double>(), glw.as<double>(), err.as<int>()};
-  k_grog_solve_log<<<(unsigned)nspk, 1024, smem_l, st>>>(la);
+  k_grog_solve_log<<<(unsigned)nspk, grog_log_threads(), smem_l, st>>>(la);
   MRSR_LAUNCH_CHECK();
   NmArgs na{trj, ndims, (int)nr, spf, ns_per_frame, nt, nspk0, nm.as<double>(), Pinv.as<double>(), nrep};
   k_grog_nm<<<1, 1024, 0, st>>>(na);
@@ -505,38 +665,59 @@ extern "C" int mrsr_grog_gridding(int ndims, const int64_t* img_shape, int64_t n
   MRSR_REQUIRE(ncoils >= 1 && ncoils <= kGrogMaxCoils, MRSR_ERR_UNSUPPORTED, "GROG supports 1..%d coils",
                kGrogMaxCoils);
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  GridArgs g{};
-  g.data = reinterpret_cast<float2*>(data);
-  g.trj = trj;
-  g.lnG = reinterpret_cast<const float2*>(lnG);
-  g.trj_cart = trj_cart_out;
-  g.d = ndims;
-  g.nc = ncoils;
-  g.nrep = nrep;
-  g.ns_pf = ns_per_frame;
-  g.nt = nt;
-  g.nr = nr;
-  for (int i = 0; i < 3; ++i) g.N[i] = i < ndims ? img_shape[i] : 1;
   // ||lnG_d||_1 on the host (tiny)
   std::vector<float2> h((size_t)ndims * ncoils * ncoils);
   MRSR_CHECK_CUDA(cudaMemcpyAsync(h.data(), lnG, sizeof(float2) * h.size(), cudaMemcpyDeviceToHost, st));
   MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  const int nn = ncoils * ncoils;
+  DevBuf tab;
+  MRSR_TRY(tab.alloc(sizeof(float2) * (2 * kGridTabMax + 1) * nn * ndims));
+  const int64_t total = ns_per_frame * nt;
   for (int dd = 0; dd < ndims; ++dd) {
-    float best = 0.f;
+    float lnorm = 0.f;
     for (int j = 0; j < ncoils; ++j) {
       float s = 0.f;
       for (int i = 0; i < ncoils; ++i) {
         const float2 v = h[dd + (size_t)ndims * (i + (size_t)ncoils * j)];
         s += std::sqrt(v.x * v.x + v.y * v.y);
       }
-      best = std::max(best, s);
+      lnorm = std::max(lnorm, s);
     }
-    g.lnorm[dd] = best;
+    // |shift| <= Nr / (2 N_d); spacing h with h ||L||_1 <= 1 unless that needs more than 2 kGridTabMax + 1 tables
+    const double smax = 0.5 * (double)nr / (double)img_shape[dd];
+    int J = 0;
+    float hs = 1.f;
+    if (lnorm > 0.f) {
+      J = (int)std::min<double>(kGridTabMax, std::ceil(smax * lnorm));
+      hs = J > 0 ? (float)std::max(1.0 / lnorm, smax / J) : 1.f;
+    }
+    float2* tabd = tab.as<float2>() + (size_t)dd * (2 * kGridTabMax + 1) * nn;
+    TabArgs ta{reinterpret_cast<const float2*>(lnG), ndims, dd, ncoils, J, hs, lnorm, tabd};
+    k_grog_exp_table<<<(unsigned)(2 * J + 1), 1024, 0, st>>>(ta);
+    MRSR_LAUNCH_CHECK();
+    GridArgs g{};
+    g.data = reinterpret_cast<float2*>(data);
+    g.trj = trj;
+    g.lnG = reinterpret_cast<const float2*>(lnG);
+    g.tab = tabd;
+    g.trj_cart = trj_cart_out;
+    g.d = ndims;
+    g.dd = dd;
+    g.nc = ncoils;
+    g.nrep = nrep;
+    g.J = J;
+    g.ns_pf = ns_per_frame;
+    g.nt = nt;
+    g.Nd = img_shape[dd];
+    g.nr = nr;
+    g.h = hs;
+    g.lnorm = lnorm;
+    const size_t smem = sizeof(float2) * (size_t)(2 * J + 2) * nn;
+    MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_grog_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(cdiv(total, 32), grog_sms()));
+    k_grog_grid<<<blocks, 1024, smem, st>>>(g);
+    MRSR_LAUNCH_CHECK();
   }
-  const int64_t total = ns_per_frame * nt;
-  const unsigned blocks = (unsigned)std::min<int64_t>(cdiv(total * 32, 256), 152 * 32);
-  k_grog_grid<<<blocks, 256, 0, st>>>(g);
-  MRSR_LAUNCH_CHECK();
   MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
   return MRSR_OK;
 }
