@@ -1,0 +1,156 @@
+"""Coil-wise calibration reconstructions: the caller of the normal operator inside
+``calculate_coil_maps`` (src/CoilMaps.jl:1-116; GPU ext/MRISubspaceReconCUDAExt/CoilMaps.jl:1-55).
+
+``reconstruct_coilwise`` (src/CoilMaps.jl:118-162, ext/.../CoilMaps.jl:57-77) builds
+one K=1 operator without coil maps and solves Nc independent systems on it, one per
+receive channel.  Non-Cartesian: the Nc fixed-iteration solves
+(``cg!(x_c, AᴴA, b_c; maxiter=Niter_cg, reltol=0)``) run as the branches of one
+CUDA graph, each branch on an operator that shares the Toeplitz kernel and kmask
+of the first (``share``) and owns its workspace.  Cartesian: IterativeSolvers'
+default tolerance applies (src/CoilMaps.jl:159), so each coil runs the
+tolerance-checked ``cg``.
+
+``calculate_calibration_kspace`` is ``calculate_coil_maps`` up to the ESPIRiT call:
+the calibration mask and the rescaled trajectory, the coil-wise reconstruction and
+``fftshift(fft(fftshift(x)))``.  ESPIRiT itself (MRICoilSensitivities) is not part
+of this library; the reference's GPU extension also hands this k-space to it on the
+host (``espirit(Array(kbp), ...)``, ext/.../CoilMaps.jl:30), so it is returned as a
+host array.
+"""
+import numpy as np
+import torch
+
+from .arrays import jl_reshape, jl_zeros, to_host, to_jl
+from .backprojection import _is_int_traj, calculate_backprojection
+from .normalop import FFTNormalOp, NFFTNormalOp
+from .solvers import CgBatch, cg
+
+
+def _first_basis_column(U, nt):
+    """``U[:, 1]`` as an (Nt, 1) basis; the GPU extension's default U is ``ones(Nt)``."""
+    if U is None:
+        return np.ones((nt, 1), dtype=np.float32)
+    if isinstance(U, torch.Tensor):
+        u = U if U.dim() == 1 else U[:, 0]
+        return u.reshape(-1, 1)
+    u = np.asarray(U)
+    u = u if u.ndim == 1 else u[:, 0]
+    return u.reshape(-1, 1)
+
+
+def reconstruct_coilwise(data, trj, img_shape, U=None, sample_mask=None, Niter_cg=None, stream=None):
+    """One image per receive channel: (img_shape..., Nc) column-major device tensor."""
+    img_shape = tuple(int(s) for s in img_shape)
+    cart = _is_int_traj(trj)
+    U1 = _first_basis_column(U, int(trj.shape[-1]))
+    if Niter_cg is None:
+        Niter_cg = 5 if cart else 100  # the reference's defaults
+    if cart:
+        A = FFTNormalOp(img_shape, trj, U1, sample_mask=sample_mask, stream=stream)
+    else:
+        A = NFFTNormalOp(img_shape, trj, U1, sample_mask=sample_mask, stream=stream)
+    b = calculate_backprojection(data, trj, img_shape, U=U1, sample_mask=sample_mask, stream=stream)
+    x = _coilwise_solve(A, b, Niter_cg, tolerance_checked=cart, stream=stream)
+    A.close()
+    return x
+
+
+def _coilwise_solve(A, b, iters, tolerance_checked=False, stream=None):
+    """x[..., c] = cg(A, b[..., 1, c]) for every coil c of the (img..., 1, Nc) backprojection.
+    Fixed iterations: one graph, one branch per coil, each on an operator sharing A's
+    kernel.  ``tolerance_checked``: IterativeSolvers' default reltol, coil by coil."""
+    img_shape = tuple(int(s) for s in b.shape[:-2])
+    nc = int(b.shape[-1])
+    x = jl_zeros(img_shape + (nc,), torch.complex64)
+    if tolerance_checked:
+        for c in range(nc):
+            x[..., c] = cg(A, b[..., 0, c], maxiter=iters, stream=stream)[..., 0]
+        return x
+    shares = [A.share(stream=stream) for _ in range(nc - 1)]
+    batch = CgBatch([A] + shares, [b[..., 0, c] for c in range(nc)], [x[..., c] for c in range(nc)], int(iters),
+                    stream=stream)
+    batch.launch(stream=stream)
+    (stream or torch.cuda.current_stream()).synchronize()
+    batch.close()
+    for op in shares:
+        op.close()
+    return x
+
+
+def _calib_size_noncartesian(img_shape):
+    """nextprod((2, 3, 5), N_i ÷ (maximum(img_shape) ÷ 32)) (src/CoilMaps.jl:37)."""
+    def nextprod235(n):
+        m = max(int(n), 1)
+        while True:
+            r = m
+            for p in (2, 3, 5):
+                while r % p == 0:
+                    r //= p
+            if r == 1:
+                return m
+            m += 1
+    q = max(img_shape) // 32
+    return tuple(nextprod235(n // q) for n in img_shape)
+
+
+def calibration_mask(trj, img_shape, calib_size=None, sample_mask=None):
+    """Calibration-region mask and trajectory of ``calculate_coil_maps``.
+
+    Non-Cartesian (src/CoilMaps.jl:44-48, ext/.../CoilMaps.jl:17-20): keep samples with
+    |k_d| * N_d / n_d < 1/2 in every dimension (products in float32, as the GPU
+    extension's ``cu`` scale vector gives); the trajectory is scaled by N_d / n_d.
+    Cartesian (src/CoilMaps.jl:80-84): keep lower < k_d < lower + n_d + 1 with
+    lower = ceil((N_d - n_d) / 2); the trajectory is unchanged.
+    Returns (mask (Ns, Nt) bool numpy, trajectory, calib_size)."""
+    img_shape = tuple(int(s) for s in img_shape)
+    t = to_host(trj) if isinstance(trj, torch.Tensor) else np.asarray(trj)
+    d = t.shape[0]
+    if np.issubdtype(t.dtype, np.integer):
+        if calib_size is None:
+            calib_size = tuple(n // (img_shape[0] // 32) for n in img_shape)
+        lower = np.array([int(np.ceil((n - c) / 2)) for n, c in zip(img_shape, calib_size)]).reshape(d, 1, 1)
+        upper = lower + np.array(calib_size).reshape(d, 1, 1) + 1
+        mask = np.all(t > lower, axis=0) & np.all(t < upper, axis=0)
+        trj_c = trj
+    else:
+        if calib_size is None:
+            calib_size = _calib_size_noncartesian(img_shape)
+        for c in calib_size:
+            r = c
+            for p in (2, 3, 5):
+                while r % p == 0:
+                    r //= p
+            if r != 1:
+                raise AssertionError("calib_size has to be composed of the prime factors 2, 3, and 5 "
+                                     "(cf. NonuniformFFTs.jl documentation).")
+        scale = np.array([n / c for n, c in zip(img_shape, calib_size)], dtype=np.float32).reshape(d, 1, 1)
+        t32 = t.astype(np.float32)
+        mask = np.all(np.abs(t32) * scale < np.float32(0.5), axis=0)
+        trj_c = (t32 * scale).astype(np.float32)
+    mask = mask.reshape(t.shape[1], -1)
+    if sample_mask is not None:
+        sm = to_host(sample_mask) if isinstance(sample_mask, torch.Tensor) else np.asarray(sample_mask)
+        mask &= sm.reshape(mask.shape).astype(bool)
+    return mask, trj_c, tuple(int(c) for c in calib_size)
+
+
+def calculate_calibration_kspace(data, trj, img_shape, U=None, sample_mask=None, calib_size=None, Niter_cg=None,
+                                 stream=None):
+    """``calculate_coil_maps`` up to ESPIRiT: the centred calibration k-space
+    ``fftshift(fft(fftshift(x)))`` of the coil-wise images, (calib_size..., Nc) complex64
+    on the host.  4D data / trajectories (readout lines on their own axis) are
+    reshaped as in src/CoilMaps.jl:99-111."""
+    if getattr(data, "ndim", None) == 4 or (isinstance(data, torch.Tensor) and data.dim() == 4):
+        data = to_jl(data, torch.complex64)
+        data = jl_reshape(data, (-1, data.shape[2], data.shape[3]))
+        t = to_host(trj) if isinstance(trj, torch.Tensor) else np.asarray(trj)
+        trj = t.reshape(t.shape[0], -1, t.shape[3], order="F")
+        if sample_mask is not None:
+            sm = to_host(sample_mask) if isinstance(sample_mask, torch.Tensor) else np.asarray(sample_mask)
+            sample_mask = sm.reshape(-1, sm.shape[-1], order="F")
+    mask, trj_c, calib_size = calibration_mask(trj, img_shape, calib_size, sample_mask)
+    x = to_host(reconstruct_coilwise(data, trj_c, calib_size, U=U, sample_mask=mask, Niter_cg=Niter_cg,
+                                     stream=stream))
+    axes = tuple(range(len(calib_size)))
+    k = np.fft.fftshift(np.fft.fftn(np.fft.fftshift(x, axes=axes), axes=axes), axes=axes)
+    return k.astype(np.complex64)
