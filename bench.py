@@ -485,7 +485,8 @@ def pipeline_arm(args, world, rank, local):
       applies/s; the fp16 operator's applies/s and its difference from the float32 apply
       on the phantom are reported beside it.
     grog_cart256_nt500_nc32_k6: 256^2 radial, Nt=500 x 2 spokes x 512 samples, 32 coils,
-      K=6.  Stages: grog_calib, grog_gridding!, FFTNormalOp from the gridded trajectory,
+      K=6.  Stages: grog_calib, grog_gridding!, the coil-wise calibration reconstruction of
+      calculate_coil_maps (32^2 region, 32 coils x 100 CG iterations), FFTNormalOp from the gridded trajectory,
       Cartesian backprojection, 20 CG iterations.  `value` = FFTNormalOp applies/s.
     Inputs are seeded synthetic data (forward model + 1% noise).  Stage times are CUDA
     events on the launching stream after one untimed run of every stage (L2 not flushed:
@@ -550,6 +551,12 @@ def pipeline_arm(args, world, rank, local):
             trj_c = mr.grog_gridding(data, trj, lnG, Nr, img)
             work = data0.clone()
             st["grog_gridding"] = _events_ms(lambda: mr.grog_gridding(work, trj, lnG, Nr, img), 1, stream)
+        # calculate_coil_maps up to ESPIRiT: 32^2 calibration region, 32 coil-wise K=1 solves of
+        # 100 CG iterations (one graph), operator and backprojection included
+        mask_cal, trj_cal, calib = mr.calibration_mask(mr.to_host(trj), img)
+        mr.reconstruct_coilwise(data0, trj_cal, calib, sample_mask=mask_cal)
+        st["coilwise_calibration"] = _wall_ms(
+            lambda: mr.reconstruct_coilwise(data0, trj_cal, calib, sample_mask=mask_cal), 1)
         A = mr.FFTNormalOp(img, trj_c, U, cmaps=cm)
         st["fft_normalop_create"] = _wall_ms(lambda: mr.FFTNormalOp(img, trj_c, U, cmaps=cm).close(), 1)
         b = mr.calculate_backprojection(data, trj_c, cm, U=U)
