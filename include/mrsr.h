@@ -50,10 +50,15 @@ enum {
 enum {
   MRSR_PREC_FP32 = 0, /* float32 everywhere (the reference's precision)   */
   MRSR_PREC_FP16 = 1, /* fp16 storage with per-tile scales, fp32 arithmetic */
-  MRSR_PREC_FP16_ARITH = 2 /* fp16 storage and fp16 (half2) FFT / kernel
-                              arithmetic on line pairs, fp32 coil sums; 2D
-                              four-step grids with an even Λ tile width,
-                              else as MRSR_PREC_FP16                       */
+  MRSR_PREC_FP16_ARITH = 2, /* fp16 storage and fp16 (half2) FFT / kernel
+                               arithmetic on line pairs, fp32 coil sums; 2D
+                               four-step grids with an even Λ tile width,
+                               else as MRSR_PREC_FP16                       */
+  MRSR_PREC_FP16_TC = 3     /* float32 stack and row passes; the Λ pass runs
+                               its 64-point column DFTs on the tensor cores
+                               (tcgen05, fp16 operands with per-tile
+                               power-of-two scales, fp32 accumulation); NFFT
+                               operators whose last grid length is 512     */
 };
 
 /* Density compensation of calculate_backprojection (src/BackProjection.jl:169-181). */

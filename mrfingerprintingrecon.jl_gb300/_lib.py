@@ -8,7 +8,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libmrsr.so"
 
 MRSR_OK, MRSR_ERR_ARG, MRSR_ERR_CUDA, MRSR_ERR_ALLOC, MRSR_ERR_UNSUPPORTED, MRSR_ERR_STATE, MRSR_ERR_DEVICE = range(7)
-PREC_FP32, PREC_FP16, PREC_FP16_ARITH = 0, 1, 2
+PREC_FP32, PREC_FP16, PREC_FP16_ARITH, PREC_FP16_TC = 0, 1, 2, 3
 DCF_NONE, DCF_RADIAL_2D, DCF_RADIAL_3D, DCF_ARRAY = range(4)
 KIND_NFFT, KIND_FFT = 0, 1
 

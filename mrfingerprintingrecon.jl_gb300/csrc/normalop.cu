@@ -445,7 +445,7 @@ static void record_cb(void* ctx) { static_cast<Recorder*>(ctx)->record(); }
 
 static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
                       Recorder rec) {
-  if (op->precision != MRSR_PREC_FP32) {
+  if (op->precision == MRSR_PREC_FP16 || op->precision == MRSR_PREC_FP16_ARITH) {
     if (pair_supported(op)) return apply_pair_impl(op, x, y, alpha, beta, st, rec.ev ? record_cb : nullptr, &rec);
     return apply_half_impl(op, x, y, alpha, beta, st, rec.ev ? record_cb : nullptr, &rec);
   }
@@ -498,7 +498,10 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
                     op->P, op->lam_mode, Ll * TC, op->lam.p, lam_stack, op->FC, (int)(Ll / op->FC)};
       dim3 grid((unsigned)(g.inner() / TC), ncg);
       const size_t smem = sizeof(float2) * ((size_t)Ll + 2 * (size_t)K * a.lstride);
-      if (fast_length(Ll))
+      if (op->precision == MRSR_PREC_FP16_TC) {
+        a.lam = op->lam_tc.p;
+        MRSR_TRY(tc_lambda(a, ncg, op->lam_max.as<float>(), op->errflag.as<int>(), st));
+      } else if (fast_length(Ll))
         MRSR_TRY(fast_lambda(a, ncg, op->Cg * K, op->errflag.as<int>(), st));
       else
         MRSR_TRY(launch_fft_kernel<LamPassArgs>(k_lambda_pass, grid, 512, smem, st, a));
@@ -552,8 +555,8 @@ int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_
   MRSR_REQUIRE(img_shape != nullptr, MRSR_ERR_ARG, "img_shape is NULL");
   MRSR_REQUIRE(K >= 1 && K <= KMAX, MRSR_ERR_UNSUPPORTED, "rank K=%d outside 1..%d", K, KMAX);
   MRSR_REQUIRE(ncoils >= 1, MRSR_ERR_ARG, "ncoils must be >= 1");
-  MRSR_REQUIRE(precision == MRSR_PREC_FP32 || precision == MRSR_PREC_FP16 || precision == MRSR_PREC_FP16_ARITH,
-               MRSR_ERR_ARG, "unknown precision %d", precision);
+  MRSR_REQUIRE(precision >= MRSR_PREC_FP32 && precision <= MRSR_PREC_FP16_TC, MRSR_ERR_ARG, "unknown precision %d",
+               precision);
   op->kind = kind;
   op->precision = precision;
   OpGeom& g = op->geo;
@@ -577,7 +580,14 @@ int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_
   int TC = (int)env_int("MRSR_LAMBDA_TC", 8);
   const int64_t budget = fast_length((int)g.glast()) ? 13000 : 12288;
   while (TC > 1 && ((int64_t)K * TC * g.glast() > budget || g.inner() % TC != 0)) TC >>= 1;
+  if (precision == MRSR_PREC_FP16_TC) TC = 4;  // the tensor-core Λ pass works on 4-column tiles
   op->TC = TC;
+  if (precision == MRSR_PREC_FP16_TC) {
+    const int nl = (int)g.n[ndims - 1], gl = (int)g.glast();
+    MRSR_REQUIRE(kind == MRSR_KIND_NFFT && tc_lambda_supported(gl, nl, nl, TC, K) && g.inner() % TC == 0,
+                 MRSR_ERR_UNSUPPORTED,
+                 "the tensor-core Λ pass needs an NFFT operator whose last grid length is 512 (got %d)", gl);
+  }
   MRSR_TRY(op->errflag.alloc(sizeof(int)));
   return MRSR_OK;
 }
@@ -596,7 +606,7 @@ int op_set_cmaps(mrsr_normalop* op, const float* cmaps, cudaStream_t st) {
 
 int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   const OpGeom& g = op->geo;
-  const bool half = op->precision != MRSR_PREC_FP32;
+  const bool half = op->precision == MRSR_PREC_FP16 || op->precision == MRSR_PREC_FP16_ARITH;
   MRSR_REQUIRE(!half || half_supported(op), MRSR_ERR_UNSUPPORTED,
                "fp16 storage needs grid lengths with a register four-step split (64, 128, 256, 384, 512, 768, 1024)");
   const int64_t esz = half ? 4 : (int64_t)sizeof(float2);
@@ -633,6 +643,15 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
       MRSR_TRY(pair_alloc(op, st));
     else
       MRSR_TRY(half_alloc_scales(op));
+  }
+  if (op->precision == MRSR_PREC_FP16_TC) {
+    MRSR_TRY(op->lam_max.alloc(sizeof(float)));
+    MRSR_TRY(tc_lambda_bound(op->lam.p, op->lam.bytes, op->lam_max.as<float>(), st));
+    const int64_t ntiles = g.inner() / op->TC;
+    const size_t esz = op->lam_mode == LAM_PACKED_REAL ? sizeof(float) : sizeof(float2);
+    MRSR_TRY(op->lam_tc.alloc(esz * (size_t)ntiles * op->P * g.glast() * op->TC));
+    MRSR_TRY(tc_lambda_layout(op->lam.p, op->lam_tc.p, ntiles, op->P, op->FC, (int)(g.glast() / op->FC),
+                              op->lam_mode == LAM_PACKED_REAL, st));
   }
   // the operator's buffers came from the pool on `st`: make them usable on any stream
   MRSR_CHECK_CUDA(cudaStreamSynchronize(st));

@@ -66,6 +66,8 @@ struct mrsr_normalop {
   mrsr::DevBuf stack1, stack2;  // intermediates of one coil group
   mrsr::DevBuf scale1, scale2;  // fp16 per-line scales
   mrsr::DevBuf errflag;         // device int
+  mrsr::DevBuf lam_max;         // device float: largest |component| of Λ (tensor-core Λ pass)
+  mrsr::DevBuf lam_tc;          // Λ rearranged for the tensor-core Λ pass
   mrsr::FftPlanHost plan[3];
   mrsr::CgWork cg;              // CG vectors, allocated on first solve
   // recorded after every call that enqueues work on the operator; the

@@ -1,0 +1,90 @@
+"""The tensor-core Λ pass (precision "fp16-tc"): 64-point column DFTs as tcgen05 MMAs with
+fp16 operands and per-tile power-of-two scales, float32 accumulation; row passes and the
+stack in float32.
+
+Two fp16 roundings of the operands (before the forward and the inverse DFT-64) and the
+fp16 DFT matrix set the error: relative L2 vs the float64 oracle of ``mul!``
+(src/NFFTNormalOp.jl:227-267) a few 1e-4; the bound written here is the mixed-precision
+target, 1e-3.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import cg as ocg
+from oracle import normalop as onormal
+from oracle import trajectories as otraj
+from tests.helpers import rand_c, rel_l2
+
+TOL = 1e-3
+pytestmark = pytest.mark.gpu
+
+
+def _problem(seed, img, K, Nc, density=0.8, complex_lam=True):
+    rng = np.random.default_rng(seed)
+    G = tuple(2 * n for n in img)
+    cells = np.flatnonzero(rng.random(int(np.prod(G))) < density) + 1
+    P = K * (K + 1) // 2
+    lam = rand_c(rng, (P, cells.size)) if complex_lam else rng.standard_normal((P, cells.size)).astype(np.float32)
+    cm = rand_c(rng, img + (Nc,))
+    x = rand_c(rng, img + (K,))
+    return lam, cells, cm, x
+
+
+@pytest.mark.parametrize("K,Nc,cplx", [(1, 2, True), (3, 2, False), (5, 3, False), (5, 2, True), (8, 2, True)])
+def test_tc_apply_matches_oracle(mr, cuda, K, Nc, cplx):
+    img = (256, 256)
+    lam, cells, cm, x = _problem(20 + K, img, K, Nc, complex_lam=cplx)
+    cml = [cm[..., c] for c in range(Nc)]
+    A = mr.NFFTNormalOp(img, lam, cells, cmaps=cml, precision="fp16-tc")
+    assert A.precision == 3
+    y = mr.to_host(A @ x)
+    ref = onormal.nfft_normalop_apply(x, onormal.unpack_lambda(lam.astype(np.complex128), K), cells, img, cmaps=cml)
+    err = rel_l2(y, ref)
+    y32 = mr.to_host(mr.NFFTNormalOp(img, lam, cells, cmaps=cml) @ x)
+    print(f"fp16-tc apply K={K} Nc={Nc} cplx={cplx}: rel L2 {err:.2e} (float32 {rel_l2(y32, ref):.2e})")
+    assert err < TOL
+
+
+def test_tc_scale_invariant(mr, cuda):
+    """Per-tile scales follow the data: tiny and huge inputs keep their accuracy, a zero
+    coil map gives exact zeros."""
+    img, K, Nc = (256, 256), 4, 3
+    lam, cells, cm, x = _problem(31, img, K, Nc)
+    cm[..., 1] = 0
+    cml = [cm[..., c] for c in range(Nc)]
+    A = mr.NFFTNormalOp(img, lam, cells, cmaps=cml, precision="fp16-tc")
+    L64 = onormal.unpack_lambda(lam.astype(np.complex128), K)
+    for s in (1e-20, 1e15):
+        xs = (x * s).astype(np.complex64)
+        y = mr.to_host(A @ xs)
+        assert np.all(np.isfinite(y))
+        assert rel_l2(y, onormal.nfft_normalop_apply(xs.astype(np.complex128), L64, cells, img, cmaps=cml)) < TOL
+
+
+def test_tc_from_trajectory_and_cg(mr, cuda):
+    """Operator from a radial trajectory (real basis, packed real kernel); cg(A, b; maxiter=20)
+    against the float64 CG on the oracle operator."""
+    rng = np.random.default_rng(5)
+    N, K, Nt, Nc = 256, 4, 40, 2
+    trj = otraj.traj_2d_radial_goldenratio(2 * N, 8, Nt)
+    U = np.linalg.svd(rng.standard_normal((Nt, K)), full_matrices=False)[0].astype(np.float32)
+    cm = rand_c(rng, (N, N, Nc))
+    cml = [cm[..., c] for c in range(Nc)]
+    A = mr.NFFTNormalOp((N, N), trj, U, cmaps=cml, precision="fp16-tc")
+    A32 = mr.NFFTNormalOp((N, N), A.Λ, A.kmask_indcs, cmaps=cml)
+    b = rand_c(rng, (N, N, K))
+    L64 = onormal.unpack_lambda(mr.to_host(A.Λ).astype(np.complex128), K)
+    km = mr.to_host(A.kmask_indcs)
+    assert rel_l2(mr.to_host(A @ b), onormal.nfft_normalop_apply(b, L64, km, (N, N), cmaps=cml)) < TOL
+    bt = mr.to_jl(b, torch.complex64)
+    x16 = mr.to_host(mr.cg(A, bt, maxiter=20, reltol=0.0)).ravel(order="F")
+    x32 = mr.to_host(mr.cg(A32, bt, maxiter=20, reltol=0.0)).ravel(order="F")
+    print(f"cg-20 fp16-tc vs float32: {rel_l2(x16, x32):.2e}")
+    assert rel_l2(x16, x32) < 2e-3
+
+
+def test_tc_rejects_other_grids(mr, cuda):
+    lam, cells, cm, _ = _problem(8, (128, 128), 3, 1)
+    with pytest.raises(NotImplementedError):
+        mr.NFFTNormalOp((128, 128), lam, cells, cmaps=[cm[..., 0]], precision="fp16-tc")
