@@ -48,7 +48,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SERVED, PIPE3D, PIPEGROG])
-    p.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "refined"],
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "fp16-tc", "refined"],
                    help="operator storage: fp32, fp16 (per-tile scaled half stacks and kernel); "
                         "refined (served workload only: fp16 inner CG + float32 residual steps)")
     p.add_argument("--rate", type=float, default=40.0, help="served workload: Poisson arrival rate (requests/s)")
@@ -255,9 +255,9 @@ def gb300_arm(args, world, rank, local):
     # operator: Toeplitz kernel precompute on the device (timed once, reported beside the headline)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    prec = "fp32" if args.precision == "fp32" else "fp16"
+    prec = args.precision if args.precision in ("fp32", "fp16-tc") else "fp16"
     A = mr.NFFTNormalOp(w["img"], trj, U, cmaps=cm, precision=prec)
-    esz, lsz = (8, 4) if prec == "fp32" else (4, 2)   # bytes per stack element / per real kernel entry
+    esz, lsz = (4, 2) if prec == "fp16" else (8, 4)   # bytes per stack element / per real kernel entry
     torch.cuda.synchronize()
     t_lambda = time.perf_counter() - t0
     x = mr.to_jl(x_h, torch.complex64)
@@ -336,9 +336,34 @@ def gb300_arm(args, world, rank, local):
     lam_bytes = 2.0 * cg * K * N2 * G1 * esz + nk * P * lsz      # stack in + out, Λ once
     achieved = lam_bytes / (lam_avg * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    lam_kernel = "k4_lambda" if prec == "fp32" else "kh_lambda"
+    lam_kernel = {"fp32": "k4_lambda", "fp16": "kh_lambda", "fp16-tc": "kt_lambda"}[prec]
     traffic = profile_traffic(lam_kernel)
     apply_bytes = N1 * N2 * K * 16 + 2 * Nc * N1 * N2 * 8 + 4 * Nc * (G1 * N2 * K) * esz + nk * P * lsz
+    # the mixed-precision tensor-core operator on the same kernel and inputs, same protocol
+    mixed = None
+    if prec == "fp32":
+        At = A.share(cmaps=cm, precision="fp16-tc")
+        yt = mr.jl_empty(x.shape, torch.complex64)
+        for _ in range(max(args.warmup, 3)):
+            flush.fill_(1.0)
+            At.mul(yt, x)
+        nt = min(args.steps, 50)
+        evt = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nt)]
+        for i in range(nt):
+            flush.fill_(float(i))
+            evt[i][0].record(stream)
+            At.mul(yt, x)
+            evt[i][1].record(stream)
+        torch.cuda.synchronize()
+        ms_t = max_over_ranks(sum(a.elapsed_time(b_) for a, b_ in evt) / nt, world)
+        A.mul(y, x)
+        torch.cuda.synchronize()
+        err = float(torch.linalg.norm(yt - y) / torch.linalg.norm(y))
+        mixed = {"precision": "fp16-tc", "operator": "tensor-core Λ pass (tcgen05 DFT-64, fp16 operands with per-tile "
+                 "scales, fp32 accumulation), float32 row passes", "applies_s": world * 1000.0 / ms_t,
+                 "ms_per_apply": ms_t, "vs_fp32": ms / ms_t, "apply_rel_l2_vs_fp32": err,
+                 "pass_ms": [round(p_, 5) for p_ in At.profile(x, yt, iters=20)]}
+        At.close()
     if rank != 0:
         return
     value = world * 1000.0 / ms
@@ -346,11 +371,12 @@ def gb300_arm(args, world, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "c64" if prec == "fp32" else "c64 (f16 storage)",
+        "vs_baseline": None, "dtype": {"fp32": "c64", "fp16": "c64 (f16 storage)", "fp16-tc": "c64 (f16 tensor-core operands)"}[prec],
         "data": "synthetic (seeded phantom, dictionary basis, coil maps)",
         "config": {"workload": args.workload, "img": list(w["img"]), "Nr": w["Nr"], "Ncyc": w["Ncyc"], "Nt": w["Nt"],
                    "Nc": Nc, "K": K, "precision": prec,
-                   "operator": "NFFTNormalOp " + ("float32" if prec == "fp32" else "fp16 storage, float32 arithmetic")
+                   "operator": "NFFTNormalOp " + {"fp32": "float32", "fp16": "fp16 storage, float32 arithmetic",
+                                                  "fp16-tc": "float32 rows, tensor-core Λ pass"}[prec]
                    + " (real basis, packed real kernel)",
                    "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) before every timed step"},
         "e2e": {"value": world * 1000.0 / ms_e2e, "unit": "applies/s", "h2d_bytes_per_step": int(xh.numel() * 8),
@@ -367,6 +393,8 @@ def gb300_arm(args, world, rank, local):
         "cpu_baseline": {"value": base_rate, "unit": "applies/s", "cores": cores, "kind": "port", "sample": sample},
         "precompute_s": {"lambda_kmask": t_lambda, "backprojection": t_bp},
     }
+    if mixed:
+        line["mixed_precision"] = mixed
     print(json.dumps(line), flush=True)
 
 
