@@ -443,6 +443,14 @@ static int mid_tc(const mrsr_normalop* op) {
 
 static void record_cb(void* ctx) { static_cast<Recorder*>(ctx)->record(); }
 
+static bool tc_rows_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("MRSR_TC_ROWS");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
                       Recorder rec) {
   if (op->precision == MRSR_PREC_FP16 || op->precision == MRSR_PREC_FP16_ARITH) {
@@ -462,12 +470,17 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
   for (int grp = 0; grp < ngroups; ++grp) {
     const int c0 = grp * op->Cg;
     const int ncg = std::min(op->Cg, g.ncoils - c0);
+    // fp16-tc: row passes on the tensor cores too (MRSR_TC_ROWS=0 keeps them in float32)
+    const bool tc_rows = op->precision == MRSR_PREC_FP16_TC && tc_rows_enabled() &&
+                         tc_rows_supported(L1, (int)g.n[0], ncg);
     // P1: rows forward
     {
       RowTiling t = rows_tiling(L1, K, nrows);
       RowsFwdArgs a{op->plan[0].plan, (int)g.n[0], nrows, t.rpc, K, c0, t.lstride, x, cm, st1};
       dim3 grid((unsigned)cdiv(nrows, t.rpc), ncg);
-      if (fast_length(L1))
+      if (tc_rows)
+        MRSR_TRY(tc_rows_fwd(a, ncg, op->tc_consts.p, op->errflag.as<int>(), st));
+      else if (fast_length(L1))
         MRSR_TRY(fast_rows_fwd(a, nrows, ncg, st));
       else
         MRSR_TRY(launch_fft_kernel<RowsFwdArgs>(k_rows_fwd, grid, t.threads, t.smem, st, a));
@@ -500,7 +513,7 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       const size_t smem = sizeof(float2) * ((size_t)Ll + 2 * (size_t)K * a.lstride);
       if (op->precision == MRSR_PREC_FP16_TC) {
         a.lam = op->lam_tc.p;
-        MRSR_TRY(tc_lambda(a, ncg, op->lam_max.as<float>(), op->errflag.as<int>(), st));
+        MRSR_TRY(tc_lambda(a, ncg, op->lam_max.as<float>(), op->tc_consts.p, op->errflag.as<int>(), st));
       } else if (fast_length(Ll))
         MRSR_TRY(fast_lambda(a, ncg, op->Cg * K, op->errflag.as<int>(), st));
       else
@@ -527,7 +540,9 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       RowsInvArgs a{op->plan[0].plan, (int)g.n[0], nrows, t.rpc, K, c0, ncg, t.lstride, grp == 0 ? 1 : 0, al, beta,
                     st1, cm, y};
       dim3 grid((unsigned)cdiv(nrows, t.rpc), K);
-      if (fast_length(L1))
+      if (tc_rows)
+        MRSR_TRY(tc_rows_inv(a, op->tc_consts.p, op->errflag.as<int>(), st));
+      else if (fast_length(L1))
         MRSR_TRY(fast_rows_inv(a, nrows, st));
       else
         MRSR_TRY(launch_fft_kernel<RowsInvArgs>(k_rows_inv, grid, t.threads, t.smem, st, a));
@@ -645,6 +660,8 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
       MRSR_TRY(half_alloc_scales(op));
   }
   if (op->precision == MRSR_PREC_FP16_TC) {
+    MRSR_TRY(op->tc_consts.alloc(tc_constants_bytes()));
+    MRSR_TRY(tc_build_constants(op->tc_consts.p, st));
     MRSR_TRY(op->lam_max.alloc(sizeof(float)));
     MRSR_TRY(tc_lambda_bound(op->lam.p, op->lam.bytes, op->lam_max.as<float>(), st));
     const int64_t ntiles = g.inner() / op->TC;

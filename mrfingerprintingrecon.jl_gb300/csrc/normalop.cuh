@@ -68,6 +68,7 @@ struct mrsr_normalop {
   mrsr::DevBuf errflag;         // device int
   mrsr::DevBuf lam_max;         // device float: largest |component| of Λ (tensor-core Λ pass)
   mrsr::DevBuf lam_tc;          // Λ rearranged for the tensor-core Λ pass
+  mrsr::DevBuf tc_consts;       // DFT-64 MMA operand and twiddles of the tensor-core passes
   mrsr::FftPlanHost plan[3];
   mrsr::CgWork cg;              // CG vectors, allocated on first solve
   // recorded after every call that enqueues work on the operator; the

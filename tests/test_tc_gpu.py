@@ -1,11 +1,11 @@
-"""The tensor-core Λ pass (precision "fp16-tc"): 64-point column DFTs as tcgen05 MMAs with
-fp16 operands and per-tile power-of-two scales, float32 accumulation; row passes and the
-stack in float32.
+"""The tensor-core operator (precision "fp16-tc"): every 64-point DFT stage of the row
+passes and of the Λ pass is a tcgen05 MMA with fp16 operands, per-tile power-of-two
+scales and float32 accumulation; the DFT-8 stages, twiddles, coil maps, K x K kernel and
+coil sums run in float32, and the stack between the passes is float32.
 
-Two fp16 roundings of the operands (before the forward and the inverse DFT-64) and the
-fp16 DFT matrix set the error: relative L2 vs the float64 oracle of ``mul!``
-(src/NFFTNormalOp.jl:227-267) a few 1e-4; the bound written here is the mixed-precision
-target, 1e-3.
+Four fp16 roundings of the operands (one per DFT-64) and the fp16 DFT matrix set the
+error: relative L2 vs the float64 oracle of ``mul!`` (src/NFFTNormalOp.jl:227-267) a few
+1e-4; the bound written here is the mixed-precision target, 1e-3.
 """
 import numpy as np
 import pytest
@@ -31,7 +31,8 @@ def _problem(seed, img, K, Nc, density=0.8, complex_lam=True):
     return lam, cells, cm, x
 
 
-@pytest.mark.parametrize("K,Nc,cplx", [(1, 2, True), (3, 2, False), (5, 3, False), (5, 2, True), (8, 2, True)])
+@pytest.mark.parametrize("K,Nc,cplx", [(1, 2, True), (3, 2, False), (5, 3, False), (5, 2, True), (8, 2, True),
+                                       (5, 20, False), (2, 5, True)])
 def test_tc_apply_matches_oracle(mr, cuda, K, Nc, cplx):
     img = (256, 256)
     lam, cells, cm, x = _problem(20 + K, img, K, Nc, complex_lam=cplx)
@@ -44,6 +45,14 @@ def test_tc_apply_matches_oracle(mr, cuda, K, Nc, cplx):
     y32 = mr.to_host(mr.NFFTNormalOp(img, lam, cells, cmaps=cml) @ x)
     print(f"fp16-tc apply K={K} Nc={Nc} cplx={cplx}: rel L2 {err:.2e} (float32 {rel_l2(y32, ref):.2e})")
     assert err < TOL
+
+
+def test_tc_without_coil_maps(mr, cuda):
+    img, K = (256, 256), 3
+    lam, cells, _, x = _problem(41, img, K, 1)
+    A = mr.NFFTNormalOp(img, lam, cells, precision="fp16-tc")
+    ref = onormal.nfft_normalop_apply(x, onormal.unpack_lambda(lam.astype(np.complex128), K), cells, img)
+    assert rel_l2(mr.to_host(A @ x), ref) < TOL
 
 
 def test_tc_scale_invariant(mr, cuda):
