@@ -151,21 +151,32 @@ __global__ void __launch_bounds__(kTcThreads, K <= 5 ? 2 : 1) kt_lambda(TcArgs t
     return ((tile * a.P * 8 + j) * 2 + h) * 128 + 2 * f2 + part;
   };
 
+  // this thread's F1 inputs of an item: rows 64 n1 + n2 (n1 < 4) of column li1, all k
+  auto item_base = [&](int64_t it) -> float2* {
+    const int c = (int)(it % a.ncg);
+    return a.stack + (int64_t)c * K * plane + (it / a.ncg) * kTcTC;
+  };
+  float2 xin[K][4];
+  auto load_inputs = [&](int64_t it) {
+    const float2* b = item_base(it);
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+#pragma unroll
+      for (int n1 = 0; n1 < 4; ++n1) xin[k][n1] = b[k * plane + (int64_t)(64 * n1 + n2) * a.inner + li1];
+  };
+  if ((int64_t)blockIdx.x < t.nitems) load_inputs(blockIdx.x);
+
   bool ok = true;
   for (int64_t item = blockIdx.x; item < t.nitems && ok; item += gridDim.x) {
-    const int cl = (int)(item % a.ncg);
     const int64_t tile = item / a.ncg;
-    float2* base = a.stack + (int64_t)cl * K * plane + tile * kTcTC;
-    // ---- F1: pruned DFT-8 over n1 and the w512 twiddle, into operand B
-    float2 xin[K][4];
+    float2* base = item_base(item);
+    // ---- F1: pruned DFT-8 over n1 and the w512 twiddle, into operand B (the inputs were
+    // loaded during the previous item)
     float mx = 0.f;
 #pragma unroll
     for (int k = 0; k < K; ++k)
 #pragma unroll
-      for (int n1 = 0; n1 < 4; ++n1) {
-        xin[k][n1] = base[k * plane + (int64_t)(64 * n1 + n2) * a.inner + li1];
-        mx = fmaxf(mx, fmaxf(fabsf(xin[k][n1].x), fabsf(xin[k][n1].y)));
-      }
+      for (int n1 = 0; n1 < 4; ++n1) mx = fmaxf(mx, fmaxf(fabsf(xin[k][n1].x), fabsf(xin[k][n1].y)));
     const int e1 = scale_exp(4.f * block_max<kTcThreads>(mx, red));
     const float s1 = ldexpf(1.f, e1);
     constexpr float r2 = 0.70710678118654752f;
@@ -189,14 +200,7 @@ __global__ void __launch_bounds__(kTcThreads, K <= 5 ? 2 : 1) kt_lambda(TcArgs t
     umma::fence_before_sync();
     __syncthreads();
     issue_mma();
-    if (!(ok = wait_mma())) break;
-    // ---- spectrum, voxel by voxel: exchange, undo the scale, K x K kernel, write conj(Y)
-    // scaled into operand B of the inverse.  |D| < 128 * 2^14 = 2^21, so |X| < 2^(21 - e1)
-    // and |Y| < K lam_max 2^(21 - e1): a power-of-two scale from that bound keeps every
-    // fp16 value finite without waiting for the block's maximum.
-    const float is1 = ldexpf(1.f, -e1);
-    const int e2 = scale_exp(kbound * ldexpf(1.f, 21 - e1));
-    const float s2 = ldexpf(1.f, e2);
+    // the first voxel's kernel entries load while the MMA runs
     const bool real_lam = a.lam_mode == LAM_PACKED_REAL;
     const float* lamr = reinterpret_cast<const float*>(a.lam);
     float lcur[P];
@@ -205,6 +209,14 @@ __global__ void __launch_bounds__(kTcThreads, K <= 5 ? 2 : 1) kt_lambda(TcArgs t
 #pragma unroll
       for (int p = 0; p < P; ++p) lcur[p] = lamr[lb + p * pstride];
     }
+    if (!(ok = wait_mma())) break;
+    // ---- spectrum, voxel by voxel: exchange, undo the scale, K x K kernel, write conj(Y)
+    // scaled into operand B of the inverse.  |D| < 128 * 2^14 = 2^21, so |X| < 2^(21 - e1)
+    // and |Y| < K lam_max 2^(21 - e1): a power-of-two scale from that bound keeps every
+    // fp16 value finite without waiting for the block's maximum.
+    const float is1 = ldexpf(1.f, -e1);
+    const int e2 = scale_exp(kbound * ldexpf(1.f, 21 - e1));
+    const float s2 = ldexpf(1.f, e2);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       float d[K][2];
@@ -230,13 +242,18 @@ __global__ void __launch_bounds__(kTcThreads, K <= 5 ? 2 : 1) kt_lambda(TcArgs t
       } else {
         lam_apply_ptr<K>(a.lam_mode, K, a.lam, lam_base(tile, j), pstride, X, Y);
       }
+      // inverse operand row k * 32 + 16 h + 2 j + part: this thread's columns of plane k
+      // come back as one run of 16 (f1 = j, li = 2 h + part)
 #pragma unroll
-      for (int k = 0; k < K; ++k) st_half2(sB, boff(k * 32 + j * 4 + li, 2 * f2), Y[k].x * s2, -Y[k].y * s2);
+      for (int k = 0; k < K; ++k)
+        st_half2(sB, boff(k * 32 + 16 * h + 2 * j + part, 2 * f2), Y[k].x * s2, -Y[k].y * s2);
     }
     umma::fence_proxy_async();
     umma::fence_before_sync();
     __syncthreads();
     issue_mma();
+    // the next item's inputs load while this item's inverse runs
+    if (item + gridDim.x < t.nitems) load_inputs(item + gridDim.x);
     if (!(ok = wait_mma())) break;
     // ---- inverse, plane by plane: conj, twiddle, output-pruned inverse DFT-8 over f1,
     // staged as float2 in the operand-B region (the MMA that read it has completed)
@@ -244,12 +261,12 @@ __global__ void __launch_bounds__(kTcThreads, K <= 5 ? 2 : 1) kt_lambda(TcArgs t
     float2* stg = reinterpret_cast<float2*>(sB);  // [k][n < 256][li], rows kTcStg apart
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      float Rk[32];
-      tmem_ld32(tl + (uint32_t)(k * 32), Rk);
+      float Rk[16];
+      umma::tmem_ld16(tl + (uint32_t)(k * 32 + 16 * h), Rk);
       float2 z[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const float2 v = pair_value(h ? Rk[4 * j + 2] : Rk[4 * j], h ? Rk[4 * j + 3] : Rk[4 * j + 1]);
+        const float2 v = pair_value(Rk[2 * j], Rk[2 * j + 1]);
         z[j] = cmulcf(make_float2(v.x * is2, -v.y * is2), tw[f2 * j]);
       }
       float2 ev[4], od[4];
