@@ -119,6 +119,25 @@ __global__ void __launch_bounds__(kRThreads, 2) kt_rows_fwd(TcRowsArgs t) {
   const int L = kL;
   constexpr float r2 = 0.70710678118654752f;
 
+  // this thread's inputs of an item: x[64 n1 + n2, r, k] (shared by every coil) and the
+  // maps of its coils 4 p + cq at the same samples; loaded one item ahead
+  float2 xv[4], sv[NP][4];
+  auto load_inputs = [&](int64_t it) {
+    const int64_t rr = it / a.K;
+    const int kk = (int)(it - rr * a.K);
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) xv[n1] = a.x[64 * n1 + n2 + (int64_t)a.n1 * (rr + a.nrows * kk)];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const int cl = 4 * p + cq;
+#pragma unroll
+      for (int n1 = 0; n1 < 4; ++n1)
+        sv[p][n1] = (a.cmaps && cl < t.ncg) ? a.cmaps[64 * n1 + n2 + (int64_t)a.n1 * (rr + a.nrows * (a.c0 + cl))]
+                                            : make_float2(1.f, 0.f);
+    }
+  };
+  if ((int64_t)blockIdx.x < t.nitems) load_inputs(blockIdx.x);
+
   bool ok = true;
   for (int64_t item = blockIdx.x; item < t.nitems && ok; item += gridDim.x) {
     const int64_t r = item / a.K;
@@ -131,12 +150,7 @@ __global__ void __launch_bounds__(kRThreads, 2) kt_rows_fwd(TcRowsArgs t) {
       const int cl = 4 * p + cq;
 #pragma unroll
       for (int n1 = 0; n1 < 4; ++n1) {
-        const int n = 64 * n1 + n2;
-        float2 val = make_float2(0.f, 0.f);
-        if (cl < t.ncg) {
-          val = a.x[n + (int64_t)a.n1 * (r + a.nrows * k)];
-          if (a.cmaps) val = cmul(a.cmaps[n + (int64_t)a.n1 * (r + a.nrows * (a.c0 + cl))], val);
-        }
+        const float2 val = cl < t.ncg ? cmul(sv[p][n1], xv[n1]) : make_float2(0.f, 0.f);
         v[p][n1] = val;
         mx = fmaxf(mx, fmaxf(fabsf(val.x), fabsf(val.y)));
       }
@@ -163,6 +177,7 @@ __global__ void __launch_bounds__(kRThreads, 2) kt_rows_fwd(TcRowsArgs t) {
     umma::fence_before_sync();
     __syncthreads();
     issue_dft64(tid, tmem, aaddr, baddr, idesc, &mbar);
+    if (item + gridDim.x < t.nitems) load_inputs(item + gridDim.x);  // under the MMA and epilogue
     if (!(ok = wait_dft64(warp, lane, &mbar, phase, &abort_flag))) break;
     // ---- epilogue: the lane pair holds re / im of row f2 for f1 = 0..7; the even lane
     // keeps f1 < 4, the odd lane f1 >= 4, so each writes 4 consecutive frequencies
@@ -266,12 +281,25 @@ __global__ void __launch_bounds__(kRThreads, 2) kt_rows_inv(TcRowsArgs t) {
     umma::fence_before_sync();
     __syncthreads();
     issue_dft64(tid, tmem, aaddr, baddr, idesc, &mbar);
+    // the maps this thread multiplies with, conj(S_c[64 m1 + m2, r]) for its coils
+    // c = h CB / 2 + 2 i + part, load while the MMA runs
+    float2 smap[CB / 4][4];
+#pragma unroll
+    for (int i = 0; i < CB / 4; ++i) {
+      const int cl = h * (CB / 2) + 2 * i + part;
+#pragma unroll
+      for (int m1 = 0; m1 < 4; ++m1)
+        smap[i][m1] = (a.cmaps && cl < t.ncg) ? a.cmaps[64 * m1 + m2 + (int64_t)a.n1 * (r + a.nrows * (a.c0 + cl))]
+                                              : make_float2(1.f, 0.f);
+    }
     if (!(ok = wait_dft64(warp, lane, &mbar, phase, &abort_flag))) break;
     // ---- epilogue: coils of half h in pairs; the even lane takes the first coil of a
     // pair, the odd lane the second, each receiving the other part from its partner
     const float is1 = ldexpf(1.f, -e1);
     float2 acc[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-    for (int cp = h * (CB / 2); cp < (h + 1) * (CB / 2); cp += 2) {
+#pragma unroll
+    for (int i = 0; i < CB / 4; ++i) {
+      const int cp = h * (CB / 2) + 2 * i;
       float da[8], db[8];
       tmem_ld8(tl + (uint32_t)(cp * 8), da);
       tmem_ld8(tl + (uint32_t)((cp + 1) * 8), db);
@@ -296,13 +324,7 @@ __global__ void __launch_bounds__(kRThreads, 2) kt_rows_inv(TcRowsArgs t) {
       yv[3] = caddf(ev[3], make_float2(-r2 * (od[3].x + od[3].y), r2 * (od[3].x - od[3].y)));
       if (cl < t.ncg) {
 #pragma unroll
-        for (int m1 = 0; m1 < 4; ++m1) {
-          const int n = 64 * m1 + m2;
-          if (a.cmaps)
-            acc[m1] = caddf(acc[m1], cmulcf(yv[m1], a.cmaps[n + (int64_t)a.n1 * (r + a.nrows * (a.c0 + cl))]));
-          else
-            acc[m1] = caddf(acc[m1], yv[m1]);
-        }
+        for (int m1 = 0; m1 < 4; ++m1) acc[m1] = caddf(acc[m1], cmulcf(yv[m1], smap[i][m1]));
       }
     }
     // ---- coil sum: lane pair, then the two halves through shared memory
