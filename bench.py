@@ -359,9 +359,30 @@ def gb300_arm(args, world, rank, local):
         A.mul(y, x)
         torch.cuda.synchronize()
         err = float(torch.linalg.norm(yt - y) / torch.linalg.norm(y))
+        # reconstructions from the backprojection: cg(A, b; maxiter=20) with each operator, and
+        # a solve to a tolerance by refinement (fp16-tc inner CG, float32 outer residual)
+        # against float32 CG converged to the same tolerance
+        xc32 = mr.cg(A, b, maxiter=20, reltol=0.0)
+        xct = mr.cg(At, b, maxiter=20, reltol=0.0)
+        torch.cuda.synchronize()
+        cg_err = float(torch.linalg.norm(xct - xc32) / torch.linalg.norm(xc32))
+        tol = 1e-4  # float32 CG reaches it here (about 80 iterations); it stagnates near 1e-5
+        t0 = time.perf_counter()
+        conv = mr.cg(A, b, maxiter=400, reltol=tol, log=True)
+        torch.cuda.synchronize()
+        t_conv = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ref = mr.cg_refined(At, A, b, inner_iters=20, max_outer=40, tol=tol, log=True)
+        torch.cuda.synchronize()
+        t_ref = time.perf_counter() - t0
+        refined = {"tol": tol, "outer_steps": ref.iters, "inner_iters": 20, "relres": ref.resnorm,
+                   "image_rel_l2_vs_fp32": float(torch.linalg.norm(ref.x - conv.x) / torch.linalg.norm(conv.x)),
+                   "fp32_cg_iters": conv.iters, "fp32_cg_relres": conv.resnorm, "fp32_cg_s": t_conv,
+                   "refined_s": t_ref}
         mixed = {"precision": "fp16-tc", "operator": "tensor-core Λ pass (tcgen05 DFT-64, fp16 operands with per-tile "
                  "scales, fp32 accumulation), float32 row passes", "applies_s": world * 1000.0 / ms_t,
                  "ms_per_apply": ms_t, "vs_fp32": ms / ms_t, "apply_rel_l2_vs_fp32": err,
+                 "cg20_image_rel_l2_vs_fp32": cg_err, "refined_solve": refined,
                  "pass_ms": [round(p_, 5) for p_ in At.profile(x, yt, iters=20)]}
         At.close()
     if rank != 0:

@@ -230,9 +230,11 @@ int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int maxiter, do
                     int* iters_out, double* resnorm_out, mrsr_stream_t stream);
 
 /* Mixed-precision iterative refinement (no counterpart in the reference):
- * outer residual r = b - A_hi x with the float32 operator, inner CG on the
- * fp16-storage operator op_lo, until ||r|| <= tol*||b|| or max_outer.
- * op_lo and op_hi must describe the same operator. */
+ * outer residual r = b - A_hi x with the float32 operator, inner CG on a
+ * reduced-precision operator op_lo (fp16, fp16-arith or fp16-tc), until
+ * ||r|| <= tol*||b||, max_outer, or an outer step that does not lower the
+ * residual (that step is undone: x is the best iterate and relres_out its
+ * residual).  op_lo and op_hi must describe the same operator. */
 int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const float* b, float* x, int inner_iters,
                     int max_outer, double tol, int* outer_out, double* relres_out, mrsr_stream_t stream);
 

@@ -253,6 +253,15 @@ __global__ void k_axpy(float2* y, const float2* x, int64_t n) {
     y[i] = b;
   }
 }
+__global__ void k_sub(float2* y, const float2* x, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = x[i];
+    float2 b = y[i];
+    b.x -= a.x;
+    b.y -= a.y;
+    y[i] = b;
+  }
+}
 __global__ void k_norm2(const float2* a, int64_t n, double* out) {
   double acc = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -307,6 +316,7 @@ extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const
   while (outer < max_outer && relres > tol) {
     int it = 0;
     double rr = 0;
+    const double prev = relres;
     MRSR_TRY(cg_run(op_lo, op_lo->cg, r.as<float2>(), d.as<float2>(), inner_iters, 0.0, 0.0, st, &it, &rr));
     k_axpy<<<nb, kCgThreads, 0, st>>>(xx, d.as<float2>(), n);
     MRSR_LAUNCH_CHECK();
@@ -321,6 +331,15 @@ extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const
     MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
     relres = std::sqrt(hn[0]) / bnorm;
     ++outer;
+    if (!(relres < prev)) {
+      // the correction did not lower the float32 residual: at this level the inner
+      // operator's rounding dominates, so further steps only add error.  Undo the step
+      // and stop at the best iterate.
+      k_sub<<<nb, kCgThreads, 0, st>>>(xx, d.as<float2>(), n);
+      MRSR_LAUNCH_CHECK();
+      relres = prev;
+      break;
+    }
   }
   if (outer_out) *outer_out = outer;
   if (relres_out) *relres_out = relres;
