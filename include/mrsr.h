@@ -232,9 +232,9 @@ int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int maxiter, do
 /* Mixed-precision iterative refinement (no counterpart in the reference):
  * outer residual r = b - A_hi x with the float32 operator, inner CG on a
  * reduced-precision operator op_lo (fp16, fp16-arith or fp16-tc), until
- * ||r|| <= tol*||b||, max_outer, or an outer step that does not lower the
- * residual (that step is undone: x is the best iterate and relres_out its
- * residual).  op_lo and op_hi must describe the same operator. */
+ * ||r|| <= tol*||b||, max_outer, or an outer step that more than doubles
+ * the residual (that step is undone and relres_out is the residual before
+ * it).  op_lo and op_hi must describe the same operator. */
 int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const float* b, float* x, int inner_iters,
                     int max_outer, double tol, int* outer_out, double* relres_out, mrsr_stream_t stream);
 

@@ -342,31 +342,36 @@ __global__ void k_tc_absmax(const float* v, int64_t n, float* out) {
   }
 }
 
-// Λ of the chunked layout [tile][chunk][p][fc][4] (f = chunk FC + fc) rearranged for the
-// tensor-core pass: dst[tile][p][j][h][f2][part] = src(tile, f = j + 8 f2, li = 2 h + part, p).
+// Λ of the chunked layout [tile][chunk][p][fc][TC] (f = chunk FC + fc, any tile width TC)
+// rearranged for the tensor-core pass on 4-column tiles:
+// dst[tile4][p][j][h][f2][part] = src(column 4 tile4 + 2 h + part, f = j + 8 f2, p).
 template <class T>
-__global__ void k_tc_lam_layout(const T* src, T* dst, int64_t ntiles, int P, int FC, int NCH) {
-  const int64_t total = ntiles * P * kTcL * kTcTC;
+__global__ void k_tc_lam_layout(const T* src, T* dst, int64_t ntiles4, int P, int FC, int NCH, int TC) {
+  const int64_t total = ntiles4 * P * kTcL * kTcTC;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int part = (int)(e & 1), f2 = (int)((e >> 1) & 63), h = (int)((e >> 7) & 1), j = (int)((e >> 8) & 7);
-    const int64_t tp = e >> 11;  // tile * P + p
+    const int64_t tp = e >> 11;  // tile4 * P + p
     const int p = (int)(tp % P);
-    const int64_t tile = tp / P;
-    const int f = j + 8 * f2, li = 2 * h + part;
+    const int64_t col = (tp / P) * kTcTC + 2 * h + part;
+    const int64_t tile = col / TC;
+    const int li = (int)(col - tile * TC);
+    const int f = j + 8 * f2;
     const int ch = f / FC, fc = f - ch * FC;
-    dst[e] = src[(((tile * NCH + ch) * P + p) * (int64_t)FC + fc) * kTcTC + li];
+    dst[e] = src[(((tile * NCH + ch) * P + p) * (int64_t)FC + fc) * TC + li];
   }
 }
 
-int tc_lambda_layout(const void* lam, void* out, int64_t ntiles, int P, int FC, int NCH, bool real, cudaStream_t st) {
-  const int64_t total = ntiles * P * kTcL * kTcTC;
+int tc_lambda_layout(const void* lam, void* out, int64_t inner, int P, int FC, int NCH, int TC, bool real,
+                     cudaStream_t st) {
+  const int64_t ntiles4 = inner / kTcTC;
+  const int64_t total = ntiles4 * P * kTcL * kTcTC;
   const unsigned grid = (unsigned)std::min<int64_t>((total + 255) / 256, 8192);
   if (real)
     k_tc_lam_layout<float><<<grid, 256, 0, st>>>(reinterpret_cast<const float*>(lam), reinterpret_cast<float*>(out),
-                                                   ntiles, P, FC, NCH);
+                                                   ntiles4, P, FC, NCH, TC);
   else
     k_tc_lam_layout<float2><<<grid, 256, 0, st>>>(reinterpret_cast<const float2*>(lam), reinterpret_cast<float2*>(out),
-                                                    ntiles, P, FC, NCH);
+                                                    ntiles4, P, FC, NCH, TC);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
 }
@@ -390,14 +395,15 @@ int tc_build_constants(void* out, cudaStream_t st) {
 
 size_t tc_constants_bytes() { return tcdft::kConstBytes; }
 
-bool tc_lambda_supported(int L, int nin, int nout, int TC, int K) {
-  return L == kTcL && nin * 2 == L && nout * 2 == L && TC == kTcTC && K >= 1 && K <= KMAX;
+bool tc_lambda_supported(int L, int nin, int nout, int inner, int K) {
+  return L == kTcL && nin * 2 == L && nout * 2 == L && inner % kTcTC == 0 && K >= 1 && K <= KMAX;
 }
 
 int tc_lambda(const LamPassArgs& a, int ncg, const float* lam_max, const void* consts, int* errword,
               cudaStream_t st) {
-  MRSR_REQUIRE(tc_lambda_supported(a.pl.L, a.nin, a.nout, a.TC, a.K), MRSR_ERR_UNSUPPORTED,
-               "tensor-core Λ pass: needs a 512-point pruned column transform, 4-column tiles and K <= 8");
+  MRSR_REQUIRE(tc_lambda_supported(a.pl.L, a.nin, a.nout, (int)a.inner, a.K), MRSR_ERR_UNSUPPORTED,
+               "tensor-core Λ pass: needs a 512-point pruned column transform, a plane width divisible by 4 "
+               "and K <= 8");
   MRSR_REQUIRE(lam_max, MRSR_ERR_STATE, "tensor-core Λ pass: the kernel bound was not computed");
   TcArgs t{a, (int64_t)(a.inner / kTcTC) * ncg, errword, lam_max, reinterpret_cast<const unsigned char*>(consts)};
   t.a.ncg = ncg;

@@ -595,12 +595,10 @@ int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_
   int TC = (int)env_int("MRSR_LAMBDA_TC", 8);
   const int64_t budget = fast_length((int)g.glast()) ? 13000 : 12288;
   while (TC > 1 && ((int64_t)K * TC * g.glast() > budget || g.inner() % TC != 0)) TC >>= 1;
-  if (precision == MRSR_PREC_FP16_TC) TC = 4;  // the tensor-core Λ pass works on 4-column tiles
   op->TC = TC;
   if (precision == MRSR_PREC_FP16_TC) {
     const int nl = (int)g.n[ndims - 1], gl = (int)g.glast();
-    MRSR_REQUIRE(kind == MRSR_KIND_NFFT && tc_lambda_supported(gl, nl, nl, TC, K) && g.inner() % TC == 0,
-                 MRSR_ERR_UNSUPPORTED,
+    MRSR_REQUIRE(kind == MRSR_KIND_NFFT && tc_lambda_supported(gl, nl, nl, (int)g.inner(), K), MRSR_ERR_UNSUPPORTED,
                  "the tensor-core Λ pass needs an NFFT operator whose last grid length is 512 (got %d)", gl);
   }
   MRSR_TRY(op->errflag.alloc(sizeof(int)));
@@ -664,10 +662,9 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
     MRSR_TRY(tc_build_constants(op->tc_consts.p, st));
     MRSR_TRY(op->lam_max.alloc(sizeof(float)));
     MRSR_TRY(tc_lambda_bound(op->lam.p, op->lam.bytes, op->lam_max.as<float>(), st));
-    const int64_t ntiles = g.inner() / op->TC;
     const size_t esz = op->lam_mode == LAM_PACKED_REAL ? sizeof(float) : sizeof(float2);
-    MRSR_TRY(op->lam_tc.alloc(esz * (size_t)ntiles * op->P * g.glast() * op->TC));
-    MRSR_TRY(tc_lambda_layout(op->lam.p, op->lam_tc.p, ntiles, op->P, op->FC, (int)(g.glast() / op->FC),
+    MRSR_TRY(op->lam_tc.alloc(esz * (size_t)g.inner() * op->P * g.glast()));
+    MRSR_TRY(tc_lambda_layout(op->lam.p, op->lam_tc.p, g.inner(), op->P, op->FC, (int)(g.glast() / op->FC), op->TC,
                               op->lam_mode == LAM_PACKED_REAL, st));
   }
   // the operator's buffers came from the pool on `st`: make them usable on any stream

@@ -140,8 +140,8 @@ int fast_lambda(const LamPassArgs& a, int ncg, int planes_total, int* errword, c
 int fast_mid(const MidArgs& a, int nplanes, cudaStream_t st);
 int fast_rows_inv(const RowsInvArgs& a, int64_t nrows, cudaStream_t st);
 
-// tensor-core Λ pass (apply_tc.cu): 512-point pruned column transforms, 4-column tiles
-bool tc_lambda_supported(int L, int nin, int nout, int TC, int K);
+// tensor-core Λ pass (apply_tc.cu): 512-point pruned column transforms on 4-column tiles
+bool tc_lambda_supported(int L, int nin, int nout, int inner, int K);
 int tc_lambda(const LamPassArgs& a, int ncg, const float* lam_max, const void* consts, int* errword,
               cudaStream_t st);
 int tc_build_constants(void* out, cudaStream_t st);  // DFT-64 operand + twiddles, tc_constants_bytes()
@@ -150,7 +150,8 @@ int tc_lambda_bound(const void* lam, size_t bytes, float* out, cudaStream_t st);
 bool tc_rows_supported(int L, int n1, int ncg);
 int tc_rows_fwd(const RowsFwdArgs& a, int ncg, const void* consts, int* errword, cudaStream_t st);
 int tc_rows_inv(const RowsInvArgs& a, const void* consts, int* errword, cudaStream_t st);
-int tc_lambda_layout(const void* lam, void* out, int64_t ntiles, int P, int FC, int NCH, bool real, cudaStream_t st);
+int tc_lambda_layout(const void* lam, void* out, int64_t inner, int P, int FC, int NCH, int TC, bool real,
+                     cudaStream_t st);
 
 // fp16-storage operator (apply_half.cu)
 bool half_supported(const mrsr_normalop* op);

@@ -45,8 +45,7 @@ def cg(A, b, maxiter=None, reltol=DEFAULT_RELTOL, abstol=0.0, log=False, stream=
 def cg_refined(A_lo, A_hi, b, inner_iters=20, max_outer=10, tol=1e-4, log=False, stream=None):
     """Mixed-precision iterative refinement: x <- x + CG_lo(b - A_hi x) until
     ||b - A_hi x|| <= tol ||b|| (A_lo a reduced-precision operator, A_hi float32),
-    or until a step fails to lower that residual (the step is undone: x is the best
-    iterate)."""
+    or until a step more than doubles that residual (the step is undone)."""
     lib = _lib.load()
     bi = A_hi._as_image(b)
     x = jl_empty(bi.shape, torch.complex64)

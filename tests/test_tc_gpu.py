@@ -97,3 +97,48 @@ def test_tc_rejects_other_grids(mr, cuda):
     lam, cells, cm, _ = _problem(8, (128, 128), 3, 1)
     with pytest.raises(NotImplementedError):
         mr.NFFTNormalOp((128, 128), lam, cells, cmaps=[cm[..., 0]], precision="fp16-tc")
+
+
+def _radial_tc(seed=6, N=256, K=4, Nt=40, Nc=2):
+    rng = np.random.default_rng(seed)
+    trj = otraj.traj_2d_radial_goldenratio(2 * N, 8, Nt)
+    U = np.linalg.svd(rng.standard_normal((Nt, K)), full_matrices=False)[0].astype(np.float32)
+    cm = rand_c(rng, (N, N, Nc))
+    return rng, trj, U, [cm[..., c] for c in range(Nc)]
+
+
+def test_tc_refinement_reaches_float32_residual(mr, cuda):
+    """Refinement with the tensor-core operator inside, float32 outer residual, on a
+    well-determined problem (32 spokes x 20 frames, 8 coils, K=3).  The operator is shared
+    from a float32 one whose Λ tiles are 8 columns wide (K=3)."""
+    rng = np.random.default_rng(6)
+    N, K, Nt, Nc = 256, 3, 20, 8
+    trj = otraj.traj_2d_radial_goldenratio(2 * N, 32, Nt)
+    U = np.linalg.svd(rng.standard_normal((Nt, K)), full_matrices=False)[0].astype(np.float32)
+    cm = rand_c(rng, (N, N, Nc))
+    cml = [cm[..., c] for c in range(Nc)]
+    A32 = mr.NFFTNormalOp((N, N), trj, U, cmaps=cml)
+    At = A32.share(cmaps=cml, precision="fp16-tc")
+    x_true = mr.to_jl(rand_c(rng, (N, N, K)), torch.complex64)
+    assert rel_l2(mr.to_host(At @ x_true), mr.to_host(A32 @ x_true)) < TOL
+    bt = A32 @ x_true
+    res = mr.cg_refined(At, A32, bt, inner_iters=30, max_outer=20, tol=1e-4, log=True)
+    print(f"fp16-tc refined: outer {res.iters}, residual {res.resnorm:.2e}")
+    assert res.resnorm <= 1e-4
+
+
+def test_tc_in_cg_batch_graph(mr, cuda):
+    """The tensor-core passes inside a captured CUDA graph (the serving path): each branch
+    equals cg on the same operator."""
+    rng, trj, U, cml = _radial_tc(seed=7, K=3)
+    N, K = 256, U.shape[1]
+    base = mr.NFFTNormalOp((N, N), trj, U, cmaps=cml, precision="fp16-tc")
+    ops = [base, base.share(cmaps=cml)]
+    bs = [mr.to_jl(rand_c(rng, (N, N, K)), torch.complex64) for _ in ops]
+    refs = [mr.to_host(mr.cg(A, b, maxiter=5, reltol=0.0)) for A, b in zip(ops, bs)]
+    xs = [mr.jl_empty(b.shape, torch.complex64) for b in bs]
+    batch = mr.CgBatch(ops, bs, xs, 5)
+    batch.launch()
+    torch.cuda.synchronize()
+    for x, r in zip(xs, refs):
+        assert rel_l2(mr.to_host(x), r) < 1e-6
