@@ -327,19 +327,30 @@ int launch_tc(const TcArgs& t, cudaStream_t st) {
 
 }  // namespace
 
-// out[0] = max |component| over n floats (one CTA; run once per operator)
+// out[0] = max |component| over n floats (run once per operator; out[0] zeroed first).
+// Non-negative floats order like their bit patterns, so the grid combines with atomicMax.
 __global__ void k_tc_absmax(const float* v, int64_t n, float* out) {
   __shared__ float red[32];
   float m = 0.f;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) m = fmaxf(m, fabsf(v[i]));
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(v[i]));
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
     float r = 0.f;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmaxf(r, red[w]);
-    out[0] = r;
+    atomicMax(reinterpret_cast<int*>(out), __float_as_int(r));
   }
+}
+
+int tc_lambda_bound(const void* lam, size_t bytes, float* out, cudaStream_t st) {
+  MRSR_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(float), st));
+  const int64_t n = (int64_t)(bytes / sizeof(float));
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 1023) / 1024, 2048));
+  k_tc_absmax<<<grid, 1024, 0, st>>>(reinterpret_cast<const float*>(lam), n, out);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
 }
 
 // Λ of the chunked layout [tile][chunk][p][fc][TC] (f = chunk FC + fc, any tile width TC)
@@ -376,11 +387,6 @@ int tc_lambda_layout(const void* lam, void* out, int64_t inner, int P, int FC, i
   return MRSR_OK;
 }
 
-int tc_lambda_bound(const void* lam, size_t bytes, float* out, cudaStream_t st) {
-  k_tc_absmax<<<1, 1024, 0, st>>>(reinterpret_cast<const float*>(lam), (int64_t)(bytes / sizeof(float)), out);
-  MRSR_LAUNCH_CHECK();
-  return MRSR_OK;
-}
 
 __global__ void k_tc_constants(unsigned char* g) {
   tcdft::setup_constants(g, reinterpret_cast<float2*>(g + tcdft::kAbytes), threadIdx.x + blockIdx.x * blockDim.x,
