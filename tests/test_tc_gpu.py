@@ -142,3 +142,16 @@ def test_tc_in_cg_batch_graph(mr, cuda):
     torch.cuda.synchronize()
     for x, r in zip(xs, refs):
         assert rel_l2(mr.to_host(x), r) < 1e-6
+
+
+def test_tc_3d_operator(mr, cuda):
+    """3D: the tensor-core row and Λ passes (512-point lines along dims 1 and 3) around the
+    float32 middle pass along dim 2."""
+    img, K, Nc = (256, 8, 256), 3, 2
+    lam, cells, cm, x = _problem(51, img, K, Nc, density=0.6, complex_lam=False)
+    cml = [cm[..., c] for c in range(Nc)]
+    A = mr.NFFTNormalOp(img, lam, cells, cmaps=cml, precision="fp16-tc")
+    ref = onormal.nfft_normalop_apply(x, onormal.unpack_lambda(lam.astype(np.complex128), K), cells, img, cmaps=cml)
+    err = rel_l2(mr.to_host(A @ x), ref)
+    print(f"fp16-tc 3D apply: rel L2 {err:.2e}")
+    assert err < TOL
