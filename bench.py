@@ -48,7 +48,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SERVED, PIPE3D, PIPEGROG])
-    p.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "fp16-tc", "refined"],
+    p.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "fp16-tc", "refined", "refined-tc"],
                    help="operator storage: fp32, fp16 (per-tile scaled half stacks and kernel); "
                         "refined (served workload only: fp16 inner CG + float32 residual steps)")
     p.add_argument("--rate", type=float, default=40.0, help="served workload: Poisson arrival rate (requests/s)")
@@ -255,7 +255,8 @@ def gb300_arm(args, world, rank, local):
     # operator: Toeplitz kernel precompute on the device (timed once, reported beside the headline)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    prec = args.precision if args.precision in ("fp32", "fp16-tc") else "fp16"
+    prec = {"fp32": "fp32", "fp16": "fp16", "refined": "fp16", "fp16-tc": "fp16-tc", "refined-tc": "fp16-tc"}[
+        args.precision]
     A = mr.NFFTNormalOp(w["img"], trj, U, cmaps=cm, precision=prec)
     esz, lsz = (4, 2) if prec == "fp16" else (8, 4)   # bytes per stack element / per real kernel entry
     torch.cuda.synchronize()
@@ -488,7 +489,7 @@ def served_arm(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "c64" if args.precision == "fp32" else "c64/f16",
         "data": "synthetic (8 seeded protocols, one 32-coil scan each, forward model + 1% noise)",
         "config": {"workload": SERVED, "requests": st.completed, "rate_hz": args.rate, "precision": args.precision,
-                   "cg_iters": iters, "outer_steps": 2 if args.precision == "refined" else None, "slots": 4,
+                   "cg_iters": iters, "outer_steps": 2 if args.precision.startswith("refined") else None, "slots": 4,
                    "max_batch": 4, "hbm_budget_gb": budget / 2 ** 30,
                    "protocols": [p.name for p in protos], "coils": [8, 32],
                    "parallelism": f"replicas x{world}", "l2": "inputs (per-request data 7-295 MB) stream through"},

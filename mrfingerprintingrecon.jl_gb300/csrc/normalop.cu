@@ -657,7 +657,7 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
     else
       MRSR_TRY(half_alloc_scales(op));
   }
-  if (op->precision == MRSR_PREC_FP16_TC) {
+  if (op->precision == MRSR_PREC_FP16_TC && !op->lam_tc.p) {  // a shared kernel may already have them
     MRSR_TRY(op->tc_consts.alloc(tc_constants_bytes()));
     MRSR_TRY(tc_build_constants(op->tc_consts.p, st));
     MRSR_TRY(op->lam_max.alloc(sizeof(float)));

@@ -35,6 +35,9 @@ struct LamStore {
   DevBuf lam;        // [tile][chunk][P][FC][TC] of float / float2 (chunked along f_last)
   DevBuf lam_scale;  // fp16: one float per tile
   DevBuf lam_half;   // fp16: the chunked kernel in half precision
+  DevBuf lam_max;    // fp16-tc: largest |component| of Λ (float)
+  DevBuf lam_tc;     // fp16-tc: Λ rearranged for the tensor-core Λ pass
+  DevBuf tc_consts;  // fp16-tc: DFT-64 MMA operand and twiddles
 };
 
 }  // namespace mrsr
@@ -43,7 +46,7 @@ struct mrsr_normalop {
   mrsr_normalop() : mrsr_normalop(std::make_shared<mrsr::LamStore>()) {}
   explicit mrsr_normalop(std::shared_ptr<mrsr::LamStore> s)
       : store(std::move(s)), kmask(store->kmask), lam(store->lam), lam_scale(store->lam_scale),
-        lam_half(store->lam_half) {}
+        lam_half(store->lam_half), lam_max(store->lam_max), lam_tc(store->lam_tc), tc_consts(store->tc_consts) {}
   mrsr_normalop(const mrsr_normalop&) = delete;
   mrsr_normalop& operator=(const mrsr_normalop&) = delete;
 
@@ -62,13 +65,13 @@ struct mrsr_normalop {
   mrsr::DevBuf& lam;
   mrsr::DevBuf& lam_scale;
   mrsr::DevBuf& lam_half;
+  mrsr::DevBuf& lam_max;   // the fp16-tc members are built once per kernel and shared
+  mrsr::DevBuf& lam_tc;
+  mrsr::DevBuf& tc_consts;
   mrsr::DevBuf cmaps;      // (img..., ncoils) complex; empty = unit coil
   mrsr::DevBuf stack1, stack2;  // intermediates of one coil group
   mrsr::DevBuf scale1, scale2;  // fp16 per-line scales
   mrsr::DevBuf errflag;         // device int
-  mrsr::DevBuf lam_max;         // device float: largest |component| of Λ (tensor-core Λ pass)
-  mrsr::DevBuf lam_tc;          // Λ rearranged for the tensor-core Λ pass
-  mrsr::DevBuf tc_consts;       // DFT-64 MMA operand and twiddles of the tensor-core passes
   mrsr::FftPlanHost plan[3];
   mrsr::CgWork cg;              // CG vectors, allocated on first solve
   // recorded after every call that enqueues work on the operator; the

@@ -98,15 +98,22 @@ def _prod(t):
     return int(np.prod([int(v) for v in t]))
 
 
-def kernel_bytes(img, K, nk=None, complex_kernel=False, fp16=False):
-    """Device bytes of one cached kernel: Λ over the 2x grid (+ fp16 copy) and the kmask."""
+def tc_grid(img):
+    """The tensor-core operator needs 512-point lines along dims 1 and the last one."""
+    return len(img) in (2, 3) and 2 * img[0] == 512 and 2 * img[-1] == 512
+
+
+def kernel_bytes(img, K, nk=None, complex_kernel=False, fp16=False, tc=False):
+    """Device bytes of one cached kernel: Λ over the 2x grid (+ fp16 copy, + the tensor-core
+    layout) and the kmask."""
     G = _prod(2 * int(n) for n in img)
     P = K * (K + 1) // 2
     lam = P * G * (8 if complex_kernel else 4)
     half = P * G * (4 if complex_kernel else 2) if fp16 else 0
+    tcl = lam + 36864 if tc else 0  # rearranged copy + DFT-64 operand and twiddles
     nk = G if nk is None else nk
     base_stack = K * 2 * _prod(img) * 8  # the cache's own one-coil operator
-    return lam + half + 8 * nk + base_stack
+    return lam + half + tcl + 8 * nk + base_stack
 
 
 def request_bytes(img, K, nc, precision="fp32", refine=False):
@@ -326,15 +333,18 @@ class GpuExecutor:
     """Device work of the server: kernels, backprojections and graph-captured CG batches.
 
     ``precision``: "fp32" (cg on the float32 operator), "fp16" (cg on the
-    fp16-storage operator) or "refined" (fp16 inner CG with ``outer`` float32
-    residual corrections, all inside one graph).  Matrix sizes whose 2x grid
-    is not a four-step length run the float32 operator in every mode.
+    fp16-storage operator), "refined" (fp16 inner CG with ``outer`` float32
+    residual corrections, all inside one graph), "fp16-tc" / "refined-tc" (the
+    same with the tensor-core operator).  Matrix sizes without the reduced
+    form (fp16: a four-step 2x grid; fp16-tc: 512-point lines, i.e. 256
+    samples along dims 1 and last) run the float32 operator in every mode.
     """
+    PRECISIONS = ("fp32", "fp16", "refined", "fp16-tc", "refined-tc")
 
     def __init__(self, mr, iters=20, precision="fp32", outer=2, keep_results=True):
         import torch
-        if precision not in ("fp32", "fp16", "refined"):
-            raise ValueError("precision must be fp32, fp16 or refined")
+        if precision not in self.PRECISIONS:
+            raise ValueError("precision must be one of " + ", ".join(self.PRECISIONS))
         self.mr = mr
         self.torch = torch
         self.iters = iters
@@ -348,13 +358,17 @@ class GpuExecutor:
             self.streams[si] = self.torch.cuda.Stream()
         return self.streams[si]
 
+    def _tc(self):
+        return self.precision in ("fp16-tc", "refined-tc")
+
     def kernel_bytes(self, proto):
         return kernel_bytes(proto.img, proto.K, complex_kernel=self.torch.is_complex(proto.U),
-                            fp16=self.precision != "fp32")
+                            fp16=self.precision in ("fp16", "refined"), tc=self._tc() and tc_grid(proto.img))
 
     def request_bytes(self, r):
         return request_bytes(r.protocol.img, r.protocol.K, r.ncoils,
-                             "fp16" if self.precision != "fp32" else "fp32", refine=self.precision == "refined")
+                             "fp16" if self.precision in ("fp16", "refined") else "fp32",
+                             refine=self.precision in ("refined", "refined-tc"))
 
     def build_kernel(self, proto, si):
         s = self._stream(si)
@@ -367,10 +381,14 @@ class GpuExecutor:
     def start(self, si, batch, kern):
         torch, mr = self.torch, self.mr
         s = self._stream(si)
-        # fp16 storage exists for the register four-step lengths; other matrix sizes run float32
-        mixed = self.precision != "fp32" and all(2 * n in FOUR_STEP_LENGTHS for n in batch[0].protocol.img)
-        lo_prec = "fp16" if mixed else "fp32"
-        refined = mixed and self.precision == "refined"
+        # the reduced forms exist for some matrix sizes only; the others run float32
+        img = batch[0].protocol.img
+        if self._tc():
+            mixed, lo_prec = tc_grid(img), "fp16-tc"
+        else:
+            mixed, lo_prec = self.precision != "fp32" and all(2 * n in FOUR_STEP_LENGTHS for n in img), "fp16"
+        lo_prec = lo_prec if mixed else "fp32"
+        refined = mixed and self.precision in ("refined", "refined-tc")
         with torch.cuda.stream(s):
             ops, ops_hi, bs, xs = [], [], [], []
             for r in batch:

@@ -174,3 +174,12 @@ def test_protocol_key_depends_on_trajectory_basis_and_size(sv):
     assert k != sv.protocol_key(trj, U, (8, 16))
     assert k != sv.protocol_key(trj, U * 2, (8, 8))
     assert not math.isnan(sv.Request(rid=0, protocol=None, data=None, cmaps=_Cm(3), arrival=1.0).arrival)
+
+
+def test_tensor_core_sizes_and_bytes(sv, mr):
+    assert sv.tc_grid((256, 256)) and sv.tc_grid((256, 64, 256))
+    assert not sv.tc_grid((128, 128)) and not sv.tc_grid((256, 128))
+    assert sv.kernel_bytes((256, 256), 5, tc=True) > sv.kernel_bytes((256, 256), 5)
+    with pytest.raises(ValueError):
+        sv.GpuExecutor(mr, precision="bf16")
+    assert set(sv.GpuExecutor.PRECISIONS) >= {"fp16-tc", "refined-tc"}

@@ -125,3 +125,31 @@ def test_server_refined_precision(mr, cuda, sv):
         res[outer] = [r.resnorm for r in rq]
     assert all(np.isfinite(v) for v in res[1] + res[3])
     assert all(a3 < a1 for a1, a3 in zip(res[1], res[3]))
+
+
+def test_server_tensor_core_precision(mr, cuda, sv):
+    """fp16-tc serving: the 256^2 protocol runs the tensor-core operator and equals the direct
+    API calls with it; the 32^2 protocol falls back to float32.  The direct calls rebuild the
+    kernel and the backprojection (float atomics: last-bit differences), and fp16 rounding
+    turns a last-bit difference near a rounding boundary into an fp16 ulp (~5e-4), so the
+    tensor-core results agree to the mixed-precision tolerance, 1e-3; float32 to 1e-5."""
+    protos = []
+    for i, (N, K, Nt) in enumerate(((256, 3, 24), (32, 3, 24))):
+        trj = mr.trajectories.traj_2d_radial_goldenratio(2 * N, 2, Nt, thetaRot=0.2 * i)
+        U = mr.synthetic.basis(mr.synthetic.dictionary(Nt, natoms=200, seed=i), K)
+        protos.append(sv.Protocol(name=f"p{i}", img=(N, N), trj=mr.to_jl(trj, torch.float32),
+                                  U=mr.to_jl(U, torch.float32), K=K))
+    scans = [sv.make_scans(mr, p, 3, seed=20 + i) for i, p in enumerate(protos)]
+    torch.cuda.synchronize()
+    reqs = sv.make_request_stream(protos, scans, 4, rate_hz=0.0, coil_range=(2, 3), seed=5)
+    iters = 6
+    srv = sv.ReconServer(sv.GpuExecutor(mr, iters=iters, precision="fp16-tc"), 8 << 30, slots=2, max_batch=2)
+    srv.run(reqs)
+    srv.close()
+    for r in reqs:
+        p = r.protocol
+        prec = "fp16-tc" if p.img[0] == 256 else "fp32"
+        A = mr.NFFTNormalOp(p.img, p.trj, p.U, cmaps=r.cmaps, precision=prec)
+        b = mr.calculate_backprojection(r.data, p.trj, r.cmaps, U=p.U)
+        x = mr.to_host(mr.cg(A, b, maxiter=iters, reltol=0.0))
+        assert rel_l2(x, mr.to_host(r.x)) < (1e-3 if prec == "fp16-tc" else 1e-5), (r.rid, prec)
