@@ -95,7 +95,48 @@ template <class SP, int KK>
 __device__ __forceinline__ void lam_voxels(const LamPassArgs& a, float2* sm, const Slots& sl, int64_t tile) {
   constexpr int R1 = SP::R1, L = SP::L;
   const int64_t pstride = (int64_t)a.FC * a.TC;
-  for (int t = threadIdx.x; t < (L << sl.tcs); t += blockDim.x) {
+  const int T = L << sl.tcs;
+  if (a.lam_mode == LAM_PACKED_REAL) {
+    // packed real kernel: the next voxel's entries load while this one is multiplied
+    constexpr int P = KK * (KK + 1) / 2;
+    const float* lam = reinterpret_cast<const float*>(a.lam);
+    auto lbase_of = [&](int tt) -> int64_t {
+      const int f = tt >> sl.tcs;
+      const int ch = (int)a.fcd.div((uint32_t)f), fc = f - ch * a.FC;
+      return (((tile * a.NCH + ch) * a.P) * (int64_t)a.FC + fc) * a.TC + (tt & (a.TC - 1));
+    };
+    float lc[P];
+    int t = threadIdx.x;
+    if (t < T) {
+      const int64_t lb = lbase_of(t);
+#pragma unroll
+      for (int p = 0; p < P; ++p) lc[p] = lam[lb + p * pstride];
+    }
+    for (; t < T; t += blockDim.x) {
+      const int tn = t + (int)blockDim.x;
+      float ln[P];
+      if (tn < T) {
+        const int64_t lb = lbase_of(tn);
+#pragma unroll
+        for (int p = 0; p < P; ++p) ln[p] = lam[lb + p * pstride];
+      }
+      const int li = t & (a.TC - 1);
+      const int f = t >> sl.tcs;
+      const int f1 = f % R1, f2 = f / R1;
+      float2 X[KK], Y[KK];
+#pragma unroll
+      for (int k = 0; k < KK; ++k) X[k] = sm[sl.at(k, f1, f2, li, R1)];
+      lam_real_regs<KK>(lc, X, Y);
+#pragma unroll
+      for (int k = 0; k < KK; ++k) sm[sl.at(k, f1, f2, li, R1)] = Y[k];
+      if (tn < T) {
+#pragma unroll
+        for (int p = 0; p < P; ++p) lc[p] = ln[p];
+      }
+    }
+    return;
+  }
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
     const int li = t & (a.TC - 1);
     const int f = t >> sl.tcs;          // f = f1 + R1 f2
     const int f1 = f % R1, f2 = f / R1;

@@ -57,25 +57,6 @@ __device__ __forceinline__ uint32_t boff(int r, int kk) {
 __host__ __device__ constexpr size_t tc_bbytes(int K) { return (size_t)K * 4 * kTcSbo; }
 constexpr int kTcStg = kTcTC + 1;  // staging row stride (float2), padded against bank conflicts
 
-// Y = Λ X at one voxel for the packed real kernel, Λ values already in registers.
-template <int K>
-__device__ __forceinline__ void lam_real_regs(const float* l, const float2* X, float2* Y) {
-#pragma unroll
-  for (int k = 0; k < K; ++k) Y[k] = make_float2(0.f, 0.f);
-  int p = 0;
-#pragma unroll
-  for (int k2 = 0; k2 < K; ++k2)
-#pragma unroll
-    for (int k1 = 0; k1 <= k2; ++k1, ++p) {
-      Y[k1].x = fmaf(l[p], X[k2].x, Y[k1].x);
-      Y[k1].y = fmaf(l[p], X[k2].y, Y[k1].y);
-      if (k1 != k2) {
-        Y[k2].x = fmaf(l[p], X[k1].x, Y[k2].x);
-        Y[k2].y = fmaf(l[p], X[k1].y, Y[k2].y);
-      }
-    }
-}
-
 template <int K>
 __global__ void __launch_bounds__(kTcThreads, K <= 5 ? 2 : 1) kt_lambda(TcArgs t) {
   const LamPassArgs& a = t.a;

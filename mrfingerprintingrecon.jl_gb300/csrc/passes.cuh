@@ -126,6 +126,25 @@ __device__ __forceinline__ void lam_apply_ptr(int mode, int K, const void* lamv,
   }
 }
 
+// Y = Λ X at one voxel for the packed real kernel, Λ values already in registers.
+template <int K>
+__device__ __forceinline__ void lam_real_regs(const float* l, const float2* X, float2* Y) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) Y[k] = make_float2(0.f, 0.f);
+  int p = 0;
+#pragma unroll
+  for (int k2 = 0; k2 < K; ++k2)
+#pragma unroll
+    for (int k1 = 0; k1 <= k2; ++k1, ++p) {
+      Y[k1].x = fmaf(l[p], X[k2].x, Y[k1].x);
+      Y[k1].y = fmaf(l[p], X[k2].y, Y[k1].y);
+      if (k1 != k2) {
+        Y[k2].x = fmaf(l[p], X[k1].x, Y[k2].x);
+        Y[k2].y = fmaf(l[p], X[k1].y, Y[k2].y);
+      }
+    }
+}
+
 template <int KM>
 __device__ __forceinline__ void lam_apply(const LamPassArgs& a, int64_t lbase, int64_t pstride, const float2* X,
                                           float2* Y) {
