@@ -183,18 +183,33 @@ __device__ void gj_solve(C* M, C* R, int n, GjStep<C>& st) {
     const bool sing = st.sing[b] != 0;
     const C rinv = st.rinv[b];
     const C f = lane < n ? st.f[b][lane] : cx_zero<C>();
-    for (int c = k + 1 + warp; c < 2 * n; c += nw) {
-      C* col = c < n ? M + n * c : R + n * (c - n);
-      const C vr = lane < n ? col[lane] : cx_zero<C>();
+    // new value of row `lane` of column c from its old value vr
+    auto update = [&](int c, C vr) -> C {
       const C vk = cx_shfl(vr, k), vp = cx_shfl(vr, p);
       const C own = lane == p ? vk : vr;  // row `lane` after the swap of rows k and p
-      C nv;
-      if (sing) {
-        nv = lane == k ? (c < n ? vp : cx_zero<C>()) : own;
-      } else {
-        const C rk = cx_mul(vp, rinv);
-        nv = lane == k ? rk : cx_sub(own, cx_mul(f, rk));
+      if (sing) return lane == k ? (c < n ? vp : cx_zero<C>()) : own;
+      const C rk = cx_mul(vp, rinv);
+      return lane == k ? rk : cx_sub(own, cx_mul(f, rk));
+    };
+    auto column = [&](int c) -> C* { return c < n ? M + n * c : R + n * (c - n); };
+    int c = k + 1 + warp;
+    // two columns at a time, so the loads and shuffles of one overlap those of the other;
+    // the warp's first column is k + 1 only in the first pair (warp 0)
+    for (; c + nw < 2 * n; c += 2 * nw) {
+      C* col0 = column(c);
+      C* col1 = column(c + nw);
+      const C v0 = lane < n ? col0[lane] : cx_zero<C>();
+      const C v1 = lane < n ? col1[lane] : cx_zero<C>();
+      const C n0 = update(c, v0), n1 = update(c + nw, v1);
+      if (lane < n) {
+        col0[lane] = n0;
+        col1[lane] = n1;
       }
+      if (c == k + 1 && c < n) gj_pivot(n0, k + 1, n, st, b ^ 1);
+    }
+    if (c < 2 * n) {
+      C* col = column(c);
+      const C nv = update(c, lane < n ? col[lane] : cx_zero<C>());
       if (lane < n) col[lane] = nv;
       if (c == k + 1 && c < n) gj_pivot(nv, k + 1, n, st, b ^ 1);
     }
