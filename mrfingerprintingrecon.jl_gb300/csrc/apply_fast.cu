@@ -32,14 +32,18 @@ __global__ void __launch_bounds__(512) k4_rows_fwd(RowsFwdArgs a, Slots sl) {
   const int NO = a.rpc * a.K;
   constexpr int nload = PR ? R1 / 2 : R1;
   __syncthreads();
-  step_a<SP, -1>(sm, sl, NO, tw, nload, [&](int lo, int, int n) -> float2 {
+  auto ld = [&](int lo, int, int n) -> float2 {
     const int rl = lo / a.K, k = lo - rl * a.K;
     if (rl >= nr || (!PR && n >= a.n1)) return make_float2(0.f, 0.f);
     const int64_t r = row0 + rl;
     float2 v = a.x[n + (int64_t)a.n1 * (r + a.nrows * k)];
     if (a.cmaps) v = cmul(a.cmaps[n + (int64_t)a.n1 * (r + a.nrows * c)], v);
     return v;
-  });
+  };
+  if constexpr (PR)
+    step_a_pf<SP, -1, nload>(sm, sl, NO, tw, ld);  // the zero-padded half leaves registers for the prefetch
+  else
+    step_a<SP, -1>(sm, sl, NO, tw, nload, ld);
   __syncthreads();
   step_b<SP, -1>(sm, sl, NO, R2, [&](int lo, int, int f1, int f2, float2 v) {
     const int rl = lo / a.K, k = lo - rl * a.K;
@@ -60,7 +64,7 @@ __global__ void __launch_bounds__(512) k4_rows_inv(RowsInvArgs a, Slots sl) {
   const int NO = a.rpc * a.ncg;
   constexpr int nkeep = PR ? R2 / 2 : R2;
   __syncthreads();
-  step_a<SP, +1>(sm, sl, NO, tw, R1, [&](int lo, int, int m) -> float2 {
+  step_a_pf<SP, +1, R1>(sm, sl, NO, tw, [&](int lo, int, int m) -> float2 {
     const int rl = lo / a.ncg, cl = lo - rl * a.ncg;
     if (rl >= nr) return make_float2(0.f, 0.f);
     return a.stack[(((int64_t)cl * a.K + k) * a.nrows + row0 + rl) * L + m];

@@ -124,6 +124,41 @@ __device__ __forceinline__ void step_a(float2* sm, const Slots& sl, int NO, cons
   }
 }
 
+// Step A with the task loop software-pipelined: the inputs of the thread's next task are
+// loaded before the current task's DFT, so their latency overlaps it.  NLOAD inputs per
+// task are read (the rest are zero), which costs NLOAD extra registers.
+template <class SP, int S, int NLOAD, class LD>
+__device__ __forceinline__ void step_a_pf(float2* sm, const Slots& sl, int NO, const float2* tw, LD ld) {
+  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
+  const int ntask = (NO * R2) << sl.tcs;
+  auto load = [&](int t, float2* v) {
+    const int li = t & (sl.TC - 1);
+    const int r = t >> sl.tcs;
+    const int n2 = r % R2;
+    const int lo = r / R2;
+#pragma unroll
+    for (int n1 = 0; n1 < NLOAD; ++n1) v[n1] = ld(lo, li, R2 * n1 + n2);
+  };
+  float2 nxt[NLOAD];
+  if ((int)threadIdx.x < ntask) load(threadIdx.x, nxt);
+  for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
+    const int li = t & (sl.TC - 1);
+    const int r = t >> sl.tcs;
+    const int n2 = r % R2;
+    const int lo = r / R2;
+    float2 v[R1];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) v[n1] = n1 < NLOAD ? nxt[n1] : make_float2(0.f, 0.f);
+    if (t + (int)blockDim.x < ntask) load(t + blockDim.x, nxt);
+    RDft<R1, S>::run(v);
+#pragma unroll
+    for (int f1 = 0; f1 < R1; ++f1) {
+      const float2 w = (f1 == 0) ? make_float2(1.f, 0.f) : twl<S>(tw, n2 * f1, L);
+      sm[sl.at(lo, f1, n2, li, R1)] = (f1 == 0) ? v[0] : cmul(v[f1], w);
+    }
+  }
+}
+
 // Step B.  Task (lo, li, f1) reads slot(lo, li, f1, n2) for all n2, applies
 // the R2-point DFT and hands X[f1 + R1 f2] for f2 < nkeep to st(lo, li, f1, f2, v).
 template <class SP, int S, class ST>
