@@ -378,7 +378,8 @@ def gb300_arm(args, world, rank, local):
         t_ref = time.perf_counter() - t0
         refined = {"tol": tol, "outer_steps": ref.iters, "inner_iters": 20, "relres": ref.resnorm,
                    "image_rel_l2_vs_fp32": float(torch.linalg.norm(ref.x - conv.x) / torch.linalg.norm(conv.x)),
-                   "fp32_cg_iters": conv.iters, "fp32_cg_relres": conv.resnorm, "fp32_cg_s": t_conv,
+                   "fp32_cg_iters": conv.iters, "fp32_cg_relres": conv.resnorm / float(torch.linalg.norm(b)),
+                   "fp32_cg_s": t_conv,
                    "refined_s": t_ref}
         mixed = {"precision": "fp16-tc", "operator": "tensor-core Λ pass (tcgen05 DFT-64, fp16 operands with per-tile "
                  "scales, fp32 accumulation), float32 row passes", "applies_s": world * 1000.0 / ms_t,

@@ -47,7 +47,10 @@ __device__ __forceinline__ double2 block_sum2(double2 v) {
   return s;
 }
 
-// Last block to finish sums the partials in block order; returns true in that block's thread 0.
+// The last block to finish sums the per-block partials; returns true in that block's
+// thread 0.  All its threads take part: thread t adds partials t, t + blockDim, ... in
+// that order, then the block tree combines them, so the total does not depend on which
+// block finished last or when (the reductions are deterministic run to run).
 __device__ __forceinline__ bool last_block(CgState* st, double2* partial, double2 mine, double2* total) {
   __shared__ bool is_last;
   if (threadIdx.x == 0) {
@@ -58,14 +61,15 @@ __device__ __forceinline__ bool last_block(CgState* st, double2* partial, double
   }
   __syncthreads();
   if (!is_last) return false;
+  __threadfence();
+  double2 s = make_double2(0.0, 0.0);
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    const volatile double* p = reinterpret_cast<volatile double*>(partial + b);
+    s.x += p[0];
+    s.y += p[1];
+  }
+  s = block_sum2(s);
   if (threadIdx.x == 0) {
-    __threadfence();
-    double2 s = make_double2(0.0, 0.0);
-    for (unsigned b = 0; b < gridDim.x; ++b) {
-      const volatile double* p = reinterpret_cast<volatile double*>(partial + b);
-      s.x += p[0];
-      s.y += p[1];
-    }
     *total = s;
     st->ticket = 0;
   }
