@@ -213,25 +213,36 @@ int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter
   return MRSR_OK;
 }
 
-int cg_fixed_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st) {
+int cg_fixed_init_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st) {
   CgWork& w = op->cg;
   const int64_t n = op->geo.nimg() * op->geo.K;
   MRSR_REQUIRE(w.n == n && w.r.p, MRSR_ERR_STATE, "CG work vectors are not allocated for this operator");
+  k_cg_init<<<vec_blocks(n), kCgThreads, 0, st>>>(b, x, w.r.as<float2>(), w.u.as<float2>(), n, 0.0, 0.0, iters,
+                                                  w.state.as<CgState>(), w.partial.as<double2>());
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+int cg_fixed_iter_enqueue(mrsr_normalop* op, float2* x, cudaStream_t st) {
+  CgWork& w = op->cg;
+  const int64_t n = op->geo.nimg() * op->geo.K;
   CgState* s = w.state.as<CgState>();
   double2* part = w.partial.as<double2>();
   const unsigned nb = vec_blocks(n);
-  k_cg_init<<<nb, kCgThreads, 0, st>>>(b, x, w.r.as<float2>(), w.u.as<float2>(), n, 0.0, 0.0, iters, s, part);
+  k_cg_dir<<<nb, kCgThreads, 0, st>>>(w.r.as<float2>(), w.u.as<float2>(), n, s);
   MRSR_LAUNCH_CHECK();
-  for (int k = 0; k < iters; ++k) {
-    k_cg_dir<<<nb, kCgThreads, 0, st>>>(w.r.as<float2>(), w.u.as<float2>(), n, s);
-    MRSR_LAUNCH_CHECK();
-    MRSR_TRY(normalop_apply_internal(op, w.u.as<float2>(), w.c.as<float2>(), make_float2(1.f, 0.f),
-                                     make_float2(0.f, 0.f), st));
-    k_cg_alpha<<<nb, kCgThreads, 0, st>>>(w.u.as<float2>(), w.c.as<float2>(), n, s, part);
-    MRSR_LAUNCH_CHECK();
-    k_cg_update<<<nb, kCgThreads, 0, st>>>(x, w.r.as<float2>(), w.u.as<float2>(), w.c.as<float2>(), n, s, part);
-    MRSR_LAUNCH_CHECK();
-  }
+  MRSR_TRY(normalop_apply_internal(op, w.u.as<float2>(), w.c.as<float2>(), make_float2(1.f, 0.f),
+                                   make_float2(0.f, 0.f), st));
+  k_cg_alpha<<<nb, kCgThreads, 0, st>>>(w.u.as<float2>(), w.c.as<float2>(), n, s, part);
+  MRSR_LAUNCH_CHECK();
+  k_cg_update<<<nb, kCgThreads, 0, st>>>(x, w.r.as<float2>(), w.u.as<float2>(), w.c.as<float2>(), n, s, part);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+int cg_fixed_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st) {
+  MRSR_TRY(cg_fixed_init_enqueue(op, b, x, iters, st));
+  for (int k = 0; k < iters; ++k) MRSR_TRY(cg_fixed_iter_enqueue(op, x, st));
   return MRSR_OK;
 }
 

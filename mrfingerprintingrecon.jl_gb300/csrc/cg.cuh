@@ -25,6 +25,10 @@ int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter
 // sized (CgWork::ensure).  cg_fixed_result reads the iteration count and
 // residual norm after the stream has finished.
 int cg_fixed_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st);
+// the same in two parts: x = 0, r = b (with the iteration limit `iters`), and one iteration;
+// iterations after the limit or the tolerance return at once
+int cg_fixed_init_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st);
+int cg_fixed_iter_enqueue(mrsr_normalop* op, float2* x, cudaStream_t st);
 int cg_fixed_result(mrsr_normalop* op, int* iters, double* res);
 
 }  // namespace mrsr
