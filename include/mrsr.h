@@ -22,7 +22,13 @@
  *  - Every function returns MRSR_OK (0) or an error code; the message is
  *    available from mrsr_last_error() (thread-local).  Device kernels never
  *    trap; kernels that can detect bad input write an error word that the
- *    host reads back and turns into MRSR_ERR_ARG.
+ *    host reads back and turns into MRSR_ERR_ARG.  The apply kernels that
+ *    wait on mbarriers bound every wait; one that gives up writes the
+ *    operator's error word and returns.  Applies are asynchronous, so the
+ *    word is read where the library synchronises anyway (the end of
+ *    mrsr_cg, mrsr_cg_noalloc, mrsr_cg_refined and mrsr_cg_batch_result)
+ *    and by mrsr_normalop_check; a set word becomes MRSR_ERR_DEVICE and is
+ *    cleared.
  *  - Handles are not thread-safe; different handles are independent.
  *  - There is no CPU fallback: without a usable sm_103a device every entry
  *    point returns MRSR_ERR_DEVICE or MRSR_ERR_CUDA.
@@ -152,6 +158,16 @@ int mrsr_normalop_get_lambda(const mrsr_normalop* op, void* out, mrsr_stream_t s
  * array of length launches_per_apply); used by the benchmark's roofline. */
 int mrsr_normalop_profile(mrsr_normalop* op, const float* x, float* y, int iters, float* ms_per_pass,
                           mrsr_stream_t stream);
+
+/* Synchronises `stream` and reports whether any apply enqueued on the operator
+ * since the last check hit a bounded device wait that gave up (MRSR_ERR_DEVICE,
+ * whose outputs are not valid); clears the word.  MRSR_OK otherwise.  The
+ * reference has no counterpart: its operators run on the CPU. */
+int mrsr_normalop_check(mrsr_normalop* op, mrsr_stream_t stream);
+
+/* Test hook: writes `code` into the operator's device error word (synchronous),
+ * so the reporting path can be exercised without provoking a device fault. */
+int mrsr_test_set_device_error(mrsr_normalop* op, int code, mrsr_stream_t stream);
 
 void mrsr_normalop_destroy(mrsr_normalop* op);
 

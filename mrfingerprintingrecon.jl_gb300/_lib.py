@@ -33,6 +33,8 @@ SIGNATURES = {
     "mrsr_normalop_get_kmask": [p, p, p],
     "mrsr_normalop_get_lambda": [p, p, p],
     "mrsr_normalop_profile": [p, p, p, i32, C.POINTER(f32), p],
+    "mrsr_normalop_check": [p, p],
+    "mrsr_test_set_device_error": [p, i32, p],
     "mrsr_normalop_destroy": [p],
     "mrsr_backprojection": [i32, i64p, i64, i64, i32, p, p, p, p, i32, i32, p, i32, p, p, p],
     "mrsr_backprojection_cartesian": [i32, i64p, i64, i64, i32, i32, p, p, p, p, i32, i32, p, p, p],

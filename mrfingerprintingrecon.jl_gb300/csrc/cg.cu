@@ -206,11 +206,13 @@ int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter
     }
   }
   CgState h;
+  int dev_err = 0;
   MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(&dev_err, op->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
   if (iters) *iters = h.it;
   if (res) *res = h.res;
-  return MRSR_OK;
+  return device_error_status(op, dev_err, st);
 }
 
 int cg_fixed_init_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st) {
@@ -249,10 +251,12 @@ int cg_fixed_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, c
 int cg_fixed_result(mrsr_normalop* op, int* iters, double* res) {
   MRSR_REQUIRE(op->cg.state.p, MRSR_ERR_STATE, "no CG has run on this operator");
   CgState h;
+  int dev_err = 0;
   MRSR_CHECK_CUDA(cudaMemcpy(&h, op->cg.state.p, sizeof(CgState), cudaMemcpyDeviceToHost));
+  MRSR_CHECK_CUDA(cudaMemcpy(&dev_err, op->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (iters) *iters = h.it;
   if (res) *res = h.res;
-  return MRSR_OK;
+  return device_error_status(op, dev_err, call_stream());
 }
 
 // r = b - A x  (outer residual of the refinement, float32 operator)
@@ -342,8 +346,11 @@ extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const
     MRSR_CHECK_CUDA(cudaMemsetAsync(nrm.p, 0, sizeof(double), st));
     k_norm2<<<nb, kCgThreads, 0, st>>>(r.as<float2>(), n, nrm.as<double>());
     MRSR_LAUNCH_CHECK();
+    int dev_err = 0;
     MRSR_CHECK_CUDA(cudaMemcpyAsync(hn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    MRSR_CHECK_CUDA(cudaMemcpyAsync(&dev_err, op_hi->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+    MRSR_TRY(device_error_status(op_hi, dev_err, st));
     relres = std::sqrt(hn[0]) / bnorm;
     ++outer;
     if (!(relres <= 2.0 * prev)) {
@@ -453,10 +460,12 @@ extern "C" int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int 
       if (h.done) break;
     }
   }
+  int dev_err = 0;
   MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(&dev_err, op->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
   if (iters_out) *iters_out = h.it;
   if (resnorm_out) *resnorm_out = h.res;
-  return MRSR_OK;
+  return device_error_status(op, dev_err, st);
 }
 

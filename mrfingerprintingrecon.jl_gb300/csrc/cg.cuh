@@ -17,6 +17,11 @@ struct CgWork {
 // y <- beta y + alpha A x on the operator's stream-ordered passes (normalop.cu)
 int normalop_apply_internal(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st);
 
+// `code` is the operator's device error word as read back after a synchronisation:
+// nonzero (a bounded wait inside an apply kernel gave up) clears the word on `st`
+// and returns MRSR_ERR_DEVICE with a message; zero returns MRSR_OK.
+int device_error_status(mrsr_normalop* op, int code, cudaStream_t st);
+
 int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter, double reltol, double abstol,
            cudaStream_t st, int* iters, double* res);
 

@@ -552,6 +552,14 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
   return MRSR_OK;
 }
 
+int device_error_status(mrsr_normalop* op, int code, cudaStream_t st) {
+  if (code == 0) return MRSR_OK;
+  cudaMemsetAsync(op->errflag.p, 0, sizeof(int), st);
+  set_error("a bounded device wait timed out during an apply (code %d): results since the last check are not valid",
+            code);
+  return MRSR_ERR_DEVICE;
+}
+
 int normalop_apply_internal(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st) {
   return apply_impl(op, x, y, alpha, beta, st, Recorder{});
 }
@@ -912,6 +920,24 @@ extern "C" int mrsr_normalop_profile(mrsr_normalop* op, const float* x, float* y
     if (s != MRSR_OK) return s;
   }
   for (int i = 0; i < op->launches; ++i) ms_per_pass[i] = (float)(acc[i] / iters);
+  return MRSR_OK;
+}
+
+extern "C" int mrsr_normalop_check(mrsr_normalop* op, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
+  MRSR_REQUIRE(op, MRSR_ERR_ARG, "operator is NULL");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int code = 0;
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(&code, op->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  return device_error_status(op, code, st);
+}
+
+extern "C" int mrsr_test_set_device_error(mrsr_normalop* op, int code, mrsr_stream_t stream) {
+  MRSR_REQUIRE(op, MRSR_ERR_ARG, "operator is NULL");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(op->errflag.p, &code, sizeof(int), cudaMemcpyHostToDevice, st));
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
   return MRSR_OK;
 }
 

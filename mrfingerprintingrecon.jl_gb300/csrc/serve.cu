@@ -319,10 +319,14 @@ extern "C" int mrsr_cg_batch_result(mrsr_cg_batch* bt, int i, int* iters_out, do
     return cg_fixed_result(en.lo, iters_out, resnorm_out);
   }
   double h[2];
+  int dev_err[2] = {0, 0};
   MRSR_CHECK_CUDA(cudaMemcpy(h, bt->nrm.as<double>() + 2 * i, sizeof(h), cudaMemcpyDeviceToHost));
+  MRSR_CHECK_CUDA(cudaMemcpy(&dev_err[0], en.lo->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+  MRSR_CHECK_CUDA(cudaMemcpy(&dev_err[1], en.hi->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
   if (iters_out) *iters_out = bt->outer;
   if (resnorm_out) *resnorm_out = h[0] > 0 ? std::sqrt(h[1] / h[0]) : 0.0;
-  return MRSR_OK;
+  MRSR_TRY(device_error_status(en.lo, dev_err[0], call_stream()));
+  return device_error_status(en.hi, dev_err[1], call_stream());
 }
 
 extern "C" void mrsr_cg_batch_destroy(mrsr_cg_batch* bt) { delete bt; }

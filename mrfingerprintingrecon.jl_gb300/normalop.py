@@ -145,6 +145,12 @@ class NormalOperator:
                                                     stream_handle(stream)))
         return list(ms)
 
+    def check(self, stream=None):
+        """Synchronise and raise ``MrsrError`` if an apply since the last check hit a
+        bounded device wait that gave up (its outputs are not valid); clears the flag.
+        The CG solvers make the same check when they finish."""
+        _lib.check(_lib.load().mrsr_normalop_check(self._h, stream_handle(stream)))
+
 
 def _new_handle(fn, *args):
     h = C.c_void_p()
