@@ -3,9 +3,12 @@
 //   u = r + (|r|^2 / prev^2) u,  c = A u,  alpha = |r|^2 / <u, c>,
 //   x += alpha u,  r -= alpha c,  prev = |r|,  |r| = norm(r)
 // stopping once |r| <= max(reltol |b|, abstol) or after maxiter iterations.
-// Vectors are ComplexF32; inner products, norms, alpha and beta are float64
-// on the device.  Reductions are deterministic (per-block partials summed in
-// a fixed order by the last block).  A device "done" flag makes iterations
+// Vectors are ComplexF32.  Inner products and norms are summed in float32 within
+// a warp (a thread's few elements, then the 32 lanes, in a fixed order) and in
+// float64 across warps and blocks; alpha and beta are formed once, in float64, by
+// the block that finishes a reduction.  GB300's float64 rate is a small fraction
+// of its float32 rate, so no per-element work runs in float64.  Reductions are
+// deterministic (per-block partials summed in a fixed order by the last block).  A device "done" flag makes iterations
 // after convergence no-ops, so the host launches without synchronising.
 #include <algorithm>
 #include <cmath>
@@ -28,7 +31,27 @@ struct CgState {
   int maxiter;
   int done;
   unsigned int ticket;
+  float beta;         // res^2 / prev^2 for the next direction update (0 before the first)
 };
+
+// Block sum of each thread's float32 pair: warp shuffles in float32, then the warp
+// sums in float64 in warp order.  The result is valid in thread 0.
+__device__ __forceinline__ double2 block_sum_f2(float2 v) {
+  __shared__ float2 wsum[kCgThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+  }
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double2 s = make_double2(0.0, 0.0);
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kCgThreads / 32; ++w) {
+      s.x += (double)wsum[w].x;
+      s.y += (double)wsum[w].y;
+    }
+  return s;
+}
 
 __device__ __forceinline__ double2 block_sum2(double2 v) {
   __shared__ double2 red[kCgThreads / 32];
@@ -79,20 +102,21 @@ __device__ __forceinline__ bool last_block(CgState* st, double2* partial, double
 // x = 0, r = b, u = 0, res = |b|
 __global__ void k_cg_init(const float2* b, float2* x, float2* r, float2* u, int64_t n, double reltol, double abstol,
                           int maxiter, CgState* st, double2* partial) {
-  double acc = 0.0;
+  float acc = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 v = b[i];
     x[i] = make_float2(0.f, 0.f);
     r[i] = v;
     u[i] = make_float2(0.f, 0.f);
-    acc += (double)v.x * v.x + (double)v.y * v.y;
+    acc = fmaf(v.x, v.x, fmaf(v.y, v.y, acc));
   }
-  double2 s = block_sum2(make_double2(acc, 0.0));
+  double2 s = block_sum_f2(make_float2(acc, 0.f));
   double2 tot;
   if (last_block(st, partial, s, &tot)) {
     const double res = sqrt(tot.x);
     st->res = res;
     st->prev = 1.0;
+    st->beta = 0.f;
     st->tol = fmax(reltol * res, abstol);
     st->it = 0;
     st->maxiter = maxiter;
@@ -100,11 +124,10 @@ __global__ void k_cg_init(const float2* b, float2* x, float2* r, float2* u, int6
   }
 }
 
-// u = r + beta u with beta = res^2 / prev^2
+// u = r + beta u with beta = res^2 / prev^2 (formed by the previous update, 0 at first)
 __global__ void k_cg_dir(const float2* r, float2* u, int64_t n, const CgState* st) {
   if (st->done) return;
-  const double beta = (st->res * st->res) / (st->prev * st->prev);
-  const float b = (float)beta;
+  const float b = st->beta;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 rv = r[i], uv = u[i];
     u[i] = make_float2(rv.x + b * uv.x, rv.y + b * uv.y);
@@ -114,13 +137,13 @@ __global__ void k_cg_dir(const float2* r, float2* u, int64_t n, const CgState* s
 // alpha = res^2 / <u, c>  (<u, c> = sum conj(u) c)
 __global__ void k_cg_alpha(const float2* u, const float2* c, int64_t n, CgState* st, double2* partial) {
   if (st->done) return;
-  double re = 0.0, im = 0.0;
+  float re = 0.f, im = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 a = u[i], b = c[i];
-    re += (double)a.x * b.x + (double)a.y * b.y;
-    im += (double)a.x * b.y - (double)a.y * b.x;
+    re = fmaf(a.x, b.x, fmaf(a.y, b.y, re));
+    im = fmaf(a.x, b.y, fmaf(-a.y, b.x, im));
   }
-  double2 s = block_sum2(make_double2(re, im));
+  double2 s = block_sum_f2(make_float2(re, im));
   double2 tot;
   if (last_block(st, partial, s, &tot)) {
     const double r2 = st->res * st->res;
@@ -136,7 +159,7 @@ __global__ void k_cg_update(float2* x, float2* r, const float2* u, const float2*
                             double2* partial) {
   if (st->done) return;
   const float ar = (float)st->ar, ai = (float)st->ai;
-  double acc = 0.0;
+  float acc = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 uv = u[i], cv = c[i];
     float2 xv = x[i], rv = r[i];
@@ -146,20 +169,22 @@ __global__ void k_cg_update(float2* x, float2* r, const float2* u, const float2*
     rv.y -= ar * cv.y + ai * cv.x;
     x[i] = xv;
     r[i] = rv;
-    acc += (double)rv.x * rv.x + (double)rv.y * rv.y;
+    acc = fmaf(rv.x, rv.x, fmaf(rv.y, rv.y, acc));
   }
-  double2 s = block_sum2(make_double2(acc, 0.0));
+  double2 s = block_sum_f2(make_float2(acc, 0.f));
   double2 tot;
   if (last_block(st, partial, s, &tot)) {
     st->prev = st->res;
     st->res = sqrt(tot.x);
+    st->beta = st->prev > 0.0 ? (float)(tot.x / (st->prev * st->prev)) : 0.f;
     st->it += 1;
     st->done = (st->res <= st->tol || st->it >= st->maxiter) ? 1 : 0;
   }
 }
 
+// about four elements per thread: the per-block partials and the final sum stay short
 static unsigned vec_blocks(int64_t n) {
-  return (unsigned)std::min<int64_t>(kCgBlocks, std::max<int64_t>(1, cdiv(n, kCgThreads)));
+  return (unsigned)std::min<int64_t>(kCgBlocks, std::max<int64_t>(1, cdiv(n, 4 * kCgThreads)));
 }
 
 int CgWork::ensure(int64_t n_) {
@@ -281,12 +306,20 @@ __global__ void k_sub(float2* y, const float2* x, int64_t n) {
     y[i] = b;
   }
 }
-__global__ void k_norm2(const float2* a, int64_t n, double* out) {
-  double acc = 0.0;
+// |a|^2: per-block partials, then k_sum_parts adds them in block order (deterministic)
+__global__ void k_norm2(const float2* a, int64_t n, double* part) {
+  float acc = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    acc += (double)a[i].x * a[i].x + (double)a[i].y * a[i].y;
-  double2 s = block_sum2(make_double2(acc, 0.0));
-  if (threadIdx.x == 0) atomicAdd(out, s.x);
+    acc = fmaf(a[i].x, a[i].x, fmaf(a[i].y, a[i].y, acc));
+  double2 s = block_sum_f2(make_float2(acc, 0.f));
+  if (threadIdx.x == 0) part[blockIdx.x] = s.x;
+}
+__global__ void k_sum_parts(const double* part, int nparts, double* out) {
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nparts; ++b) s += part[b];
+    out[0] = s;
+  }
 }
 
 }  // namespace mrsr
@@ -315,14 +348,16 @@ extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const
   const int64_t n = op_hi->geo.nimg() * op_hi->geo.K;
   const float2* bb = reinterpret_cast<const float2*>(b);
   float2* xx = reinterpret_cast<float2*>(x);
-  DevBuf r, d, nrm;
+  DevBuf r, d, nrm, part;
   MRSR_TRY(r.alloc(sizeof(float2) * n));
   MRSR_TRY(d.alloc(sizeof(float2) * n));
   MRSR_TRY(nrm.alloc(sizeof(double) * 2));
   const unsigned nb = vec_blocks(n);
+  MRSR_TRY(part.alloc(sizeof(double) * nb));
   MRSR_CHECK_CUDA(cudaMemsetAsync(xx, 0, sizeof(float2) * n, st));
-  MRSR_CHECK_CUDA(cudaMemsetAsync(nrm.p, 0, sizeof(double) * 2, st));
-  k_norm2<<<nb, kCgThreads, 0, st>>>(bb, n, nrm.as<double>());
+  k_norm2<<<nb, kCgThreads, 0, st>>>(bb, n, part.as<double>());
+  MRSR_LAUNCH_CHECK();
+  k_sum_parts<<<1, 32, 0, st>>>(part.as<double>(), (int)nb, nrm.as<double>());
   MRSR_LAUNCH_CHECK();
   double hn[2];
   MRSR_CHECK_CUDA(cudaMemcpyAsync(hn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -343,8 +378,9 @@ extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const
     k_copy<<<nb, kCgThreads, 0, st>>>(bb, r.as<float2>(), n);
     MRSR_LAUNCH_CHECK();
     MRSR_TRY(normalop_apply_internal(op_hi, xx, r.as<float2>(), make_float2(-1.f, 0.f), make_float2(1.f, 0.f), st));
-    MRSR_CHECK_CUDA(cudaMemsetAsync(nrm.p, 0, sizeof(double), st));
-    k_norm2<<<nb, kCgThreads, 0, st>>>(r.as<float2>(), n, nrm.as<double>());
+    k_norm2<<<nb, kCgThreads, 0, st>>>(r.as<float2>(), n, part.as<double>());
+    MRSR_LAUNCH_CHECK();
+    k_sum_parts<<<1, 32, 0, st>>>(part.as<double>(), (int)nb, nrm.as<double>());
     MRSR_LAUNCH_CHECK();
     int dev_err = 0;
     MRSR_CHECK_CUDA(cudaMemcpyAsync(hn, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, st));

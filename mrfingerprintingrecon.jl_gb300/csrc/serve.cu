@@ -37,19 +37,41 @@ __global__ void k_sv_add(float2* y, const float2* x, int64_t n) {
     y[i] = make_float2(b.x + a.x, b.y + a.y);
   }
 }
-// out[0] = |a|^2 as a deterministic single-block float64 sum
-__global__ void k_sv_norm2(const float2* a, int64_t n, double* out) {
-  __shared__ double red[kVecThreads / 32];
-  double acc = 0.0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) acc += (double)a[i].x * a[i].x + (double)a[i].y * a[i].y;
+// |a|^2, deterministic, in two launches: per-block partials (float32 within a warp,
+// float64 across warps), then one block sums them in a fixed order.  No per-element
+// work runs in float64 (a small fraction of the float32 rate on GB300).
+constexpr int kNormBlocks = 256;
+static unsigned norm_grid(int64_t n) {
+  return (unsigned)std::min<int64_t>(kNormBlocks, std::max<int64_t>(1, cdiv(n, 4 * kVecThreads)));
+}
+__global__ void k_sv_norm2_part(const float2* a, int64_t n, double* part) {
+  __shared__ float wsum[kVecThreads / 32];
+  float acc = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc = fmaf(a[i].x, a[i].x, fmaf(a[i].y, a[i].y, acc));
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int w = 0; w < kVecThreads / 32; ++w) s += red[w];
+    for (int w = 0; w < kVecThreads / 32; ++w) s += (double)wsum[w];
+    part[blockIdx.x] = s;
+  }
+}
+__global__ void k_sv_norm2_fin(const double* part, int nparts, double* out) {
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nparts; ++b) s += part[b];
     out[0] = s;
   }
+}
+static int sv_norm2(const float2* a, int64_t n, double* part, double* out, cudaStream_t st) {
+  const unsigned g = norm_grid(n);
+  k_sv_norm2_part<<<g, kVecThreads, 0, st>>>(a, n, part);
+  MRSR_LAUNCH_CHECK();
+  k_sv_norm2_fin<<<1, 32, 0, st>>>(part, (int)g, out);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
 }
 
 }  // namespace mrsr
@@ -93,6 +115,7 @@ struct mrsr_cg_batch {
     const float2* b = nullptr;
     float2* x = nullptr;
     DevBuf r, d;   // refinement: outer residual and correction
+    DevBuf part;   // refinement: per-block partial sums of a norm
   };
   std::unique_ptr<Entry[]> e;
   int ne = 0;
@@ -131,8 +154,7 @@ static int batch_branch(mrsr_cg_batch* bt, int i, cudaStream_t st) {
   if (!en.hi) return cg_fixed_enqueue(en.lo, en.b, en.x, bt->inner, st);
   // refinement with a fixed schedule: x = 0, r = b; repeat: d = CG_lo(r), x += d, r = b - A_hi x
   double* nrm = bt->nrm.as<double>() + 2 * i;
-  k_sv_norm2<<<1, kVecThreads, 0, st>>>(en.b, n, nrm);
-  MRSR_LAUNCH_CHECK();
+  MRSR_TRY(sv_norm2(en.b, n, en.part.as<double>(), nrm, st));
   k_sv_zero<<<nb, kVecThreads, 0, st>>>(en.x, n);
   MRSR_LAUNCH_CHECK();
   k_sv_copy<<<nb, kVecThreads, 0, st>>>(en.b, en.r.as<float2>(), n);
@@ -145,8 +167,7 @@ static int batch_branch(mrsr_cg_batch* bt, int i, cudaStream_t st) {
     MRSR_LAUNCH_CHECK();
     MRSR_TRY(normalop_apply_internal(en.hi, en.x, en.r.as<float2>(), make_float2(-1.f, 0.f), make_float2(1.f, 0.f), st));
   }
-  k_sv_norm2<<<1, kVecThreads, 0, st>>>(en.r.as<float2>(), n, nrm + 1);
-  MRSR_LAUNCH_CHECK();
+  MRSR_TRY(sv_norm2(en.r.as<float2>(), n, en.part.as<double>(), nrm + 1, st));
   return MRSR_OK;
 }
 
@@ -267,6 +288,7 @@ extern "C" int mrsr_cg_batch_create(mrsr_normalop* const* ops_lo, mrsr_normalop*
     s = en.lo->cg.ensure(nv);
     if (s == MRSR_OK && en.hi) s = en.r.alloc(sizeof(float2) * nv);
     if (s == MRSR_OK && en.hi) s = en.d.alloc(sizeof(float2) * nv);
+    if (s == MRSR_OK && en.hi) s = en.part.alloc(sizeof(double) * kNormBlocks);
   }
   if (s == MRSR_OK) s = bt->nrm.alloc(sizeof(double) * 2 * n);
   if (s == MRSR_OK) {

@@ -48,6 +48,8 @@ def _problem(seed, img, K, Nc, density=0.8, complex_lam=True):
     ((192, 96), 3, 2, True),     # 384 = 12 x 32 and 192 (generic)
     ((32, 32, 32), 5, 2, False), # 3D four-step: 64 = 8 x 8
     ((32, 64, 32), 3, 2, True),  # 3D mixed: 64 / 128
+    ((256, 256), 5, 3, False),   # K = 5 on 512-point columns (the benchmark's Λ pass)
+    ((128, 256), 5, 2, True),    # the same with a complex kernel
 ])
 def test_nfft_apply_matches_oracle(mr, cuda, img, K, Nc, cplx):
     lam, cells, cm, x = _problem(1, img, K, Nc, complex_lam=cplx)
