@@ -223,8 +223,9 @@ int mrsr_grog_gridding(int ndims, const int64_t* img_shape, int64_t nr, int64_t 
 /* ---------------------------------------------------------------------
  * cg(A, b; maxiter, reltol, abstol) with x0 = 0 as IterativeSolvers.jl 0.9
  * runs it on the LinearOperator (call sites test/*.jl, src/CoilMaps.jl:136).
- * Inner products, norms and alpha/beta in float64 on the device; vectors
- * ComplexF32.  Stops after maxiter iterations or once
+ * Vectors ComplexF32; each thread sums its few elements' products in float32,
+ * the rest of every inner product and norm, and alpha/beta, in float64 on the
+ * device (deterministic).  Stops after maxiter iterations or once
  * ||r|| <= max(reltol*||b||, abstol).  iters_out / resnorm_out are host
  * pointers (may be NULL); the call synchronises the stream to return them.
  */
@@ -243,6 +244,21 @@ int mrsr_cg(mrsr_normalop* op, const float* b, float* x, int maxiter, double rel
  * overlap on the GPU (other streams, other host threads) race and must be
  * serialised by the caller.  The operator itself must already exist. */
 int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
+                    int* iters_out, double* resnorm_out, mrsr_stream_t stream);
+
+/* Stacked right-hand sides (reconstruct_coilwise, src/CoilMaps.jl:118-162:
+ * `for i in 1:Nc; x[.., i] = cg(AᴴA, b[.., i]; maxiter)`, and its GPU form
+ * ext/MRISubspaceReconCUDAExt/CoilMaps.jl:57-77).
+ * mrsr_normalop_stack: from a float32 rank-1 operator src (K = 1), an operator
+ * on nrhs (1..64) stacked images x (img..., nrhs) that applies src to every
+ * plane independently (same kernel, kmask and coil maps; planes are not mixed).
+ * mrsr_cg_stacked runs one independent cg per plane of such an operator in
+ * one set of launches: each plane has its own alpha, beta, tolerance test and
+ * iteration count, exactly as nrhs separate mrsr_cg calls would (the planes'
+ * reductions are the same arithmetic, so results agree to float32 rounding).
+ * iters_out / resnorm_out receive nrhs entries (host, may be NULL). */
+int mrsr_normalop_stack(const mrsr_normalop* src, int nrhs, mrsr_stream_t stream, mrsr_normalop** out);
+int mrsr_cg_stacked(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
                     int* iters_out, double* resnorm_out, mrsr_stream_t stream);
 
 /* Mixed-precision iterative refinement (no counterpart in the reference):

@@ -3,12 +3,11 @@
 
 ``reconstruct_coilwise`` (src/CoilMaps.jl:118-162, ext/.../CoilMaps.jl:57-77) builds
 one K=1 operator without coil maps and solves Nc independent systems on it, one per
-receive channel.  Non-Cartesian: the Nc fixed-iteration solves
-(``cg!(x_c, AᴴA, b_c; maxiter=Niter_cg, reltol=0)``) run as the branches of one
-CUDA graph, each branch on an operator that shares the Toeplitz kernel and kmask
-of the first (``share``) and owns its workspace.  Cartesian: IterativeSolvers'
-default tolerance applies (src/CoilMaps.jl:159), so each coil runs the
-tolerance-checked ``cg``.
+receive channel: non-Cartesian with a fixed iteration count
+(``cg!(x_c, AᴴA, b_c; maxiter=Niter_cg, reltol=0)``), Cartesian with IterativeSolvers'
+default tolerance (src/CoilMaps.jl:159).  Here the Nc systems run together on the
+operator stacked over the coils (``NormalOperator.stack``, ``cg_stacked``): every pass
+and CG step is one launch for all coils, while each coil keeps its own CG iteration.
 
 ``calculate_calibration_kspace`` is ``calculate_coil_maps`` up to the ESPIRiT call:
 the calibration mask and the rescaled trajectory, the coil-wise reconstruction and
@@ -23,7 +22,7 @@ import torch
 from .arrays import jl_reshape, jl_zeros, to_host, to_jl
 from .backprojection import _is_int_traj, calculate_backprojection
 from .normalop import FFTNormalOp, NFFTNormalOp
-from .solvers import CgBatch, cg
+from .solvers import DEFAULT_RELTOL, CgBatch, cg, cg_stacked
 
 
 def _first_basis_column(U, nt):
@@ -57,10 +56,24 @@ def reconstruct_coilwise(data, trj, img_shape, U=None, sample_mask=None, Niter_c
 
 def _coilwise_solve(A, b, iters, tolerance_checked=False, stream=None):
     """x[..., c] = cg(A, b[..., 1, c]) for every coil c of the (img..., 1, Nc) backprojection.
-    Fixed iterations: one graph, one branch per coil, each on an operator sharing A's
-    kernel.  ``tolerance_checked``: IterativeSolvers' default reltol, coil by coil."""
+
+    The Nc solves run together on A stacked over the coils (``A.stack(Nc)``, one launch
+    per pass and CG step for all coils), each with its own CG iteration: fixed
+    iterations (reltol = 0), or with ``tolerance_checked`` IterativeSolvers' default
+    reltol, coil by coil.  Where the stacked planes do not fit one block's shared memory
+    (very long lines), the fixed solves run as the branches of one CUDA graph on operators
+    sharing A's kernel and the tolerance-checked ones one after another."""
     img_shape = tuple(int(s) for s in b.shape[:-2])
     nc = int(b.shape[-1])
+    try:
+        S = A.stack(nc, stream=stream)
+    except NotImplementedError:
+        S = None
+    if S is not None:
+        reltol = DEFAULT_RELTOL if tolerance_checked else 0.0
+        x = cg_stacked(S, b[..., 0, :], maxiter=int(iters), reltol=reltol, stream=stream)
+        S.close()
+        return x
     x = jl_zeros(img_shape + (nc,), torch.complex64)
     if tolerance_checked:
         for c in range(nc):

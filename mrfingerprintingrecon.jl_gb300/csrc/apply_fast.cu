@@ -94,6 +94,25 @@ __global__ void __launch_bounds__(512) k4_rows_inv(RowsInvArgs a, Slots sl) {
   }
 }
 
+// stacked right-hand sides: every plane times the same scalar kernel entry, at every
+// frequency f of the tile (any number of planes)
+template <class SP>
+__device__ __forceinline__ void lam_voxels_diag(const LamPassArgs& a, float2* sm, const Slots& sl, int64_t tile) {
+  constexpr int R1 = SP::R1, L = SP::L;
+  const int T = L << sl.tcs;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    const int li = t & (a.TC - 1);
+    const int f = t >> sl.tcs;
+    const int f1 = f % R1, f2 = f / R1;
+    const int ch = (int)a.fcd.div((uint32_t)f), fc = f - ch * a.FC;
+    const float2 l = lam_diag_entry(a.lam_mode, a.lam, ((tile * a.NCH + ch) * (int64_t)a.FC + fc) * a.TC + li);
+    for (int k = 0; k < a.K; ++k) {
+      float2* v = &sm[sl.at(k, f1, f2, li, R1)];
+      *v = cmul(l, *v);
+    }
+  }
+}
+
 // per-voxel K x K product at every frequency f of the tile, rank KK known at compile time
 template <class SP, int KK>
 __device__ __forceinline__ void lam_voxels(const LamPassArgs& a, float2* sm, const Slots& sl, int64_t tile) {
@@ -176,7 +195,9 @@ __global__ void __launch_bounds__(256, 2) k4_lambda(LamPassArgs a, Slots sl) {
   __syncthreads();
   step_b<SP, -1>(sm, sl, a.K, R2, [&](int lo, int li, int f1, int f2, float2 v) { sm[sl.at(lo, f1, f2, li, R1)] = v; });
   __syncthreads();
-  switch (a.K) {
+  if (lam_is_diag(a.lam_mode)) {
+    lam_voxels_diag<SP>(a, sm, sl, tile);
+  } else switch (a.K) {
     case 1: lam_voxels<SP, 1>(a, sm, sl, tile); break;
     case 2: lam_voxels<SP, 2>(a, sm, sl, tile); break;
     case 3: lam_voxels<SP, 3>(a, sm, sl, tile); break;
@@ -475,6 +496,7 @@ int fast_lambda(const LamPassArgs& a, int ncg, int planes_total, int* errword, c
     off += (uint32_t)(a.K * SP::R1 * sl.W * 8);
     const bool box_aligned = ((int64_t)a.K * cf.box_rows * a.TC * 8) % 128 == 0 || cf.nboxes == 1;
     const bool tma_ok = a.TC >= 2 && off <= 227u * 1024u && cf.chunk_bytes % 16 == 0 && box_aligned &&
+                        !lam_is_diag(a.lam_mode) &&
                         std::getenv("MRSR_TMA_LAMBDA") != nullptr;
     if (tma_ok) {
       CUtensorMap tm;

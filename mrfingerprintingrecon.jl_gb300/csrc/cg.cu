@@ -3,16 +3,17 @@
 //   u = r + (|r|^2 / prev^2) u,  c = A u,  alpha = |r|^2 / <u, c>,
 //   x += alpha u,  r -= alpha c,  prev = |r|,  |r| = norm(r)
 // stopping once |r| <= max(reltol |b|, abstol) or after maxiter iterations.
-// Vectors are ComplexF32.  Inner products and norms are summed in float32 within
-// a warp (a thread's few elements, then the 32 lanes, in a fixed order) and in
-// float64 across warps and blocks; alpha and beta are formed once, in float64, by
-// the block that finishes a reduction.  GB300's float64 rate is a small fraction
-// of its float32 rate, so no per-element work runs in float64.  Reductions are
-// deterministic (per-block partials summed in a fixed order by the last block).  A device "done" flag makes iterations
+// Vectors are ComplexF32.  Each thread sums the products of its few elements
+// (about four) with float32 FMAs; everything above that (warp, block, grid) is
+// float64, and alpha and beta are formed once, in float64, by the block that
+// finishes a reduction.  GB300's float64 rate is a small fraction of its float32
+// rate, so no per-element work runs in float64.  Reductions are deterministic
+// (per-block partials summed in a fixed order by the last block).  A device "done" flag makes iterations
 // after convergence no-ops, so the host launches without synchronising.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <vector>
 
 #include "cg.cuh"
 #include "normalop.cuh"
@@ -34,25 +35,6 @@ struct CgState {
   float beta;         // res^2 / prev^2 for the next direction update (0 before the first)
 };
 
-// Block sum of each thread's float32 pair: warp shuffles in float32, then the warp
-// sums in float64 in warp order.  The result is valid in thread 0.
-__device__ __forceinline__ double2 block_sum_f2(float2 v) {
-  __shared__ float2 wsum[kCgThreads / 32];
-  for (int o = 16; o > 0; o >>= 1) {
-    v.x += __shfl_down_sync(0xffffffffu, v.x, o);
-    v.y += __shfl_down_sync(0xffffffffu, v.y, o);
-  }
-  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double2 s = make_double2(0.0, 0.0);
-  if (threadIdx.x == 0)
-    for (int w = 0; w < kCgThreads / 32; ++w) {
-      s.x += (double)wsum[w].x;
-      s.y += (double)wsum[w].y;
-    }
-  return s;
-}
-
 __device__ __forceinline__ double2 block_sum2(double2 v) {
   __shared__ double2 red[kCgThreads / 32];
   for (int o = 16; o > 0; o >>= 1) {
@@ -69,6 +51,11 @@ __device__ __forceinline__ double2 block_sum2(double2 v) {
     }
   return s;
 }
+
+// Block sum of each thread's float32 partials (the products of its few elements): the
+// partials are widened to float64 and combined in float64 in a fixed order.  The result
+// is valid in thread 0.
+__device__ __forceinline__ double2 block_sum_f2(float2 v) { return block_sum2(make_double2(v.x, v.y)); }
 
 // The last block to finish sums the per-block partials; returns true in that block's
 // thread 0.  All its threads take part: thread t adds partials t, t + blockDim, ... in
@@ -100,8 +87,16 @@ __device__ __forceinline__ bool last_block(CgState* st, double2* partial, double
 }
 
 // x = 0, r = b, u = 0, res = |b|
+// Every vector kernel works on plane blockIdx.y of gridDim.y independent systems of n
+// unknowns each (one system for a plain solve), each with its own state and partials.
 __global__ void k_cg_init(const float2* b, float2* x, float2* r, float2* u, int64_t n, double reltol, double abstol,
                           int maxiter, CgState* st, double2* partial) {
+  {
+    const int64_t o = (int64_t)blockIdx.y * n;
+    b += o; x += o; r += o; u += o;
+    st += blockIdx.y;
+    partial += (int64_t)blockIdx.y * gridDim.x;
+  }
   float acc = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float2 v = b[i];
@@ -126,6 +121,9 @@ __global__ void k_cg_init(const float2* b, float2* x, float2* r, float2* u, int6
 
 // u = r + beta u with beta = res^2 / prev^2 (formed by the previous update, 0 at first)
 __global__ void k_cg_dir(const float2* r, float2* u, int64_t n, const CgState* st) {
+  r += (int64_t)blockIdx.y * n;
+  u += (int64_t)blockIdx.y * n;
+  st += blockIdx.y;
   if (st->done) return;
   const float b = st->beta;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -136,6 +134,10 @@ __global__ void k_cg_dir(const float2* r, float2* u, int64_t n, const CgState* s
 
 // alpha = res^2 / <u, c>  (<u, c> = sum conj(u) c)
 __global__ void k_cg_alpha(const float2* u, const float2* c, int64_t n, CgState* st, double2* partial) {
+  u += (int64_t)blockIdx.y * n;
+  c += (int64_t)blockIdx.y * n;
+  st += blockIdx.y;
+  partial += (int64_t)blockIdx.y * gridDim.x;
   if (st->done) return;
   float re = 0.f, im = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -157,6 +159,12 @@ __global__ void k_cg_alpha(const float2* u, const float2* c, int64_t n, CgState*
 // x += alpha u, r -= alpha c, then res = |r|, it += 1, done flag
 __global__ void k_cg_update(float2* x, float2* r, const float2* u, const float2* c, int64_t n, CgState* st,
                             double2* partial) {
+  {
+    const int64_t o = (int64_t)blockIdx.y * n;
+    x += o; r += o; u += o; c += o;
+    st += blockIdx.y;
+    partial += (int64_t)blockIdx.y * gridDim.x;
+  }
   if (st->done) return;
   const float ar = (float)st->ar, ai = (float)st->ai;
   float acc = 0.f;
@@ -187,63 +195,71 @@ static unsigned vec_blocks(int64_t n) {
   return (unsigned)std::min<int64_t>(kCgBlocks, std::max<int64_t>(1, cdiv(n, 4 * kCgThreads)));
 }
 
-int CgWork::ensure(int64_t n_) {
-  if (n == n_ && r.p) return MRSR_OK;
+int CgWork::ensure(int64_t n_, int nseg_) {
+  if (n == n_ && nseg == nseg_ && r.p) return MRSR_OK;
   n = n_;
+  nseg = nseg_;
   MRSR_TRY(r.alloc(sizeof(float2) * n));
   MRSR_TRY(u.alloc(sizeof(float2) * n));
   MRSR_TRY(c.alloc(sizeof(float2) * n));
-  MRSR_TRY(state.alloc(sizeof(CgState)));
-  MRSR_TRY(partial.alloc(sizeof(double2) * kCgBlocks));
-  MRSR_CHECK_CUDA(cudaMemsetAsync(state.p, 0, sizeof(CgState), call_stream()));
+  MRSR_TRY(state.alloc(sizeof(CgState) * nseg));
+  MRSR_TRY(partial.alloc(sizeof(double2) * kCgBlocks * nseg));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(state.p, 0, sizeof(CgState) * nseg, call_stream()));
   return MRSR_OK;
 }
 
 int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter, double reltol, double abstol,
-           cudaStream_t st, int* iters, double* res) {
+           cudaStream_t st, int* iters, double* res, int nseg) {
   const int64_t n = op->geo.nimg() * op->geo.K;
-  MRSR_TRY(w.ensure(n));
+  const int64_t m = n / nseg;  // unknowns per system
+  MRSR_TRY(w.ensure(n, nseg));
   CgState* s = w.state.as<CgState>();
   double2* part = w.partial.as<double2>();
-  const unsigned nb = vec_blocks(n);
-  k_cg_init<<<nb, kCgThreads, 0, st>>>(b, x, w.r.as<float2>(), w.u.as<float2>(), n, reltol, abstol, maxiter, s, part);
+  const dim3 nb(vec_blocks(m), (unsigned)nseg);
+  k_cg_init<<<nb, kCgThreads, 0, st>>>(b, x, w.r.as<float2>(), w.u.as<float2>(), m, reltol, abstol, maxiter, s, part);
   MRSR_LAUNCH_CHECK();
-  // launch iterations in chunks; between chunks read the done flag so a
-  // converged solve does not keep paying for applies
+  // launch iterations in chunks; between chunks read the done flags so converged solves
+  // do not keep paying for applies
+  std::vector<CgState> h((size_t)nseg);
+  auto all_done = [&]() {
+    for (const CgState& v : h)
+      if (!v.done) return false;
+    return true;
+  };
   const int chunk = 8;
   for (int it0 = 0; it0 < maxiter; it0 += chunk) {
     const int nit = std::min(chunk, maxiter - it0);
     for (int k = 0; k < nit; ++k) {
-      k_cg_dir<<<nb, kCgThreads, 0, st>>>(w.r.as<float2>(), w.u.as<float2>(), n, s);
+      k_cg_dir<<<nb, kCgThreads, 0, st>>>(w.r.as<float2>(), w.u.as<float2>(), m, s);
       MRSR_LAUNCH_CHECK();
       MRSR_TRY(normalop_apply_internal(op, w.u.as<float2>(), w.c.as<float2>(), make_float2(1.f, 0.f),
                                        make_float2(0.f, 0.f), st));
-      k_cg_alpha<<<nb, kCgThreads, 0, st>>>(w.u.as<float2>(), w.c.as<float2>(), n, s, part);
+      k_cg_alpha<<<nb, kCgThreads, 0, st>>>(w.u.as<float2>(), w.c.as<float2>(), m, s, part);
       MRSR_LAUNCH_CHECK();
-      k_cg_update<<<nb, kCgThreads, 0, st>>>(x, w.r.as<float2>(), w.u.as<float2>(), w.c.as<float2>(), n, s, part);
+      k_cg_update<<<nb, kCgThreads, 0, st>>>(x, w.r.as<float2>(), w.u.as<float2>(), w.c.as<float2>(), m, s, part);
       MRSR_LAUNCH_CHECK();
     }
     if (it0 + nit < maxiter) {
-      CgState h;
-      MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+      MRSR_CHECK_CUDA(cudaMemcpyAsync(h.data(), s, sizeof(CgState) * nseg, cudaMemcpyDeviceToHost, st));
       MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
-      if (h.done) break;
+      if (all_done()) break;
     }
   }
-  CgState h;
   int dev_err = 0;
-  MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(h.data(), s, sizeof(CgState) * nseg, cudaMemcpyDeviceToHost, st));
   MRSR_CHECK_CUDA(cudaMemcpyAsync(&dev_err, op->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
-  if (iters) *iters = h.it;
-  if (res) *res = h.res;
+  for (int i = 0; i < nseg; ++i) {
+    if (iters) iters[i] = h[i].it;
+    if (res) res[i] = h[i].res;
+  }
   return device_error_status(op, dev_err, st);
 }
 
 int cg_fixed_init_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st) {
   CgWork& w = op->cg;
   const int64_t n = op->geo.nimg() * op->geo.K;
-  MRSR_REQUIRE(w.n == n && w.r.p, MRSR_ERR_STATE, "CG work vectors are not allocated for this operator");
+  MRSR_REQUIRE(w.n == n && w.nseg == 1 && w.r.p, MRSR_ERR_STATE, "CG work vectors are not allocated for this operator");
   k_cg_init<<<vec_blocks(n), kCgThreads, 0, st>>>(b, x, w.r.as<float2>(), w.u.as<float2>(), n, 0.0, 0.0, iters,
                                                   w.state.as<CgState>(), w.partial.as<double2>());
   MRSR_LAUNCH_CHECK();
@@ -335,6 +351,20 @@ extern "C" int mrsr_cg(mrsr_normalop* op, const float* b, float* x, int maxiter,
   OpUse use{op, reinterpret_cast<cudaStream_t>(stream)};
   return cg_run(op, op->cg, reinterpret_cast<const float2*>(b), reinterpret_cast<float2*>(x), maxiter, reltol, abstol,
                 reinterpret_cast<cudaStream_t>(stream), iters_out, resnorm_out);
+}
+
+extern "C" int mrsr_cg_stacked(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
+                               int* iters_out, double* resnorm_out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
+  MRSR_REQUIRE(op && b && x, MRSR_ERR_ARG, "NULL argument to mrsr_cg_stacked");
+  MRSR_REQUIRE((const void*)b != (const void*)x, MRSR_ERR_ARG, "b and x must not alias");
+  MRSR_REQUIRE(maxiter >= 0, MRSR_ERR_ARG, "maxiter must be >= 0");
+  MRSR_REQUIRE(lam_is_diag(op->lam_mode), MRSR_ERR_ARG,
+               "mrsr_cg_stacked needs a stacked operator (mrsr_normalop_stack): the planes of any other "
+               "operator are coupled by its kernel");
+  OpUse use{op, reinterpret_cast<cudaStream_t>(stream)};
+  return cg_run(op, op->cg, reinterpret_cast<const float2*>(b), reinterpret_cast<float2*>(x), maxiter, reltol, abstol,
+                reinterpret_cast<cudaStream_t>(stream), iters_out, resnorm_out, op->geo.K);
 }
 
 extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const float* b, float* x, int inner_iters,

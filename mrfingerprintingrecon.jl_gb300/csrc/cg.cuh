@@ -8,10 +8,11 @@ namespace mrsr {
 
 struct CgWork {
   int64_t n = 0;
+  int nseg = 0;     // independent systems (planes of n / nseg unknowns each)
   DevBuf r, u, c;   // residual, direction, A*direction
-  DevBuf state;     // device CgState (float64 scalars, iteration count, done flag)
-  DevBuf partial;   // per-block float64 partial sums
-  int ensure(int64_t n);
+  DevBuf state;     // device CgState per system (float64 scalars, iteration count, done flag)
+  DevBuf partial;   // per-block float64 partial sums, per system
+  int ensure(int64_t n, int nseg = 1);
 };
 
 // y <- beta y + alpha A x on the operator's stream-ordered passes (normalop.cu)
@@ -22,8 +23,10 @@ int normalop_apply_internal(mrsr_normalop* op, const float2* x, float2* y, float
 // and returns MRSR_ERR_DEVICE with a message; zero returns MRSR_OK.
 int device_error_status(mrsr_normalop* op, int code, cudaStream_t st);
 
+// nseg independent CG solves on the nseg consecutive planes of b and x (a stacked
+// operator's right-hand sides); iters and res receive nseg entries
 int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter, double reltol, double abstol,
-           cudaStream_t st, int* iters, double* res);
+           cudaStream_t st, int* iters, double* res, int nseg = 1);
 
 // `iters` CG iterations with no tolerance test and no host synchronisation,
 // so the sequence can be recorded into a CUDA graph; op->cg must already be

@@ -108,7 +108,13 @@ __global__ void __launch_bounds__(512) k_lambda_pass(LamPassArgs a) {
   float2* X0 = fft_lines(s, s1, a.pl, ly, -1.f, tw, pin, false);
   float2* X1 = (X0 == s) ? s1 : s;
   // per-voxel contraction (in place in the spectrum buffer)
-  for (int pos = threadIdx.x; pos < a.TC * L; pos += blockDim.x) {
+  if (lam_is_diag(a.lam_mode)) {
+    for (int pos = threadIdx.x; pos < a.TC * L; pos += blockDim.x) {
+      const float2 l = lam_diag_entry(a.lam_mode, a.lam, lam_elem(tile, pos / a.TC, pos % a.TC, 0, a.TC, 1, a.FC, a.NCH));
+      for (int k = 0; k < a.K; ++k) X0[k * a.lstride + pos] = cmul(l, X0[k * a.lstride + pos]);
+    }
+  }
+  for (int pos = threadIdx.x; pos < a.TC * L && !lam_is_diag(a.lam_mode); pos += blockDim.x) {
     const int li = pos % a.TC;
     const int f = pos / a.TC;
     float2 X[KMAX], Y[KMAX];
@@ -258,6 +264,13 @@ __global__ void k_lam_to_packed(LamLayout g, const T* lam, const int64_t* kmask,
     const int64_t cell = kmask[i] - 1;
     for (int p = 0; p < g.P; ++p) packed[p + (int64_t)g.P * i] = lam[lam_int_index(g, cell, p)];
   }
+}
+
+// the same rank-1 kernel in another chunked layout (P = 1 in both), every grid cell
+template <class T>
+__global__ void k_lam_relayout(LamLayout src, LamLayout dst, const T* a, T* b) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < dst.ngrid; c += (int64_t)gridDim.x * blockDim.x)
+    b[lam_int_index(dst, c, 0)] = a[lam_int_index(src, c, 0)];
 }
 
 __global__ void k_flags_nonzero_c(const float2* lam_full, int64_t stride, int64_t n, uint8_t* flags) {
@@ -610,10 +623,10 @@ static int64_t env_int(const char* name, int64_t dflt) {
 }
 
 int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_shape, int K, int ncoils,
-                     int precision) {
+                     int precision, int kmax) {
   MRSR_REQUIRE(ndims == 2 || ndims == 3, MRSR_ERR_ARG, "ndims must be 2 or 3 (got %d)", ndims);
   MRSR_REQUIRE(img_shape != nullptr, MRSR_ERR_ARG, "img_shape is NULL");
-  MRSR_REQUIRE(K >= 1 && K <= KMAX, MRSR_ERR_UNSUPPORTED, "rank K=%d outside 1..%d", K, KMAX);
+  MRSR_REQUIRE(K >= 1 && K <= kmax, MRSR_ERR_UNSUPPORTED, "rank K=%d outside 1..%d", K, kmax);
   MRSR_REQUIRE(ncoils >= 1, MRSR_ERR_ARG, "ncoils must be >= 1");
   MRSR_REQUIRE(precision >= MRSR_PREC_FP32 && precision <= MRSR_PREC_FP16_TC, MRSR_ERR_ARG, "unknown precision %d",
                precision);
@@ -734,7 +747,7 @@ static LamLayout lam_layout(const mrsr_normalop* op) {
 // and at most 16 KB per chunk, so a chunk streams through a small shared ring.
 static void choose_fc(mrsr_normalop* op) {
   const int L = (int)op->geo.glast();
-  const int esz = op->lam_mode == LAM_PACKED_REAL ? 4 : 8;
+  const int esz = lam_is_real(op->lam_mode) ? 4 : 8;
   int best = 1;
   for (int fc = 1; fc <= L; ++fc) {
     if (L % fc) continue;
@@ -872,7 +885,7 @@ extern "C" int mrsr_normalop_info(const mrsr_normalop* op, int64_t* info) {
   MRSR_REQUIRE(op && info, MRSR_ERR_ARG, "NULL argument");
   const OpGeom& g = op->geo;
   int64_t v[12] = {op->kind, g.ndims, g.n[0], g.n[1], g.n[2], g.K, g.ncoils, op->nk,
-                   op->lam_mode != LAM_PACKED_REAL ? 1 : 0, op->precision, op->P, op->launches};
+                   lam_is_real(op->lam_mode) ? 0 : 1, op->precision, op->P, op->launches};
   std::memcpy(info, v, sizeof(v));
   return MRSR_OK;
 }
@@ -905,6 +918,8 @@ __global__ void k_unpack_full(const void* packed, int real, int K, int64_t nk, f
 extern "C" int mrsr_normalop_get_lambda(const mrsr_normalop* op, void* out, mrsr_stream_t stream) {
   MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(op && out, MRSR_ERR_ARG, "NULL argument");
+  MRSR_REQUIRE(!lam_is_diag(op->lam_mode), MRSR_ERR_UNSUPPORTED,
+               "a stacked operator holds its source operator's kernel: read Λ from the source");
   cudaStream_t st = as_stream(stream);
   OpUse use{op, st};
   LamLayout l = lam_layout(op);
@@ -958,6 +973,64 @@ extern "C" int mrsr_normalop_profile(mrsr_normalop* op, const float* x, float* y
     if (s != MRSR_OK) return s;
   }
   for (int i = 0; i < op->launches; ++i) ms_per_pass[i] = (float)(acc[i] / iters);
+  return MRSR_OK;
+}
+
+extern "C" int mrsr_normalop_stack(const mrsr_normalop* src, int nrhs, mrsr_stream_t stream, mrsr_normalop** out) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
+  MRSR_REQUIRE(out, MRSR_ERR_ARG, "out is NULL");
+  *out = nullptr;
+  MRSR_REQUIRE(src, MRSR_ERR_ARG, "source operator is NULL");
+  MRSR_REQUIRE(src->lam.p, MRSR_ERR_STATE, "source operator has no kernel");
+  MRSR_REQUIRE(src->geo.K == 1 && src->precision == MRSR_PREC_FP32 && !lam_is_diag(src->lam_mode),
+               MRSR_ERR_UNSUPPORTED, "stacking needs a float32 operator of rank K = 1 (got K = %d)", src->geo.K);
+  MRSR_REQUIRE(nrhs >= 1 && nrhs <= kStackMax, MRSR_ERR_ARG, "nrhs must be in 1..%d (got %d)", kStackMax, nrhs);
+  const OpGeom& g = src->geo;
+  // the row and Λ passes hold every plane of a line (two copies in the generic kernels)
+  const int64_t lmax = std::max(g.g[0], g.glast());
+  MRSR_REQUIRE((2 * (int64_t)nrhs + 1) * lmax * 8 <= 227 * 1024, MRSR_ERR_UNSUPPORTED,
+               "%d stacked right-hand sides of %lld-point lines exceed the shared memory of one block", nrhs,
+               (long long)lmax);
+  cudaStream_t st = as_stream(stream);
+  mrsr_normalop* op = new mrsr_normalop();
+  int s = op_init_geometry(op, src->kind, g.ndims, g.n, nrhs, g.ncoils, MRSR_PREC_FP32, kStackMax);
+  if (s == MRSR_OK) {
+    const bool real = lam_is_real(src->lam_mode);
+    op->lam_mode = real ? LAM_DIAG_REAL : LAM_DIAG_CPLX;
+    op->P = 1;
+    op->nk = src->nk;
+    choose_fc(op);
+    const size_t esz = real ? sizeof(float) : sizeof(float2);
+    s = op->lam.alloc(esz * (size_t)g.ngrid());
+    if (s == MRSR_OK) {
+      const LamLayout ls = lam_layout(src), ld = lam_layout(op);
+      const unsigned blocks = (unsigned)std::min<int64_t>(cdiv(g.ngrid(), 256), 65535);
+      if (real)
+        k_lam_relayout<float><<<blocks, 256, 0, st>>>(ls, ld, src->lam.as<float>(), op->lam.as<float>());
+      else
+        k_lam_relayout<float2><<<blocks, 256, 0, st>>>(ls, ld, src->lam.as<float2>(), op->lam.as<float2>());
+      if (cudaGetLastError() != cudaSuccess) {
+        set_error("Λ relayout launch failed");
+        s = MRSR_ERR_CUDA;
+      }
+    }
+    if (s == MRSR_OK) s = op->kmask.alloc(sizeof(int64_t) * (size_t)src->nk);
+    if (s == MRSR_OK &&
+        cudaMemcpyAsync(op->kmask.p, src->kmask.p, sizeof(int64_t) * src->nk, cudaMemcpyDeviceToDevice, st) !=
+            cudaSuccess) {
+      set_error("kmask copy failed");
+      s = MRSR_ERR_CUDA;
+    }
+    if (s == MRSR_OK && src->cmaps.p) s = op_set_cmaps(op, src->cmaps.as<float>(), st);
+  }
+  if (s == MRSR_OK) s = op_finalize(op, st);
+  if (s != MRSR_OK) {
+    delete op;
+    return s;
+  }
+  mark_use(src, st);
+  mark_use(op, st);
+  *out = op;
   return MRSR_OK;
 }
 

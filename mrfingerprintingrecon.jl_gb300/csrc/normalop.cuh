@@ -11,8 +11,14 @@ namespace mrsr {
 enum LamMode : int {
   LAM_PACKED_REAL = 0,  // P = K(K+1)/2 reals, symmetric (real basis, ext:140-191)
   LAM_PACKED_CPLX = 1,  // P complex, Hermitian upper triangle (ext:89-137)
-  LAM_FULL_CPLX = 2     // K*K complex, column-major (FFTNormalOp, src/FFTNormalOp.jl:331)
+  LAM_FULL_CPLX = 2,    // K*K complex, column-major (FFTNormalOp, src/FFTNormalOp.jl:331)
+  // an operator on stacked right-hand sides (mrsr_normalop_stack): K planes, each
+  // transformed by the same scalar kernel of a rank-1 operator (P = 1)
+  LAM_DIAG_REAL = 3,
+  LAM_DIAG_CPLX = 4
 };
+__host__ __device__ inline bool lam_is_diag(int mode) { return mode == LAM_DIAG_REAL || mode == LAM_DIAG_CPLX; }
+__host__ __device__ inline bool lam_is_real(int mode) { return mode == LAM_PACKED_REAL || mode == LAM_DIAG_REAL; }
 
 struct OpGeom {
   int ndims = 2;
@@ -82,8 +88,10 @@ struct mrsr_normalop {
 
 namespace mrsr {
 // Build helpers shared by the constructors (normalop.cu).
+// kmax: the largest K accepted (the rank limit of the K x K contraction unless the
+// operator is a stacked one, whose planes are independent)
 int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_shape, int K,
-                     int ncoils, int precision);
+                     int ncoils, int precision, int kmax = 8);
 int op_set_cmaps(mrsr_normalop* op, const float* cmaps, cudaStream_t st);
 int op_finalize(mrsr_normalop* op, cudaStream_t st);
 // Λ from the reference's packed (P, nk) layout at 1-based kmask cells.

@@ -5,7 +5,8 @@
 
 namespace mrsr {
 
-constexpr int KMAX = 8;  // largest subspace rank compiled into the contraction
+constexpr int KMAX = 8;        // largest subspace rank compiled into the contraction
+constexpr int kStackMax = 64;  // most right-hand sides of a stacked operator (mrsr_normalop_stack)
 
 struct RowsFwdArgs {
   FftPlan pl;        // along dim 1, L = g1
@@ -69,6 +70,12 @@ struct RowsInvArgs {
   const float2* cmaps;  // (n1, nrows, ncoils) or null
   float2* y;            // (n1, nrows, K)
 };
+
+// Stacked right-hand sides: v <- λ v with the plane-independent scalar kernel entry at idx.
+__device__ __forceinline__ float2 lam_diag_entry(int mode, const void* lam, int64_t idx) {
+  return mode == LAM_DIAG_REAL ? make_float2(reinterpret_cast<const float*>(lam)[idx], 0.f)
+                               : reinterpret_cast<const float2*>(lam)[idx];
+}
 
 // Per-voxel K x K product Y = Λ X at one frequency (X, Y in registers).
 // lam points at entry p = 0 of this voxel; consecutive entries are pstride apart.

@@ -37,24 +37,26 @@ __global__ void k_sv_add(float2* y, const float2* x, int64_t n) {
     y[i] = make_float2(b.x + a.x, b.y + a.y);
   }
 }
-// |a|^2, deterministic, in two launches: per-block partials (float32 within a warp,
-// float64 across warps), then one block sums them in a fixed order.  No per-element
-// work runs in float64 (a small fraction of the float32 rate on GB300).
+// |a|^2, deterministic, in two launches: per-block partials (a thread's few squares in
+// float32, then float64 across threads and warps), then one thread sums them in block
+// order.  No per-element work runs in float64 (a small fraction of the float32 rate on
+// GB300).
 constexpr int kNormBlocks = 256;
 static unsigned norm_grid(int64_t n) {
   return (unsigned)std::min<int64_t>(kNormBlocks, std::max<int64_t>(1, cdiv(n, 4 * kVecThreads)));
 }
 __global__ void k_sv_norm2_part(const float2* a, int64_t n, double* part) {
-  __shared__ float wsum[kVecThreads / 32];
+  __shared__ double wsum[kVecThreads / 32];
   float acc = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     acc = fmaf(a[i].x, a[i].x, fmaf(a[i].y, a[i].y, acc));
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;
+  double d = acc;
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = d;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int w = 0; w < kVecThreads / 32; ++w) s += (double)wsum[w];
+    for (int w = 0; w < kVecThreads / 32; ++w) s += wsum[w];
     part[blockIdx.x] = s;
   }
 }

@@ -137,6 +137,13 @@ class NormalOperator:
         op._cmaps_ref = S
         return op
 
+    def stack(self, nrhs, stream=None):
+        """An operator on ``nrhs`` stacked images (img..., nrhs) that applies this rank-1
+        float32 operator to each plane independently (for :func:`cg_stacked`)."""
+        op = _new_handle(_lib.load().mrsr_normalop_stack, self._h, int(nrhs), stream_handle(stream))
+        op._stack_source = self
+        return op
+
     def profile(self, x, y, iters=10, stream=None):
         """Per-pass device milliseconds of one apply (CUDA events between launches)."""
         xi, yi = self._as_image(x), self._as_image(y)

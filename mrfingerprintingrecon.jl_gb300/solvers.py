@@ -42,6 +42,26 @@ def cg(A, b, maxiter=None, reltol=DEFAULT_RELTOL, abstol=0.0, log=False, stream=
     return out
 
 
+def cg_stacked(A, b, maxiter=None, reltol=DEFAULT_RELTOL, abstol=0.0, log=False, stream=None):
+    """One ``cg(A1, b[..., i]; maxiter, reltol, abstol)`` per plane i of ``b`` (img..., nrhs),
+    where ``A = A1.stack(nrhs)``; the solves run together (one launch per step for all
+    planes) but each keeps its own iteration.  ``log=True`` also returns per-plane
+    iteration counts and residual norms (lists)."""
+    lib = _lib.load()
+    bi = A._as_image(b)
+    x = jl_empty(bi.shape, torch.complex64)
+    nrhs = A.Ncoeff
+    if maxiter is None:
+        maxiter = int(np.prod(A.shape_img))  # size(A1, 2) of the rank-1 operator
+    its = (C.c_int * nrhs)()
+    rns = (C.c_double * nrhs)()
+    _lib.check(lib.mrsr_cg_stacked(A.handle, ptr(bi), ptr(x), int(maxiter), float(reltol), float(abstol), its, rns,
+                                   stream_handle(stream)))
+    if log:
+        return CgResult(x, list(its), list(rns))
+    return x
+
+
 def cg_refined(A_lo, A_hi, b, inner_iters=20, max_outer=10, tol=1e-4, log=False, stream=None):
     """Mixed-precision iterative refinement: x <- x + CG_lo(b - A_hi x) until
     ||b - A_hi x|| <= tol ||b|| (A_lo a reduced-precision operator, A_hi float32),

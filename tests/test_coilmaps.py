@@ -3,7 +3,8 @@ coil-wise reconstructions on the GPU against the float64 oracle.
 
 ``reconstruct_coilwise`` solves one K=1 system per receive channel on a single
 operator (src/CoilMaps.jl:118-162).  Checks:
-* the graph of Nc solves equals Nc sequential ``cg`` calls on the same operator (1e-6);
+* the Nc solves on the operator stacked over the coils equal Nc sequential ``cg`` calls
+  on the same operator (1e-6);
 * the coil images agree with the float64 oracle's 20-iteration CG on the exact-PSF
   operator within 1e-2 (the reference's CPU-vs-GPU tolerance,
   test/reconstruct_radial_gpu.jl:103; the GPU NUFFT uses the ES kernel).  Two operators
@@ -106,7 +107,7 @@ def test_reconstruct_coilwise_noncartesian(mr, cuda, cplx_u, masked):
     U1 = U[:, :1]
     ref = _oracle_coilwise(data, trj, img, U1, mask, 20)
     assert rel_l2(x, ref) < 1e-2
-    # the graph of per-coil solves against the sequential entry point on the same operator
+    # the stacked per-coil solves against the sequential entry point on the same operator
     A = mr.NFFTNormalOp(img, trj, U1, sample_mask=mask)
     b = mr.calculate_backprojection(data, trj, img, U=U1, sample_mask=mask)
     xb = mr.to_host(coilmaps._coilwise_solve(A, b, 20))
