@@ -603,7 +603,8 @@ def pipeline_arm(args, world, rank, local):
             work = data0.clone()
             st["grog_gridding"] = _events_ms(lambda: mr.grog_gridding(work, trj, lnG, Nr, img), 1, stream)
         # calculate_coil_maps up to ESPIRiT: 32^2 calibration region, 32 coil-wise K=1 solves of
-        # 100 CG iterations (one graph), operator and backprojection included
+        # 100 CG iterations (on the operator stacked over the coils), operator and backprojection
+        # included
         mask_cal, trj_cal, calib = mr.calibration_mask(mr.to_host(trj), img)
         mr.reconstruct_coilwise(data0, trj_cal, calib, sample_mask=mask_cal)
         st["coilwise_calibration"] = _wall_ms(

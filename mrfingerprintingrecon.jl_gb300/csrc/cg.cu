@@ -226,7 +226,9 @@ int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter
       if (!v.done) return false;
     return true;
   };
-  const int chunk = 8;
+  // with no tolerance only an exact zero residual ends a solve early, and the device's
+  // done flag already turns the iterations after it into no-ops: launch them all
+  const int chunk = (reltol > 0.0 || abstol > 0.0) ? 8 : std::max(maxiter, 1);
   for (int it0 = 0; it0 < maxiter; it0 += chunk) {
     const int nit = std::min(chunk, maxiter - it0);
     for (int k = 0; k < nit; ++k) {

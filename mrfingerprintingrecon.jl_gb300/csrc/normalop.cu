@@ -523,15 +523,22 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
     // fp16-tc: row passes on the tensor cores too (MRSR_TC_ROWS=0 keeps them in float32)
     const bool tc_rows = op->precision == MRSR_PREC_FP16_TC && tc_rows_enabled() &&
                          tc_rows_supported(L1, (int)g.n[0], ncg);
+    // a stacked operator's planes are independent: without coil maps the rows pass sees
+    // them as more rows of one plane, and the Λ pass as more coils, so small images still
+    // fill the GPU (the stack layout [coil][plane][row][...] is the same either way)
+    const bool diag = lam_is_diag(op->lam_mode);
+    const bool flat_rows = diag && !cm;
     // P1: rows forward
     {
-      RowTiling t = rows_tiling(L1, K, nrows, true);
-      RowsFwdArgs a{op->plan[0].plan, (int)g.n[0], nrows, t.rpc, K, c0, t.lstride, x, cm, st1};
-      dim3 grid((unsigned)cdiv(nrows, t.rpc), ncg);
+      const int Kr = flat_rows ? 1 : K;
+      const int64_t nr = flat_rows ? nrows * K : nrows;
+      RowTiling t = rows_tiling(L1, Kr, nr, true);
+      RowsFwdArgs a{op->plan[0].plan, (int)g.n[0], nr, t.rpc, Kr, c0, t.lstride, x, cm, st1};
+      dim3 grid((unsigned)cdiv(nr, t.rpc), ncg);
       if (tc_rows)
         MRSR_TRY(tc_rows_fwd(a, ncg, op->tc_consts.p, op->errflag.as<int>(), st));
       else if (fast_length(L1))
-        MRSR_TRY(fast_rows_fwd(a, nrows, ncg, st));
+        MRSR_TRY(fast_rows_fwd(a, nr, ncg, st));
       else
         MRSR_TRY(launch_fft_kernel<RowsFwdArgs>(k_rows_fwd, grid, t.threads, t.smem, st, a));
       MRSR_TRY(rec.record());
@@ -557,15 +564,16 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
     {
       const int Ll = (int)g.glast();
       const int TC = op->TC;
-      LamPassArgs a{op->plan[g.ndims - 1].plan, (int)g.nlast(), (int)g.nlast(), (int)g.nlast(), g.inner(), TC, K,
+      const int Kl = diag ? 1 : K, ncl = diag ? ncg * K : ncg;
+      LamPassArgs a{op->plan[g.ndims - 1].plan, (int)g.nlast(), (int)g.nlast(), (int)g.nlast(), g.inner(), TC, Kl,
                     op->P, op->lam_mode, Ll * TC, op->lam.p, lam_stack, op->FC, (int)(Ll / op->FC)};
-      dim3 grid((unsigned)(g.inner() / TC), ncg);
-      const size_t smem = sizeof(float2) * ((size_t)Ll + 2 * (size_t)K * a.lstride);
+      dim3 grid((unsigned)(g.inner() / TC), ncl);
+      const size_t smem = sizeof(float2) * ((size_t)Ll + 2 * (size_t)Kl * a.lstride);
       if (op->precision == MRSR_PREC_FP16_TC) {
         a.lam = op->lam_tc.p;
         MRSR_TRY(tc_lambda(a, ncg, op->lam_max.as<float>(), op->tc_consts.p, op->errflag.as<int>(), st));
       } else if (fast_length(Ll))
-        MRSR_TRY(fast_lambda(a, ncg, op->Cg * K, op->errflag.as<int>(), st));
+        MRSR_TRY(fast_lambda(a, ncl, op->Cg * K, op->errflag.as<int>(), st));
       else
         MRSR_TRY(launch_fft_kernel<LamPassArgs>(k_lambda_pass, grid, 512, smem, st, a));
       MRSR_TRY(rec.record());
