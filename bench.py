@@ -381,8 +381,9 @@ def gb300_arm(args, world, rank, local):
                    "fp32_cg_iters": conv.iters, "fp32_cg_relres": conv.resnorm / float(torch.linalg.norm(b)),
                    "fp32_cg_s": t_conv,
                    "refined_s": t_ref}
-        mixed = {"precision": "fp16-tc", "operator": "tensor-core Λ pass (tcgen05 DFT-64, fp16 operands with per-tile "
-                 "scales, fp32 accumulation), float32 row passes", "applies_s": world * 1000.0 / ms_t,
+        mixed = {"precision": "fp16-tc", "operator": "tensor-core Λ pass and inverse row pass (tcgen05 DFT-64, fp16 "
+                 "operands with per-tile scales, fp32 accumulation), float32 forward row pass",
+                 "applies_s": world * 1000.0 / ms_t,
                  "ms_per_apply": ms_t, "vs_fp32": ms / ms_t, "apply_rel_l2_vs_fp32": err,
                  "cg20_image_rel_l2_vs_fp32": cg_err, "refined_solve": refined,
                  "pass_ms": [round(p_, 5) for p_ in At.profile(x, yt, iters=20)]}
@@ -399,7 +400,8 @@ def gb300_arm(args, world, rank, local):
         "config": {"workload": args.workload, "img": list(w["img"]), "Nr": w["Nr"], "Ncyc": w["Ncyc"], "Nt": w["Nt"],
                    "Nc": Nc, "K": K, "precision": prec,
                    "operator": "NFFTNormalOp " + {"fp32": "float32", "fp16": "fp16 storage, float32 arithmetic",
-                                                  "fp16-tc": "float32 rows, tensor-core Λ pass"}[prec]
+                                                  "fp16-tc": "tensor-core Λ and inverse row passes, float32 "
+                                                             "forward row pass"}[prec]
                    + " (real basis, packed real kernel)",
                    "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) before every timed step"},
         "e2e": {"value": world * 1000.0 / ms_e2e, "unit": "applies/s", "h2d_bytes_per_step": int(xh.numel() * 8),

@@ -501,6 +501,17 @@ static bool tc_rows_enabled() {
   return on;
 }
 
+// The forward row pass of the fp16-tc operator stays float32 unless MRSR_TC_ROWS_FWD=1:
+// on 256^2 with 20 coils the float32 four-step kernel (rows per CTA chosen to fill its
+// threads) takes 0.039 ms against the tensor-core kernel's 0.042, and adds no fp16 rounding.
+static bool tc_rows_fwd_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("MRSR_TC_ROWS_FWD");
+    return e && e[0] == '1';
+  }();
+  return on;
+}
+
 static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
                       Recorder rec) {
   if (op->precision == MRSR_PREC_FP16 || op->precision == MRSR_PREC_FP16_ARITH) {
@@ -520,9 +531,10 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
   for (int grp = 0; grp < ngroups; ++grp) {
     const int c0 = grp * op->Cg;
     const int ncg = std::min(op->Cg, g.ncoils - c0);
-    // fp16-tc: row passes on the tensor cores too (MRSR_TC_ROWS=0 keeps them in float32)
+    // fp16-tc: the inverse row pass on the tensor cores too (MRSR_TC_ROWS=0 keeps it in float32)
     const bool tc_rows = op->precision == MRSR_PREC_FP16_TC && tc_rows_enabled() &&
                          tc_rows_supported(L1, (int)g.n[0], ncg);
+    const bool tc_rows_f = tc_rows && tc_rows_fwd_enabled();
     // a stacked operator's planes are independent: without coil maps the rows pass sees
     // them as more rows of one plane, and the Λ pass as more coils, so small images still
     // fill the GPU (the stack layout [coil][plane][row][...] is the same either way)
@@ -535,7 +547,7 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       RowTiling t = rows_tiling(L1, Kr, nr, true);
       RowsFwdArgs a{op->plan[0].plan, (int)g.n[0], nr, t.rpc, Kr, c0, t.lstride, x, cm, st1};
       dim3 grid((unsigned)cdiv(nr, t.rpc), ncg);
-      if (tc_rows)
+      if (tc_rows_f)
         MRSR_TRY(tc_rows_fwd(a, ncg, op->tc_consts.p, op->errflag.as<int>(), st));
       else if (fast_length(L1))
         MRSR_TRY(fast_rows_fwd(a, nr, ncg, st));
