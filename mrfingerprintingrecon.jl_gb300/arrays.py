@@ -57,6 +57,16 @@ def to_jl(a, dtype):
     return out
 
 
+def mask_u8(m):
+    """Column-major uint8 CUDA tensor of a sample mask (numpy array or tensor, bool or
+    integer), or None."""
+    if m is None:
+        return None
+    if isinstance(m, torch.Tensor):
+        return to_jl(m if m.dtype == torch.uint8 else m.to(torch.uint8), torch.uint8)
+    return to_jl(np.asarray(m, dtype=np.uint8), torch.uint8)
+
+
 def jl_reshape(t, shape):
     """Julia ``reshape`` (column-major) of a column-major tensor; shares memory."""
     shape = list(shape)

@@ -5,7 +5,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .arrays import is_complex_array, jl_empty, jl_reshape, ptr, stack_cmaps, stream_handle, to_jl
+from .arrays import is_complex_array, jl_empty, jl_reshape, mask_u8, ptr, stack_cmaps, stream_handle, to_jl
 
 _DCF = {"none": _lib.DCF_NONE, "radial_2D": _lib.DCF_RADIAL_2D, "radial_3D": _lib.DCF_RADIAL_3D}
 
@@ -61,7 +61,9 @@ def calculate_backprojection(data, trj, cmaps_or_img_shape, U=None, sample_mask=
     if t.dim() == 4 and dt.dim() == 4:  # wrapper for (Nr, Ncyc, ...) sample axes (src/BackProjection.jl:159-164)
         dt = jl_reshape(dt, (-1, dt.shape[2], dt.shape[3]))
         t = jl_reshape(t, (t.shape[0], -1, t.shape[3]))
-        if sample_mask is not None:
+        if isinstance(sample_mask, torch.Tensor):
+            sample_mask = jl_reshape(mask_u8(sample_mask), (-1, sample_mask.shape[-1]))
+        elif sample_mask is not None:
             m = np.asarray(sample_mask)
             sample_mask = m.reshape((-1, m.shape[-1]), order="F")
     nrep = int(dt.shape[3]) if dt.dim() == 4 else 1
@@ -75,7 +77,7 @@ def calculate_backprojection(data, trj, cmaps_or_img_shape, U=None, sample_mask=
     ncoils = int(dt.shape[2])
     if S is not None and not int_traj:
         test_dimension(dt, t, Ut, ncm, d, nt_u)
-    m = None if sample_mask is None else to_jl(np.asarray(sample_mask, dtype=np.uint8), torch.uint8)
+    m = mask_u8(sample_mask)
     out = jl_empty(img_shape + ((K,) if S is not None else (K, ncoils)), torch.complex64)
     if int_traj:
         _lib.check(lib.mrsr_backprojection_cartesian(d, _lib.int64_array(img_shape), int(t.shape[1]), nt, ncoils, nrep,

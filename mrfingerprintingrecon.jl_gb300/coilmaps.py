@@ -19,7 +19,7 @@ host array.
 import numpy as np
 import torch
 
-from .arrays import jl_reshape, jl_zeros, to_host, to_jl
+from .arrays import jl_reshape, jl_zeros, mask_u8, to_host, to_jl
 from .backprojection import _is_int_traj, calculate_backprojection
 from .normalop import FFTNormalOp, NFFTNormalOp
 from .solvers import DEFAULT_RELTOL, CgBatch, cg, cg_stacked
@@ -44,6 +44,10 @@ def reconstruct_coilwise(data, trj, img_shape, U=None, sample_mask=None, Niter_c
     U1 = _first_basis_column(U, int(trj.shape[-1]))
     if Niter_cg is None:
         Niter_cg = 5 if cart else 100  # the reference's defaults
+    # the operator and the backprojection read the same trajectory and mask: upload once
+    if trj.ndim == 3:
+        trj = to_jl(trj, torch.int32 if cart else torch.float32)
+        sample_mask = mask_u8(sample_mask)
     if cart:
         A = FFTNormalOp(img_shape, trj, U1, sample_mask=sample_mask, stream=stream)
     else:

@@ -14,7 +14,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .arrays import (is_complex_array, jl_empty, ptr, stack_cmaps, stream_handle, to_jl)
+from .arrays import (is_complex_array, jl_empty, jl_reshape, mask_u8, ptr, stack_cmaps, stream_handle, to_jl)
 
 _PREC = {"fp32": _lib.PREC_FP32, "fp16": _lib.PREC_FP16, "fp16-arith": _lib.PREC_FP16_ARITH,
          "fp16-tc": _lib.PREC_FP16_TC}
@@ -191,13 +191,15 @@ def NFFTNormalOp(img_shape, trj_or_lambda, U_or_kmask, cmaps=None, sample_mask=N
         trj = to_jl(arr, torch.float32)
         if trj.dim() == 4:  # 4D wrapper (src/NFFTNormalOp.jl:45-49)
             trj = to_jl(trj.reshape(trj.shape[0], -1, trj.shape[3]), torch.float32)
-            if sample_mask is not None:
+            if isinstance(sample_mask, torch.Tensor):
+                sample_mask = jl_reshape(mask_u8(sample_mask), (-1, sample_mask.shape[-1]))
+            elif sample_mask is not None:
                 sample_mask = np.asarray(sample_mask).reshape(-1, np.asarray(sample_mask).shape[-1], order="F")
         U = U_or_kmask
         ucplx = is_complex_array(U)
         Ut = to_jl(U, torch.complex64 if ucplx else torch.float32)
         K = int(Ut.shape[1])
-        m = None if sample_mask is None else to_jl(np.asarray(sample_mask, dtype=np.uint8), torch.uint8)
+        m = mask_u8(sample_mask)
         return _new_handle(lib.mrsr_nfft_normalop_create, d, _lib.int64_array(img_shape), int(trj.shape[1]),
                            int(trj.shape[2]), ptr(trj), ptr(m), ptr(Ut), int(ucplx), K, ptr(S), nc,
                            _prec(precision), stream_handle(stream))
@@ -242,7 +244,7 @@ def FFTNormalOp(*args, cmaps=None, sample_mask=None, precision="fp32", stream=No
     ucplx = is_complex_array(U)
     Ut = to_jl(U, torch.complex64 if ucplx else torch.float32)
     nrep = int(Ut.shape[2]) if Ut.dim() == 3 else 1
-    m = None if sample_mask is None else to_jl(np.asarray(sample_mask, dtype=np.uint8), torch.uint8)
+    m = mask_u8(sample_mask)
     return _new_handle(lib.mrsr_fft_normalop_create, len(img_shape), _lib.int64_array(img_shape), int(t.shape[1]),
                        int(t.shape[2]), ptr(t), ptr(m), ptr(Ut), int(ucplx), int(Ut.shape[1]), nrep, ptr(S), nc,
                        _prec(precision), stream_handle(stream))
