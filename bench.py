@@ -529,6 +529,13 @@ def _wall_ms(fn, reps):
     return 1e3 * (time.perf_counter() - t0) / reps
 
 
+def _apply_roofline(nbytes, ms):
+    peak, kind = measured_peaks()
+    gbs = nbytes / (ms * 1e-3) / 1e9
+    return {"algorithmic_bytes": int(nbytes), "achieved_gbs": gbs, "peak": peak, "frac": gbs / peak,
+            "peak_source": f"{kind} MEASURED_PEAKS hbm_gbs" if kind == "measured" else "fallback"}
+
+
 def pipeline_arm(args, world, rank, local):
     """The other benchmark configurations, stage by stage (one process per GPU, replicas).
 
@@ -582,8 +589,14 @@ def pipeline_arm(args, world, rank, local):
         st["refined_2x20_fp16"] = _events_ms(lambda: mr.cg_refined(A16, A, b, inner_iters=20, max_outer=2, tol=0.0),
                                              1, stream)
         value, unit = 1000.0 / ms32, "applies/s"
+        # algorithmic bytes of one 3D apply: x in, y out, coil maps in both row passes, the two
+        # half-pruned stacks (2N x N x N and 2N x 2N x N per coil and coefficient) written and
+        # read once per direction, the kernel read once
+        m1, m2 = 2 * N * N * N * K, 4 * N * N * N * K
+        b3 = N ** 3 * K * 16 + 2 * Nc * N ** 3 * 8 + 4 * Nc * (m1 + m2) * 8 + A.nk * A.P * (
+            8 if A.lambda_is_complex else 4)
         extra = {"fp16_applies_s": 1000.0 / ms16, "fp16_vs_fp32_apply_rel_l2": diff,
-                 "refined_relres_after_2x20": res.resnorm}
+                 "refined_relres_after_2x20": res.resnorm, "apply_roofline": _apply_roofline(b3, ms32)}
         cfg = {"workload": PIPE3D, "img": list(img), "Nr": Nr, "Ncyc": Ncyc, "Nt": Nt, "Nc": Nc, "K": K,
                "trajectory": "koosh-ball golden means", "samples": Nr * Ncyc * Nt}
     else:
@@ -623,7 +636,11 @@ def pipeline_arm(args, world, rank, local):
         st["apply"] = ms
         st["cg20"] = _events_ms(lambda: mr.cg(A, b, maxiter=20, reltol=0.0), 1, stream)
         value, unit = 1000.0 / ms, "applies/s"
-        extra = {}
+        # Cartesian apply: x in, y out, coil maps twice, the N^2 K stack per coil written and read
+        # once per direction, the kernel read once
+        bc = N * N * K * 16 + 2 * Nc * N * N * 8 + 4 * Nc * N * N * K * 8 + A.nk * A.P * (
+            8 if A.lambda_is_complex else 4)
+        extra = {"apply_roofline": _apply_roofline(bc, ms)}
         cfg = {"workload": PIPEGROG, "img": list(img), "Nr": Nr, "Ncyc": Ncyc, "Nt": Nt, "Nc": Nc, "K": K,
                "operator": "FFTNormalOp after GROG gridding"}
     if rank != 0:
