@@ -12,6 +12,7 @@
 // after convergence no-ops, so the host launches without synchronising.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
@@ -195,8 +196,21 @@ static unsigned vec_blocks(int64_t n) {
   return (unsigned)std::min<int64_t>(kCgBlocks, std::max<int64_t>(1, cdiv(n, 4 * kCgThreads)));
 }
 
+void CgWork::drop_graphs() {
+  if (it8) cudaGraphExecDestroy(it8);
+  if (it1) cudaGraphExecDestroy(it1);
+  it8 = it1 = nullptr;
+}
+
+CgWork::~CgWork() {
+  drop_graphs();
+  if (cap) cudaStreamDestroy(cap);
+}
+
 int CgWork::ensure(int64_t n_, int nseg_) {
   if (n == n_ && nseg == nseg_ && r.p) return MRSR_OK;
+  drop_graphs();
+  xw.release();  // cg_run allocates it at the new size
   n = n_;
   nseg = nseg_;
   MRSR_TRY(r.alloc(sizeof(float2) * n));
@@ -208,45 +222,101 @@ int CgWork::ensure(int64_t n_, int nseg_) {
   return MRSR_OK;
 }
 
+// one CG iteration on the workspace (iterate w.xw), enqueued on st
+static int cg_iter_enqueue(mrsr_normalop* op, CgWork& w, cudaStream_t st) {
+  const int64_t m = w.n / w.nseg;
+  CgState* s = w.state.as<CgState>();
+  double2* part = w.partial.as<double2>();
+  const dim3 nb(vec_blocks(m), (unsigned)w.nseg);
+  k_cg_dir<<<nb, kCgThreads, 0, st>>>(w.r.as<float2>(), w.u.as<float2>(), m, s);
+  MRSR_LAUNCH_CHECK();
+  MRSR_TRY(normalop_apply_internal(op, w.u.as<float2>(), w.c.as<float2>(), make_float2(1.f, 0.f),
+                                   make_float2(0.f, 0.f), st));
+  k_cg_alpha<<<nb, kCgThreads, 0, st>>>(w.u.as<float2>(), w.c.as<float2>(), m, s, part);
+  MRSR_LAUNCH_CHECK();
+  k_cg_update<<<nb, kCgThreads, 0, st>>>(w.xw.as<float2>(), w.r.as<float2>(), w.u.as<float2>(), w.c.as<float2>(), m,
+                                         s, part);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+// `iters` iterations recorded on the workspace's private stream into an executable graph
+static int cg_capture(mrsr_normalop* op, CgWork& w, int iters, cudaGraphExec_t* out) {
+  if (!w.cap) MRSR_CHECK_CUDA(cudaStreamCreateWithFlags(&w.cap, cudaStreamNonBlocking));
+  MRSR_CHECK_CUDA(cudaStreamBeginCapture(w.cap, cudaStreamCaptureModeThreadLocal));
+  int s = MRSR_OK;
+  for (int k = 0; k < iters && s == MRSR_OK; ++k) s = cg_iter_enqueue(op, w, w.cap);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(w.cap, &g);
+  if (s == MRSR_OK && e != cudaSuccess) {
+    set_error("CG graph capture failed: %s", cudaGetErrorString(e));
+    s = MRSR_ERR_CUDA;
+  }
+  if (s == MRSR_OK && cudaGraphInstantiate(out, g, 0) != cudaSuccess) {
+    set_error("CG graph instantiation failed");
+    s = MRSR_ERR_CUDA;
+  }
+  if (g) cudaGraphDestroy(g);
+  return s;
+}
+
+// MRSR_CG_GRAPH=0 launches every kernel of every iteration from the host instead
+static bool cg_graphs_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("MRSR_CG_GRAPH");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter, double reltol, double abstol,
            cudaStream_t st, int* iters, double* res, int nseg) {
   const int64_t n = op->geo.nimg() * op->geo.K;
   const int64_t m = n / nseg;  // unknowns per system
   MRSR_TRY(w.ensure(n, nseg));
+  if (!w.xw.p) MRSR_TRY(w.xw.alloc(sizeof(float2) * n));
   CgState* s = w.state.as<CgState>();
   double2* part = w.partial.as<double2>();
   const dim3 nb(vec_blocks(m), (unsigned)nseg);
-  k_cg_init<<<nb, kCgThreads, 0, st>>>(b, x, w.r.as<float2>(), w.u.as<float2>(), m, reltol, abstol, maxiter, s, part);
+  k_cg_init<<<nb, kCgThreads, 0, st>>>(b, w.xw.as<float2>(), w.r.as<float2>(), w.u.as<float2>(), m, reltol, abstol,
+                                       maxiter, s, part);
   MRSR_LAUNCH_CHECK();
-  // launch iterations in chunks; between chunks read the done flags so converged solves
-  // do not keep paying for applies
+  // The iterations run as graph launches of 8 (and single) iterations, recorded once per
+  // workspace; between blocks of 8 the host reads the done flags when a tolerance is set,
+  // so converged solves do not keep paying for applies.  Without a tolerance only an
+  // exact zero residual ends a solve early, and the device's done flag already turns the
+  // iterations after it into no-ops.
+  const bool graphs = cg_graphs_enabled();
+  if (graphs && maxiter >= 8 && !w.it8) MRSR_TRY(cg_capture(op, w, 8, &w.it8));
+  if (graphs && maxiter % 8 != 0 && !w.it1) MRSR_TRY(cg_capture(op, w, 1, &w.it1));
   std::vector<CgState> h((size_t)nseg);
   auto all_done = [&]() {
     for (const CgState& v : h)
       if (!v.done) return false;
     return true;
   };
-  // with no tolerance only an exact zero residual ends a solve early, and the device's
-  // done flag already turns the iterations after it into no-ops: launch them all
-  const int chunk = (reltol > 0.0 || abstol > 0.0) ? 8 : std::max(maxiter, 1);
-  for (int it0 = 0; it0 < maxiter; it0 += chunk) {
-    const int nit = std::min(chunk, maxiter - it0);
-    for (int k = 0; k < nit; ++k) {
-      k_cg_dir<<<nb, kCgThreads, 0, st>>>(w.r.as<float2>(), w.u.as<float2>(), m, s);
-      MRSR_LAUNCH_CHECK();
-      MRSR_TRY(normalop_apply_internal(op, w.u.as<float2>(), w.c.as<float2>(), make_float2(1.f, 0.f),
-                                       make_float2(0.f, 0.f), st));
-      k_cg_alpha<<<nb, kCgThreads, 0, st>>>(w.u.as<float2>(), w.c.as<float2>(), m, s, part);
-      MRSR_LAUNCH_CHECK();
-      k_cg_update<<<nb, kCgThreads, 0, st>>>(x, w.r.as<float2>(), w.u.as<float2>(), w.c.as<float2>(), m, s, part);
-      MRSR_LAUNCH_CHECK();
+  const bool check = reltol > 0.0 || abstol > 0.0;
+  int done_its = 0;
+  while (done_its < maxiter) {
+    const int nit = std::min(8, maxiter - done_its);
+    if (graphs && nit == 8) {
+      MRSR_CHECK_CUDA(cudaGraphLaunch(w.it8, st));
+    } else {
+      for (int k = 0; k < nit; ++k) {
+        if (graphs)
+          MRSR_CHECK_CUDA(cudaGraphLaunch(w.it1, st));
+        else
+          MRSR_TRY(cg_iter_enqueue(op, w, st));
+      }
     }
-    if (it0 + nit < maxiter) {
+    done_its += nit;
+    if (check && done_its < maxiter) {
       MRSR_CHECK_CUDA(cudaMemcpyAsync(h.data(), s, sizeof(CgState) * nseg, cudaMemcpyDeviceToHost, st));
       MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
       if (all_done()) break;
     }
   }
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(x, w.xw.p, sizeof(float2) * n, cudaMemcpyDeviceToDevice, st));
   int dev_err = 0;
   MRSR_CHECK_CUDA(cudaMemcpyAsync(h.data(), s, sizeof(CgState) * nseg, cudaMemcpyDeviceToHost, st));
   MRSR_CHECK_CUDA(cudaMemcpyAsync(&dev_err, op->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -10,9 +10,19 @@ struct CgWork {
   int64_t n = 0;
   int nseg = 0;     // independent systems (planes of n / nseg unknowns each)
   DevBuf r, u, c;   // residual, direction, A*direction
+  DevBuf xw;        // the iterate of cg_run (copied to the caller's x at the end)
   DevBuf state;     // device CgState per system (float64 scalars, iteration count, done flag)
   DevBuf partial;   // per-block float64 partial sums, per system
+  // cg_run's iterations recorded once per workspace as CUDA graphs of 8 and of 1
+  // iteration (they touch only this workspace and the operator's own buffers)
+  cudaGraphExec_t it8 = nullptr, it1 = nullptr;
+  cudaStream_t cap = nullptr;  // private stream the graphs are captured on
   int ensure(int64_t n, int nseg = 1);
+  void drop_graphs();
+  CgWork() = default;
+  CgWork(const CgWork&) = delete;
+  CgWork& operator=(const CgWork&) = delete;
+  ~CgWork();
 };
 
 // y <- beta y + alpha A x on the operator's stream-ordered passes (normalop.cu)
