@@ -26,7 +26,8 @@
  *    wait on mbarriers bound every wait; one that gives up writes the
  *    operator's error word and returns.  Applies are asynchronous, so the
  *    word is read where the library synchronises anyway (the end of
- *    mrsr_cg, mrsr_cg_noalloc, mrsr_cg_refined and mrsr_cg_batch_result)
+ *    mrsr_cg, mrsr_cg_stacked, mrsr_cg_noalloc, mrsr_cg_refined and
+ *    mrsr_cg_batch_result)
  *    and by mrsr_normalop_check; a set word becomes MRSR_ERR_DEVICE and is
  *    cleared.
  *  - Handles are not thread-safe; different handles are independent.
@@ -228,6 +229,8 @@ int mrsr_grog_gridding(int ndims, const int64_t* img_shape, int64_t nr, int64_t 
  * device (deterministic).  Stops after maxiter iterations or once
  * ||r|| <= max(reltol*||b||, abstol).  iters_out / resnorm_out are host
  * pointers (may be NULL); the call synchronises the stream to return them.
+ * The iterations run as launches of CUDA graphs (8 and 1 iterations) that the
+ * first solve on an operator records into its workspace.
  */
 int mrsr_cg(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
             int* iters_out, double* resnorm_out, mrsr_stream_t stream);
