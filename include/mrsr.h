@@ -4,8 +4,8 @@
  * Drop-in boundary for the GPU methods of MRISubspaceRecon.jl (published as
  * MRFingerprintingRecon.jl).  Each entry point replaces one reference method;
  * the reference file:line it replaces is given beside it.  A Julia package
- * extension binds these with `ccall` and keeps the
- * reference's Julia signatures.
+ * extension binds these with `ccall` and keeps the reference's Julia
+ * signatures.
  *
  * Conventions
  *  - All array arguments are DEVICE pointers unless stated otherwise, in
@@ -57,10 +57,7 @@ enum {
 enum {
   MRSR_PREC_FP32 = 0, /* float32 everywhere (the reference's precision)   */
   MRSR_PREC_FP16 = 1, /* fp16 storage with per-tile scales, fp32 arithmetic */
-  MRSR_PREC_FP16_ARITH = 2, /* fp16 storage and fp16 (half2) FFT / kernel
-                               arithmetic on line pairs, fp32 coil sums; 2D
-                               four-step grids with an even Λ tile width,
-                               else as MRSR_PREC_FP16                       */
+  /* 2 is not used (rejected with MRSR_ERR_ARG) */
   MRSR_PREC_FP16_TC = 3     /* float32 stack and row passes; the Λ pass runs
                                its 64-point column DFTs on the tensor cores
                                (tcgen05, fp16 operands with per-tile
@@ -166,10 +163,6 @@ int mrsr_normalop_profile(mrsr_normalop* op, const float* x, float* y, int iters
  * reference has no counterpart: its operators run on the CPU. */
 int mrsr_normalop_check(mrsr_normalop* op, mrsr_stream_t stream);
 
-/* Test hook: writes `code` into the operator's device error word (synchronous),
- * so the reporting path can be exercised without provoking a device fault. */
-int mrsr_test_set_device_error(mrsr_normalop* op, int code, mrsr_stream_t stream);
-
 void mrsr_normalop_destroy(mrsr_normalop* op);
 
 /* ---------------------------------------------------------------------
@@ -242,10 +235,12 @@ int mrsr_cg(mrsr_normalop* op, const float* b, float* x, int maxiter, double rel
  * static 32 MiB device array compiled into the library, so the solve is
  * limited to about 1.39 million unknowns (nimg * K); larger operators are
  * rejected with MRSR_ERR_UNSUPPORTED.  The first call on each device looks up
- * the array's device address (cudaGetSymbolAddress); make that first call
- * before any stream capture.  All calls share the one array: calls that
- * overlap on the GPU (other streams, other host threads) race and must be
- * serialised by the caller.  The operator itself must already exist. */
+ * the array's device address (cudaGetSymbolAddress).  Every call synchronises
+ * `stream` at its end (it reads the iteration count and residual back) and,
+ * when a tolerance is set, every 8 iterations, so it cannot be called inside
+ * a stream capture.  All calls share the one array: calls that overlap on the
+ * GPU (other streams, other host threads) race and must be serialised by the
+ * caller.  The operator itself must already exist. */
 int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int maxiter, double reltol, double abstol,
                     int* iters_out, double* resnorm_out, mrsr_stream_t stream);
 
@@ -266,7 +261,7 @@ int mrsr_cg_stacked(mrsr_normalop* op, const float* b, float* x, int maxiter, do
 
 /* Mixed-precision iterative refinement (no counterpart in the reference):
  * outer residual r = b - A_hi x with the float32 operator, inner CG on a
- * reduced-precision operator op_lo (fp16, fp16-arith or fp16-tc), until
+ * reduced-precision operator op_lo (fp16 or fp16-tc), until
  * ||r|| <= tol*||b||, max_outer, or an outer step that more than doubles
  * the residual (that step is undone and relres_out is the residual before
  * it).  op_lo and op_hi must describe the same operator. */

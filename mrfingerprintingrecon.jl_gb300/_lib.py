@@ -8,7 +8,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libmrsr.so"
 
 MRSR_OK, MRSR_ERR_ARG, MRSR_ERR_CUDA, MRSR_ERR_ALLOC, MRSR_ERR_UNSUPPORTED, MRSR_ERR_STATE, MRSR_ERR_DEVICE = range(7)
-PREC_FP32, PREC_FP16, PREC_FP16_ARITH, PREC_FP16_TC = 0, 1, 2, 3
+PREC_FP32, PREC_FP16, PREC_FP16_TC = 0, 1, 3
 DCF_NONE, DCF_RADIAL_2D, DCF_RADIAL_3D, DCF_ARRAY = range(4)
 KIND_NFFT, KIND_FFT = 0, 1
 
@@ -34,7 +34,6 @@ SIGNATURES = {
     "mrsr_normalop_get_lambda": [p, p, p],
     "mrsr_normalop_profile": [p, p, p, i32, C.POINTER(f32), p],
     "mrsr_normalop_check": [p, p],
-    "mrsr_test_set_device_error": [p, i32, p],
     "mrsr_normalop_destroy": [p],
     "mrsr_backprojection": [i32, i64p, i64, i64, i32, p, p, p, p, i32, i32, p, i32, p, p, p],
     "mrsr_backprojection_cartesian": [i32, i64p, i64, i64, i32, i32, p, p, p, p, i32, i32, p, p, p],
@@ -51,6 +50,8 @@ SIGNATURES = {
     "mrsr_cg_batch_launch": [p, p],
     "mrsr_cg_batch_result": [p, i32, C.POINTER(i32), C.POINTER(f64)],
     "mrsr_cg_batch_destroy": [p],
+    # internal test hook (include/mrsr_test.h), not part of the product ABI
+    "mrsr_test_set_device_error": [p, i32, p],
 }
 _VOID = {"mrsr_normalop_destroy", "mrsr_cg_batch_destroy"}
 _STR = {"mrsr_last_error"}

@@ -5,8 +5,6 @@
 // keeps its spectrum in the exchange buffer for the K x K product.
 #include "fft4.cuh"
 #include "passes.cuh"
-#include "tma.cuh"
-#include "tmap.cuh"
 
 #include <algorithm>
 #include <cstdlib>
@@ -245,139 +243,6 @@ __global__ void __launch_bounds__(512) k4_mid(MidArgs a, Slots sl) {
 }
 
 
-// Persistent Λ pass with TMA.  Each CTA walks over (tile, coil) items with a
-// grid stride.  The input tile (K planes x nin rows x TC columns) of the next
-// item is fetched by one cp.async.bulk.tensor copy into the second of two
-// staging buffers while the current item is transformed; Λ streams through a
-// ring of kLamRing chunk buffers filled by 1D bulk copies.  Both are tracked
-// by transaction-count mbarriers; waits are bounded and report KERR_MBAR_TIMEOUT.
-constexpr int kLamRing = 3;
-
-struct Lam5Cfg {
-  int nboxes, box_rows;   // input row boxes (box_rows <= 256)
-  int in_elems;           // float2 per input buffer = K * nboxes * box_rows * TC
-  int chunk_bytes;        // bytes per Λ chunk
-  int64_t ntiles, nitems;
-  int* err;
-  uint32_t off_tw, off_in0, off_in1, off_ring, off_slots;  // byte offsets in dynamic smem
-};
-
-template <class SP>
-__global__ void __launch_bounds__(512, 1) k5_lambda(LamPassArgs a, Slots sl, Lam5Cfg cf,
-                                                    const __grid_constant__ CUtensorMap tin) {
-  constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
-  extern __shared__ __align__(1024) unsigned char sraw[];
-  uint64_t* bar_in = reinterpret_cast<uint64_t*>(sraw);
-  uint64_t* bar_lam = bar_in + 2;
-  float2* tw = reinterpret_cast<float2*>(sraw + cf.off_tw);
-  float2* in0 = reinterpret_cast<float2*>(sraw + cf.off_in0);
-  float2* in1 = reinterpret_cast<float2*>(sraw + cf.off_in1);
-  unsigned char* ring = sraw + cf.off_ring;
-  float2* sm = reinterpret_cast<float2*>(sraw + cf.off_slots);
-  const bool leader = threadIdx.x == 0;
-  if (leader) {
-    mbar_init(&bar_in[0], 1);
-    mbar_init(&bar_in[1], 1);
-    for (int r = 0; r < kLamRing; ++r) mbar_init(&bar_lam[r], 1);
-    fence_mbar_init();
-  }
-  load_twiddles(tw, a.pl);
-  __syncthreads();
-  const int64_t G = gridDim.x;
-  const int64_t first = blockIdx.x;
-  const int nload = (a.nin * 2 == L) ? R1 / 2 : R1;
-  const int nkeep = (a.nout * 2 == L) ? R1 / 2 : R1;
-  const int64_t plane = (int64_t)a.nrow * a.inner;
-  const uint32_t in_bytes = (uint32_t)cf.in_elems * 8u;
-
-  auto issue_input = [&](int64_t item, int buf) {
-    const int64_t tile = item % cf.ntiles;
-    const int cl = (int)(item / cf.ntiles);
-    float2* dst = buf ? in1 : in0;
-    mbar_arrive_expect_tx(&bar_in[buf], in_bytes);
-    for (int b = 0; b < cf.nboxes; ++b)
-      tma_g2s_3d(dst + (int64_t)b * a.K * cf.box_rows * a.TC, &tin, (int)(2 * tile * a.TC), b * cf.box_rows,
-                 cl * a.K, &bar_in[buf]);
-  };
-  auto issue_chunk = [&](int64_t s) {  // s: this CTA's running chunk number
-    const int64_t j = s / a.NCH;
-    const int ch = (int)(s - j * a.NCH);
-    const int64_t item = first + j * G;
-    if (item >= cf.nitems) return;
-    const int64_t tile = item % cf.ntiles;
-    const int r = (int)(s % kLamRing);
-    const unsigned char* src = reinterpret_cast<const unsigned char*>(a.lam) + (tile * a.NCH + ch) * (int64_t)cf.chunk_bytes;
-    mbar_arrive_expect_tx(&bar_lam[r], (uint32_t)cf.chunk_bytes);
-    bulk_g2s(ring + (int64_t)r * cf.chunk_bytes, src, (uint32_t)cf.chunk_bytes, &bar_lam[r]);
-  };
-
-  if (leader) {
-    if (first < cf.nitems) issue_input(first, 0);
-    for (int s = 0; s < kLamRing; ++s) issue_chunk(s);
-  }
-  int failed = 0;
-  for (int64_t j = 0; first + j * G < cf.nitems; ++j) {
-    const int64_t item = first + j * G;
-    const int64_t tile = item % cf.ntiles;
-    const int cl = (int)(item / cf.ntiles);
-    const int buf = (int)(j & 1);
-    if (leader && item + G < cf.nitems) {
-      fence_proxy_async_smem();
-      issue_input(item + G, buf ^ 1);
-    }
-    const bool ok_in = mbar_wait(&bar_in[buf], (uint32_t)((j >> 1) & 1));
-    if (__syncthreads_or(!ok_in)) { failed = 1; break; }
-    const float2* ib = buf ? in1 : in0;
-    float2* base = a.stack + (int64_t)cl * a.K * plane + tile * a.TC;
-    step_a<SP, -1>(sm, sl, a.K, tw, nload, [&](int k, int li, int n) -> float2 {
-      if (n >= a.nin) return make_float2(0.f, 0.f);
-      const int b = n / cf.box_rows, rr = n - b * cf.box_rows;
-      return ib[(((int64_t)b * a.K + k) * cf.box_rows + rr) * a.TC + li];
-    });
-    __syncthreads();
-    step_b<SP, -1>(sm, sl, a.K, R2, [&](int lo, int li, int f1, int f2, float2 v) { sm[sl.at(lo, f1, f2, li, R1)] = v; });
-    __syncthreads();
-    for (int ch = 0; ch < a.NCH; ++ch) {
-      const int64_t s = j * a.NCH + ch;
-      const int r = (int)(s % kLamRing);
-      const bool ok = mbar_wait(&bar_lam[r], (uint32_t)((s / kLamRing) & 1));
-      if (__syncthreads_or(!ok)) { failed = 1; break; }
-      const unsigned char* lc = ring + (int64_t)r * cf.chunk_bytes;
-      for (int t = threadIdx.x; t < a.FC * a.TC; t += blockDim.x) {
-        const int li = t & (a.TC - 1);
-        const int fc = t >> sl.tcs;
-        const int f = ch * a.FC + fc;
-        const int f1 = f % R1, f2 = f / R1;
-        float2 X[KMAX], Y[KMAX];
-#pragma unroll
-        for (int k = 0; k < KMAX; ++k) X[k] = (k < a.K) ? sm[sl.at(k, f1, f2, li, R1)] : make_float2(0.f, 0.f);
-        lam_apply_ptr<KMAX>(a.lam_mode, a.K, lc, (int64_t)fc * a.TC + li, (int64_t)a.FC * a.TC, X, Y);
-#pragma unroll
-        for (int k = 0; k < KMAX; ++k)
-          if (k < a.K) sm[sl.at(k, f1, f2, li, R1)] = Y[k];
-      }
-      __syncthreads();
-      if (leader) {
-        fence_proxy_async_smem();
-        issue_chunk(s + kLamRing);
-      }
-    }
-    if (failed) break;
-    inv_step_a_slots<SP>(sm, sl, a.K, tw);
-    __syncthreads();
-    inv_step_b_slots<SP>(sm, sl, a.K, nkeep, [&](int k, int li, int n, float2 v) {
-      if (n < a.nout) base[k * plane + (int64_t)n * a.inner + li] = v;
-    });
-    __syncthreads();
-  }
-  if (failed) {
-    if (leader) atomicExch(cf.err, KERR_MBAR_TIMEOUT);
-    // give copies still in flight a bounded chance to land before the CTA exits
-    for (int b = 0; b < 2; ++b) (void)mbar_try_wait(&bar_in[b], 0);
-    __syncthreads();
-  }
-}
-
 // -------------------------------------------------------- dispatch ---
 
 template <class F>
@@ -423,14 +288,7 @@ static int round_threads(int tasks) {
 // threads of a row-pass CTA: its step-B tasks, capped at 256 (a thread then runs
 // several tasks) so that two CTAs fit next to the register-heavy DFTs.  Measured
 // on 256^2, 20 coils: rows inverse 0.079 -> 0.063 ms (320 -> 256 threads).
-static int row_threads(int tasks) {
-  static const int cap = [] {
-    const char* v = std::getenv("MRSR_ROW_THREADS");
-    const int c = v ? std::atoi(v) : 0;
-    return c >= 64 ? c : 256;
-  }();
-  return std::min(round_threads(tasks), cap);
-}
+static int row_threads(int tasks) { return std::min(round_threads(tasks), 256); }
 
 int fast_rows_fwd(const RowsFwdArgs& a, int64_t nrows, int ncg, cudaStream_t st) {
   return with_split(a.pl.L, [&](auto sp) -> int {
@@ -456,62 +314,10 @@ int fast_rows_inv(const RowsInvArgs& a, int64_t nrows, cudaStream_t st) {
   });
 }
 
-static int num_sms() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
-
-static uint32_t align128(uint32_t x) { return (x + 127u) & ~127u; }
-
 int fast_lambda(const LamPassArgs& a, int ncg, int planes_total, int* errword, cudaStream_t st) {
   return with_split(a.pl.L, [&](auto sp) -> int {
     using SP = decltype(sp);
     const Slots sl = make_slots(SP::R2, a.TC);
-    const int esz = a.lam_mode == LAM_PACKED_REAL ? 4 : 8;
-    // TMA pipeline: needs >= 16-byte column boxes and everything in shared memory
-    Lam5Cfg cf{};
-    cf.nboxes = (a.nin + 255) / 256;
-    cf.box_rows = (a.nin + cf.nboxes - 1) / cf.nboxes;
-    cf.in_elems = a.K * cf.nboxes * cf.box_rows * a.TC;
-    cf.chunk_bytes = a.P * a.FC * a.TC * esz;
-    cf.ntiles = a.inner / a.TC;
-    cf.nitems = cf.ntiles * ncg;
-    cf.err = errword;
-    uint32_t off = 128;  // mbarriers
-    cf.off_tw = off;
-    off = align128(off + SP::L * 8);
-    cf.off_in0 = off;
-    off = align128(off + cf.in_elems * 8);
-    cf.off_in1 = off;
-    off = align128(off + cf.in_elems * 8);
-    cf.off_ring = off;
-    off = align128(off + kLamRing * cf.chunk_bytes);
-    cf.off_slots = off;
-    off += (uint32_t)(a.K * SP::R1 * sl.W * 8);
-    const bool box_aligned = ((int64_t)a.K * cf.box_rows * a.TC * 8) % 128 == 0 || cf.nboxes == 1;
-    const bool tma_ok = a.TC >= 2 && off <= 227u * 1024u && cf.chunk_bytes % 16 == 0 && box_aligned &&
-                        !lam_is_diag(a.lam_mode) &&
-                        std::getenv("MRSR_TMA_LAMBDA") != nullptr;
-    if (tma_ok) {
-      CUtensorMap tm;
-      const uint64_t dims[3] = {(uint64_t)(2 * a.inner), (uint64_t)a.nrow, (uint64_t)planes_total};
-      const uint64_t strides[2] = {(uint64_t)(2 * a.inner * 4), (uint64_t)(2 * a.inner * 4) * (uint64_t)a.nrow};
-      const uint32_t box[3] = {(uint32_t)(2 * a.TC), (uint32_t)cf.box_rows, (uint32_t)a.K};
-      MRSR_TRY(encode_tmap_f32_3d(&tm, a.stack, dims, strides, box));
-      auto k = k5_lambda<SP>;
-      MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)off));
-      MRSR_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
-      const int64_t grid = std::min<int64_t>(cf.nitems, num_sms());
-      k<<<(unsigned)grid, 512, off, st>>>(a, sl, cf, tm);
-      MRSR_LAUNCH_CHECK();
-      return MRSR_OK;
-    }
     const size_t smem = sizeof(float2) * ((size_t)SP::L + (size_t)a.K * SP::R1 * sl.W);
     LamPassArgs b = a;
     b.ncg = ncg;

@@ -1,10 +1,9 @@
-// Row passes of the precision MRSR_PREC_FP16_TC operator with the 64-point DFTs on
-// the tensor cores (the Λ pass is in apply_tc.cu; the four-step split and the operand
-// conventions are the same).  One work item is one image row r and one basis index k;
-// the MMA's N vectors are (coil, f1) for every coil of the group.
+// Inverse row pass of the precision MRSR_PREC_FP16_TC operator with the 64-point DFTs
+// on the tensor cores (the Λ pass is in apply_tc.cu; the four-step split and the
+// operand conventions are the same).  One work item is one image row r and one basis
+// index k; the MMA's N vectors are (coil, f1) for every coil of the group.  (The
+// forward row pass stays the float32 four-step kernel, which is faster there.)
 //
-// Forward (coil multiply, zero-pad to L = 512, DFT along dim 1):
-//   v[n] = x[n, r, k] S_c[n, r] (n < 256),  X[f1 + 8 f2] = sum_n2 w64^(n2 f2) w512^(n2 f1) sum_{n1<4} v[64 n1 + n2] w8^(n1 f1)
 // Inverse (DFT^-1 along dim 1, crop to 256, conj map, coil sum, alpha / beta):
 //   y[64 m1 + m2] = sum_c conj(S_c) sum_f1 w8^(-m1 f1) w512^(-m2 f1) conj(sum_f2 w64^(m2 f2) conj(Y_c[f1 + 8 f2]))
 // Operand B rows are (coil, f1); the core matrices along K sit 144 bytes apart, so the
@@ -34,8 +33,7 @@ __device__ __forceinline__ uint32_t roff(int r, int kk) {
 }
 
 struct TcRowsArgs {
-  RowsFwdArgs f;     // forward pass (unused by the inverse)
-  RowsInvArgs i;     // inverse pass (unused by the forward)
+  RowsInvArgs i;     // inverse pass arguments
   int ncg;           // coils of the group
   int cb;            // coils per MMA: ncg rounded up to a multiple of 4 (<= 32)
   int64_t nitems;    // rows x K
@@ -80,132 +78,6 @@ __device__ __forceinline__ void finish(bool ok, int tid, int warp, uint64_t* mba
   }
 }
 
-// ------------------------------------------------------------ forward ---
-template <int CB>
-__global__ void __launch_bounds__(kRThreads, 2) kt_rows_fwd(TcRowsArgs t) {
-  const RowsFwdArgs& a = t.f;
-  extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* sA = smem;
-  unsigned char* sB = smem + kAbytes;
-  float2* tw = reinterpret_cast<float2*>(sB + (size_t)CB * kRSbo);
-  __shared__ uint64_t mbar;
-  __shared__ uint32_t tmem_base;
-  __shared__ float red[kRThreads / 32];
-  __shared__ int abort_flag;
-  constexpr int N = 8 * CB, NP = CB / 4;  // F1 passes: 4 coils x 64 n2 per pass
-  constexpr uint32_t idesc = umma::idesc_f16(128, N);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  load_constants(sA, tw, t.consts, tid, kRThreads);
-  if (warp == 0) umma::tmem_alloc(&tmem_base, kRTmemCols);
-  if (tid == 0) {
-    umma::mbar_init(&mbar, 1);
-    abort_flag = 0;
-  }
-  umma::fence_proxy_async();
-  umma::fence_before_sync();
-  __syncthreads();
-  umma::fence_after_sync();
-  const uint32_t tmem = tmem_base, aaddr = umma::smem_u32(sA), baddr = umma::smem_u32(sB);
-  uint32_t phase = 0;
-  // F1: n2 fixed per thread, so are its seven w512 twiddles
-  const int n2 = tid & 63, cq = tid >> 6;
-  float2 twr[8];
-#pragma unroll
-  for (int f1 = 0; f1 < 8; ++f1) twr[f1] = tw[n2 * f1];
-  // epilogue: TMEM lane m = 2 f2 + part, coil half h
-  const int q = warp & 3, h = warp >> 2;
-  const int m = 32 * q + lane, f2 = m >> 1, part = m & 1;
-  const uint32_t tl = tmem + ((uint32_t)(32 * q) << 16);
-  const int L = kL;
-  constexpr float r2 = 0.70710678118654752f;
-
-  // this thread's inputs of an item: x[64 n1 + n2, r, k] (shared by every coil) and the
-  // maps of its coils 4 p + cq at the same samples; loaded one item ahead
-  float2 xv[4], sv[NP][4];
-  auto load_inputs = [&](int64_t it) {
-    const int64_t rr = it / a.K;
-    const int kk = (int)(it - rr * a.K);
-#pragma unroll
-    for (int n1 = 0; n1 < 4; ++n1) xv[n1] = a.x[64 * n1 + n2 + (int64_t)a.n1 * (rr + a.nrows * kk)];
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      const int cl = 4 * p + cq;
-#pragma unroll
-      for (int n1 = 0; n1 < 4; ++n1)
-        sv[p][n1] = (a.cmaps && cl < t.ncg) ? a.cmaps[64 * n1 + n2 + (int64_t)a.n1 * (rr + a.nrows * (a.c0 + cl))]
-                                            : make_float2(1.f, 0.f);
-    }
-  };
-  if ((int64_t)blockIdx.x < t.nitems) load_inputs(blockIdx.x);
-
-  bool ok = true;
-  for (int64_t item = blockIdx.x; item < t.nitems && ok; item += gridDim.x) {
-    const int64_t r = item / a.K;
-    const int k = (int)(item - r * a.K);
-    // ---- F1: v = x S_c, pruned DFT-8 over n1, twiddle, into operand B
-    float2 v[NP][4];
-    float mx = 0.f;
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      const int cl = 4 * p + cq;
-#pragma unroll
-      for (int n1 = 0; n1 < 4; ++n1) {
-        const float2 val = cl < t.ncg ? cmul(sv[p][n1], xv[n1]) : make_float2(0.f, 0.f);
-        v[p][n1] = val;
-        mx = fmaxf(mx, fmaxf(fabsf(val.x), fabsf(val.y)));
-      }
-    }
-    const int e1 = scale_exp(4.f * block_max<kRThreads>(mx, red));
-    const float s1 = ldexpf(1.f, e1);
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      const int cl = 4 * p + cq;
-      float2 ev[4], od[4];
-      dft4<-1>(v[p][0], v[p][1], v[p][2], v[p][3], ev);
-      const float2 x1 = make_float2(r2 * (v[p][1].x + v[p][1].y), r2 * (v[p][1].y - v[p][1].x));
-      const float2 x2 = mul_mi(v[p][2]);
-      const float2 x3 = make_float2(r2 * (v[p][3].y - v[p][3].x), -r2 * (v[p][3].x + v[p][3].y));
-      dft4<-1>(v[p][0], x1, x2, x3, od);
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float2 a0 = cmulf(ev[j], twr[2 * j]), a1 = cmulf(od[j], twr[2 * j + 1]);
-        st_half2(sB, roff(cl * 8 + 2 * j, 2 * n2), a0.x * s1, a0.y * s1);
-        st_half2(sB, roff(cl * 8 + 2 * j + 1, 2 * n2), a1.x * s1, a1.y * s1);
-      }
-    }
-    umma::fence_proxy_async();
-    umma::fence_before_sync();
-    __syncthreads();
-    issue_dft64(tid, tmem, aaddr, baddr, idesc, &mbar);
-    if (item + gridDim.x < t.nitems) load_inputs(item + gridDim.x);  // under the MMA and epilogue
-    if (!(ok = wait_dft64(warp, lane, &mbar, phase, &abort_flag))) break;
-    // ---- epilogue: the lane pair holds re / im of row f2 for f1 = 0..7; the even lane
-    // keeps f1 < 4, the odd lane f1 >= 4, so each writes 4 consecutive frequencies
-    const float is1 = ldexpf(1.f, -e1);
-    for (int cl = h * (CB / 2); cl < (h + 1) * (CB / 2); ++cl) {
-      float d[8];
-      tmem_ld8(tl + (uint32_t)(cl * 8), d);
-      float2 o[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const float keep = part ? d[4 + i] : d[i];
-        const float send = part ? d[i] : d[4 + i];
-        const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
-        o[i] = part ? make_float2(recv * is1, keep * is1) : make_float2(keep * is1, recv * is1);
-      }
-      if (cl < t.ncg) {
-        float4* dst = reinterpret_cast<float4*>(a.out + (((int64_t)cl * a.K + k) * a.nrows + r) * L + 8 * f2 + 4 * part);
-        dst[0] = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
-        dst[1] = make_float4(o[2].x, o[2].y, o[3].x, o[3].y);
-      }
-    }
-    umma::fence_before_sync();
-    __syncthreads();
-  }
-  finish(ok, tid, warp, &mbar, phase, tmem, t.err);
-}
-
-// ------------------------------------------------------------ inverse ---
 template <int CB>
 __global__ void __launch_bounds__(kRThreads, 2) kt_rows_inv(TcRowsArgs t) {
   const RowsInvArgs& a = t.i;
@@ -383,44 +255,27 @@ int launch_rows(void (*kern)(TcRowsArgs), const TcRowsArgs& t, size_t extra, cud
   return MRSR_OK;
 }
 
-template <bool FWD, int CB>
+template <int CB>
 int dispatch_cb(const TcRowsArgs& t, cudaStream_t st) {
-  if constexpr (FWD)
-    return launch_rows<CB>(kt_rows_fwd<CB>, t, 0, st);
-  else
-    return launch_rows<CB>(kt_rows_inv<CB>, t, sizeof(float2) * 4 * 128, st);
+  return launch_rows<CB>(kt_rows_inv<CB>, t, sizeof(float2) * 4 * 128, st);
 }
 
-template <bool FWD>
 int dispatch(const TcRowsArgs& t, cudaStream_t st) {
   switch (t.cb) {
-    case 4: return dispatch_cb<FWD, 4>(t, st);
-    case 8: return dispatch_cb<FWD, 8>(t, st);
-    case 12: return dispatch_cb<FWD, 12>(t, st);
-    case 16: return dispatch_cb<FWD, 16>(t, st);
-    case 20: return dispatch_cb<FWD, 20>(t, st);
-    case 24: return dispatch_cb<FWD, 24>(t, st);
-    case 28: return dispatch_cb<FWD, 28>(t, st);
-    default: return dispatch_cb<FWD, 32>(t, st);
+    case 4: return dispatch_cb<4>(t, st);
+    case 8: return dispatch_cb<8>(t, st);
+    case 12: return dispatch_cb<12>(t, st);
+    case 16: return dispatch_cb<16>(t, st);
+    case 20: return dispatch_cb<20>(t, st);
+    case 24: return dispatch_cb<24>(t, st);
+    case 28: return dispatch_cb<28>(t, st);
+    default: return dispatch_cb<32>(t, st);
   }
 }
 
 }  // namespace
 
 bool tc_rows_supported(int L, int n1, int ncg) { return L == kL && 2 * n1 == L && ncg >= 1 && ncg <= kRMaxCoils; }
-
-int tc_rows_fwd(const RowsFwdArgs& a, int ncg, const void* consts, int* errword, cudaStream_t st) {
-  MRSR_REQUIRE(tc_rows_supported(a.pl.L, a.n1, ncg), MRSR_ERR_UNSUPPORTED,
-               "tensor-core row pass: needs 512-point rows of 256 image samples and <= %d coils per group", kRMaxCoils);
-  TcRowsArgs t{};
-  t.f = a;
-  t.ncg = ncg;
-  t.cb = (ncg + 3) / 4 * 4;
-  t.nitems = a.nrows * a.K;
-  t.err = errword;
-  t.consts = reinterpret_cast<const unsigned char*>(consts);
-  return dispatch<true>(t, st);
-}
 
 int tc_rows_inv(const RowsInvArgs& a, const void* consts, int* errword, cudaStream_t st) {
   MRSR_REQUIRE(tc_rows_supported(a.pl.L, a.n1, a.ncg), MRSR_ERR_UNSUPPORTED,
@@ -432,7 +287,7 @@ int tc_rows_inv(const RowsInvArgs& a, const void* consts, int* errword, cudaStre
   t.nitems = a.nrows * a.K;
   t.err = errword;
   t.consts = reinterpret_cast<const unsigned char*>(consts);
-  return dispatch<false>(t, st);
+  return dispatch(t, st);
 }
 
 }  // namespace mrsr

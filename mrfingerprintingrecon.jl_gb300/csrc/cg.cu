@@ -260,15 +260,6 @@ static int cg_capture(mrsr_normalop* op, CgWork& w, int iters, cudaGraphExec_t* 
   return s;
 }
 
-// MRSR_CG_GRAPH=0 launches every kernel of every iteration from the host instead
-static bool cg_graphs_enabled() {
-  static const bool on = [] {
-    const char* e = std::getenv("MRSR_CG_GRAPH");
-    return !(e && e[0] == '0');
-  }();
-  return on;
-}
-
 int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter, double reltol, double abstol,
            cudaStream_t st, int* iters, double* res, int nseg) {
   const int64_t n = op->geo.nimg() * op->geo.K;
@@ -286,9 +277,8 @@ int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter
   // so converged solves do not keep paying for applies.  Without a tolerance only an
   // exact zero residual ends a solve early, and the device's done flag already turns the
   // iterations after it into no-ops.
-  const bool graphs = cg_graphs_enabled();
-  if (graphs && maxiter >= 8 && !w.it8) MRSR_TRY(cg_capture(op, w, 8, &w.it8));
-  if (graphs && maxiter % 8 != 0 && !w.it1) MRSR_TRY(cg_capture(op, w, 1, &w.it1));
+  if (maxiter >= 8 && !w.it8) MRSR_TRY(cg_capture(op, w, 8, &w.it8));
+  if (maxiter % 8 != 0 && !w.it1) MRSR_TRY(cg_capture(op, w, 1, &w.it1));
   std::vector<CgState> h((size_t)nseg);
   auto all_done = [&]() {
     for (const CgState& v : h)
@@ -299,15 +289,10 @@ int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter
   int done_its = 0;
   while (done_its < maxiter) {
     const int nit = std::min(8, maxiter - done_its);
-    if (graphs && nit == 8) {
+    if (nit == 8) {
       MRSR_CHECK_CUDA(cudaGraphLaunch(w.it8, st));
     } else {
-      for (int k = 0; k < nit; ++k) {
-        if (graphs)
-          MRSR_CHECK_CUDA(cudaGraphLaunch(w.it1, st));
-        else
-          MRSR_TRY(cg_iter_enqueue(op, w, st));
-      }
+      for (int k = 0; k < nit; ++k) MRSR_CHECK_CUDA(cudaGraphLaunch(w.it1, st));
     }
     done_its += nit;
     if (check && done_its < maxiter) {
@@ -510,8 +495,8 @@ extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const
 // ---------------------------------------------------------------------------
 // CG without device allocation.
 //
-// mrsr_cg allocates its three work vectors with cudaMalloc on the first solve
-// of an operator.  Some callers cannot allow that: a host framework that
+// mrsr_cg allocates its three work vectors from the device's stream-ordered
+// pool (cudaMallocAsync) on the first solve of an operator.  Some callers cannot allow that: a host framework that
 // reserves device memory up front through its own pool (Julia's CUDA.jl, a
 // serving process with a fixed memory budget) or a latency-critical loop that
 // forbids allocation after start-up.  mrsr_cg_noalloc runs the same kernels
@@ -579,6 +564,10 @@ extern "C" int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int 
   const unsigned nb = vec_blocks(n);
   k_cg_init<<<nb, kCgThreads, 0, st>>>(bb, xx, r, u, n, reltol, abstol, maxiter, s, part);
   MRSR_LAUNCH_CHECK();
+  // as in cg_run: without a tolerance only an exact zero residual ends a solve early, and
+  // the device's done flag already turns the iterations after it into no-ops, so the host
+  // reads the state back between blocks of 8 iterations only when a tolerance is set
+  const bool check = reltol > 0.0 || abstol > 0.0;
   const int chunk = 8;
   CgState h;
   for (int it0 = 0; it0 < maxiter; it0 += chunk) {
@@ -592,7 +581,7 @@ extern "C" int mrsr_cg_noalloc(mrsr_normalop* op, const float* b, float* x, int 
       k_cg_update<<<nb, kCgThreads, 0, st>>>(xx, r, u, c, n, s, part);
       MRSR_LAUNCH_CHECK();
     }
-    if (it0 + nit < maxiter) {
+    if (check && it0 + nit < maxiter) {
       MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
       MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
       if (h.done) break;

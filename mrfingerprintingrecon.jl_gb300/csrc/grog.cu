@@ -586,15 +586,8 @@ static int grog_sms() {
   return n;
 }
 
-// Threads of the per-spoke logarithm CTA (a multiple of 32, 32..1024; env MRSR_GROG_THREADS).
-static unsigned grog_log_threads() {
-  static const unsigned t = [] {
-    const char* e = std::getenv("MRSR_GROG_THREADS");
-    const int v = e ? std::atoi(e) : 256;
-    return (unsigned)std::min(1024, std::max(32, v / 32 * 32));
-  }();
-  return t;
-}
+// Threads of the per-spoke logarithm CTA.
+constexpr unsigned kGrogLogThreads = 256;
 
 static void gauss_legendre01(int n, std::vector<double>& t, std::vector<double>& w) {
   t.assign(n, 0.0);
@@ -656,7 +649,7 @@ extern "C" int mrsr_grog_calib(int ndims, int64_t nr, int64_t ns_per_frame, int6
   // opt in whatever the size: the dynamic part plus the kernel's static pivot records can pass 48 KB
   MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_grog_solve_log, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l));
   LogArgs la{AB.as<double2>(), ncoils, vth.as<double2>(), glt.as<double>(), glw.as<double>(), err.as<int>()};
-  k_grog_solve_log<<<(unsigned)nspk, grog_log_threads(), smem_l, st>>>(la);
+  k_grog_solve_log<<<(unsigned)nspk, kGrogLogThreads, smem_l, st>>>(la);
   MRSR_LAUNCH_CHECK();
   NmArgs na{trj, ndims, (int)nr, spf, ns_per_frame, nt, nspk0, nm.as<double>(), Pinv.as<double>(), nrep};
   k_grog_nm<<<1, 1024, 0, st>>>(na);

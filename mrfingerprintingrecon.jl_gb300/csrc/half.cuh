@@ -1,4 +1,4 @@
-// Shared pieces of the fp16-storage operators (apply_half.cu, apply_pair.cu):
+// Shared pieces of the fp16-storage operator (apply_half.cu):
 // tile geometry of the per-tile scale arrays and launch helpers.
 #pragma once
 #include <algorithm>

@@ -428,13 +428,6 @@ struct RowTiling {
   size_t smem;
 };
 
-static int64_t env_int(const char* name, int64_t dflt);
-
-// line elements per CTA of the four-step row passes (one exchange buffer)
-static int64_t fast_row_elems() {
-  static const int64_t v = env_int("MRSR_ROW_ELEMS", 4096);
-  return v;
-}
 
 // R1 of the register four-step split of L (apply_fast.cu's table), 0 if none
 static int fast_r1(int L) {
@@ -475,9 +468,9 @@ static int balanced_rpc(int L, int lines, int64_t elems) {
 static RowTiling rows_tiling(int L, int lines_per_row, int64_t nrows, bool balance = false) {
   RowTiling t;
   t.lstride = L;
-  const int64_t elems = fast_length(L) ? fast_row_elems() : kRowElems;
+  const int64_t elems = kRowElems;
   int rpc = (int)std::max<int64_t>(1, elems / ((int64_t)lines_per_row * L));
-  if (balance && fast_length(L) && !std::getenv("MRSR_ROW_ELEMS")) rpc = balanced_rpc(L, lines_per_row, elems);
+  if (balance && fast_length(L)) rpc = balanced_rpc(L, lines_per_row, elems);
   rpc = (int)std::min<int64_t>(rpc, nrows);
   t.rpc = rpc;
   t.threads = 256;
@@ -493,29 +486,9 @@ static int mid_tc(const mrsr_normalop* op) {
 
 static void record_cb(void* ctx) { static_cast<Recorder*>(ctx)->record(); }
 
-static bool tc_rows_enabled() {
-  static const bool on = [] {
-    const char* e = std::getenv("MRSR_TC_ROWS");
-    return !(e && e[0] == '0');
-  }();
-  return on;
-}
-
-// The forward row pass of the fp16-tc operator stays float32 unless MRSR_TC_ROWS_FWD=1:
-// on 256^2 with 20 coils the float32 four-step kernel (rows per CTA chosen to fill its
-// threads) takes 0.039 ms against the tensor-core kernel's 0.042, and adds no fp16 rounding.
-static bool tc_rows_fwd_enabled() {
-  static const bool on = [] {
-    const char* e = std::getenv("MRSR_TC_ROWS_FWD");
-    return e && e[0] == '1';
-  }();
-  return on;
-}
-
 static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
                       Recorder rec) {
-  if (op->precision == MRSR_PREC_FP16 || op->precision == MRSR_PREC_FP16_ARITH) {
-    if (pair_supported(op)) return apply_pair_impl(op, x, y, alpha, beta, st, rec.ev ? record_cb : nullptr, &rec);
+  if (op->precision == MRSR_PREC_FP16) {
     return apply_half_impl(op, x, y, alpha, beta, st, rec.ev ? record_cb : nullptr, &rec);
   }
   const OpGeom& g = op->geo;
@@ -531,10 +504,10 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
   for (int grp = 0; grp < ngroups; ++grp) {
     const int c0 = grp * op->Cg;
     const int ncg = std::min(op->Cg, g.ncoils - c0);
-    // fp16-tc: the inverse row pass on the tensor cores too (MRSR_TC_ROWS=0 keeps it in float32)
-    const bool tc_rows = op->precision == MRSR_PREC_FP16_TC && tc_rows_enabled() &&
-                         tc_rows_supported(L1, (int)g.n[0], ncg);
-    const bool tc_rows_f = tc_rows && tc_rows_fwd_enabled();
+    // fp16-tc: the inverse row pass runs on the tensor cores too.  The forward row pass stays
+    // the float32 four-step kernel: on 256^2 with 20 coils it takes 0.039 ms against 0.042 ms
+    // for a tensor-core form, and adds no fp16 rounding.
+    const bool tc_rows = op->precision == MRSR_PREC_FP16_TC && tc_rows_supported(L1, (int)g.n[0], ncg);
     // a stacked operator's planes are independent: without coil maps the rows pass sees
     // them as more rows of one plane, and the Λ pass as more coils, so small images still
     // fill the GPU (the stack layout [coil][plane][row][...] is the same either way)
@@ -547,9 +520,7 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       RowTiling t = rows_tiling(L1, Kr, nr, true);
       RowsFwdArgs a{op->plan[0].plan, (int)g.n[0], nr, t.rpc, Kr, c0, t.lstride, x, cm, st1};
       dim3 grid((unsigned)cdiv(nr, t.rpc), ncg);
-      if (tc_rows_f)
-        MRSR_TRY(tc_rows_fwd(a, ncg, op->tc_consts.p, op->errflag.as<int>(), st));
-      else if (fast_length(L1))
+      if (fast_length(L1))
         MRSR_TRY(fast_rows_fwd(a, nr, ncg, st));
       else
         MRSR_TRY(launch_fft_kernel<RowsFwdArgs>(k_rows_fwd, grid, t.threads, t.smem, st, a));
@@ -636,19 +607,14 @@ int normalop_apply_internal(mrsr_normalop* op, const float2* x, float2* y, float
 
 // ---------------------------------------------------------- builders ---
 
-static int64_t env_int(const char* name, int64_t dflt) {
-  const char* v = std::getenv(name);
-  if (!v || !*v) return dflt;
-  return std::atoll(v);
-}
-
 int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_shape, int K, int ncoils,
                      int precision, int kmax) {
   MRSR_REQUIRE(ndims == 2 || ndims == 3, MRSR_ERR_ARG, "ndims must be 2 or 3 (got %d)", ndims);
   MRSR_REQUIRE(img_shape != nullptr, MRSR_ERR_ARG, "img_shape is NULL");
   MRSR_REQUIRE(K >= 1 && K <= kmax, MRSR_ERR_UNSUPPORTED, "rank K=%d outside 1..%d", K, kmax);
   MRSR_REQUIRE(ncoils >= 1, MRSR_ERR_ARG, "ncoils must be >= 1");
-  MRSR_REQUIRE(precision >= MRSR_PREC_FP32 && precision <= MRSR_PREC_FP16_TC, MRSR_ERR_ARG, "unknown precision %d",
+  MRSR_REQUIRE(precision == MRSR_PREC_FP32 || precision == MRSR_PREC_FP16 || precision == MRSR_PREC_FP16_TC, MRSR_ERR_ARG,
+               "unknown precision %d",
                precision);
   op->kind = kind;
   op->precision = precision;
@@ -670,7 +636,7 @@ int op_init_geometry(mrsr_normalop* op, int kind, int ndims, const int64_t* img_
   }
   // Λ-pass tile width: up to 8 columns, a divisor of the plane width, <= 16384 elements per CTA
   // generic kernels: two K*TC*L buffers; four-step kernels: one K*TC*L exchange buffer (<= ~110 KB, 2 CTAs/SM)
-  int TC = (int)env_int("MRSR_LAMBDA_TC", 8);
+  int TC = 8;
   const int64_t budget = fast_length((int)g.glast()) ? 13000 : 12288;
   while (TC > 1 && ((int64_t)K * TC * g.glast() > budget || g.inner() % TC != 0)) TC >>= 1;
   op->TC = TC;
@@ -698,7 +664,7 @@ int op_set_cmaps(mrsr_normalop* op, const float* cmaps, cudaStream_t st) {
 
 int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   const OpGeom& g = op->geo;
-  const bool half = op->precision == MRSR_PREC_FP16 || op->precision == MRSR_PREC_FP16_ARITH;
+  const bool half = op->precision == MRSR_PREC_FP16;
   MRSR_REQUIRE(!half || half_supported(op), MRSR_ERR_UNSUPPORTED,
                "fp16 storage needs grid lengths with a register four-step split (64, 128, 256, 384, 512, 768, 1024)");
   const int64_t esz = half ? 4 : (int64_t)sizeof(float2);
@@ -706,16 +672,14 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   // between the three passes (measured on 256^2, K=5, Nc=20: one group of 20 coils is 5%
   // faster than groups of 7 or 10)
   const int64_t per_coil = (int64_t)g.K * g.g[0] * g.n[1] * g.n[2] * esz;
-  int64_t cg = env_int("MRSR_COIL_GROUP", 0);
-  if (cg <= 0) {
-    if (g.ndims == 2) {
-      cg = std::max<int64_t>(1, (112ll << 20) / std::max<int64_t>(per_coil, 1));
-    } else {
-      // 3D stacks are far larger than L2; group as many coils as a 12 GB stack budget
-      // allows, so one Λ pass streams the kernel once for all of them
-      const int64_t per_coil3 = per_coil + (int64_t)g.K * g.g[0] * g.g[1] * g.n[2] * esz;
-      cg = std::max<int64_t>(1, (env_int("MRSR_STACK_BUDGET_MB", 12288) << 20) / std::max<int64_t>(per_coil3, 1));
-    }
+  int64_t cg;
+  if (g.ndims == 2) {
+    cg = std::max<int64_t>(1, (112ll << 20) / std::max<int64_t>(per_coil, 1));
+  } else {
+    // 3D stacks are far larger than L2; group as many coils as a 12 GB stack budget
+    // allows, so one Λ pass streams the kernel once for all of them
+    const int64_t per_coil3 = per_coil + (int64_t)g.K * g.g[0] * g.g[1] * g.n[2] * esz;
+    cg = std::max<int64_t>(1, (12288ll << 20) / std::max<int64_t>(per_coil3, 1));
   }
   // rows inverse holds one row of every coil of the group in shared memory (<= ~200 KB)
   cg = std::min<int64_t>(cg, std::max<int64_t>(1, (200ll << 10) / (9 * g.g[0])));
@@ -731,10 +695,7 @@ int op_finalize(mrsr_normalop* op, cudaStream_t st) {
   op->launches = (int)ngroups * (g.ndims == 2 ? 3 : 5);
   if (half) {
     if (!op->lam_half.p) MRSR_TRY(half_lambda_convert(op, st));  // a shared kernel may already have it
-    if (pair_supported(op))
-      MRSR_TRY(pair_alloc(op, st));
-    else
-      MRSR_TRY(half_alloc_scales(op));
+    MRSR_TRY(half_alloc_scales(op));
   }
   if (op->precision == MRSR_PREC_FP16_TC && !op->lam_tc.p) {  // a shared kernel may already have them
     MRSR_TRY(op->tc_consts.alloc(tc_constants_bytes()));
@@ -1062,14 +1023,6 @@ extern "C" int mrsr_normalop_check(mrsr_normalop* op, mrsr_stream_t stream) {
   MRSR_CHECK_CUDA(cudaMemcpyAsync(&code, op->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
   return device_error_status(op, code, st);
-}
-
-extern "C" int mrsr_test_set_device_error(mrsr_normalop* op, int code, mrsr_stream_t stream) {
-  MRSR_REQUIRE(op, MRSR_ERR_ARG, "operator is NULL");
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  MRSR_CHECK_CUDA(cudaMemcpyAsync(op->errflag.p, &code, sizeof(int), cudaMemcpyHostToDevice, st));
-  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
-  return MRSR_OK;
 }
 
 extern "C" void mrsr_normalop_destroy(mrsr_normalop* op) { delete op; }

@@ -329,7 +329,6 @@ static int spread_cl_finish(float2* gcl, int nch, int nout, int64_t cells, float
 
 int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
-  if (tiles_applicable(a.S, a.S.d, a.U) && a.K <= 8) return spread_lambda_tiled(a, st);
   if (a.np >= 160 && a.np <= 64 * kClPairs) {  // see spread_data
     const int nchp = a.np + (a.np & 1);
     DevBuf gcl;
@@ -346,7 +345,6 @@ int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
 
 int spread_data(const SpreadDataArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
-  if (tiles_applicable(a.S, a.S.d, a.U)) return spread_data_tiled(a, st);
   // channel-last pays off for many channels (GB300, 2D radial: 100 channels 8.6 ms vs
   // 5.7 ms for the scattered kernel, 192 channels 20.5 ms vs 31 ms)
   const int nch = a.nc * a.K;

@@ -93,10 +93,4 @@ struct SpreadDataArgs {
 };
 int spread_data(const SpreadDataArgs& a, cudaStream_t st);
 
-// Tile-sorted shared-memory spreading of 2D grids (spread_tiles.cu); used by
-// spread_data / spread_lambda when tiles_applicable().
-bool tiles_applicable(const SampleSet& S, int d, const void* U);
-int spread_data_tiled(const SpreadDataArgs& a, cudaStream_t st);
-int spread_lambda_tiled(const SpreadLambdaArgs& a, cudaStream_t st);
-
 }  // namespace mrsr

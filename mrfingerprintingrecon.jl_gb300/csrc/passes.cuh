@@ -174,7 +174,6 @@ int tc_build_constants(void* out, cudaStream_t st);  // DFT-64 operand + twiddle
 size_t tc_constants_bytes();
 int tc_lambda_bound(const void* lam, size_t bytes, float* out, cudaStream_t st);
 bool tc_rows_supported(int L, int n1, int ncg);
-int tc_rows_fwd(const RowsFwdArgs& a, int ncg, const void* consts, int* errword, cudaStream_t st);
 int tc_rows_inv(const RowsInvArgs& a, const void* consts, int* errword, cudaStream_t st);
 int tc_lambda_layout(const void* lam, void* out, int64_t inner, int P, int FC, int NCH, int TC, bool real,
                      cudaStream_t st);
@@ -184,11 +183,6 @@ bool half_supported(const mrsr_normalop* op);
 int half_lambda_convert(mrsr_normalop* op, cudaStream_t st);
 int half_alloc_scales(mrsr_normalop* op);
 int apply_half_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
-                    void (*record)(void*), void* rec_ctx);
-// fp16-arithmetic operator on line pairs (apply_pair.cu), 2D four-step grids with an even Λ tile width
-bool pair_supported(const mrsr_normalop* op);
-int pair_alloc(mrsr_normalop* op, cudaStream_t st);
-int apply_pair_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alpha, float2 beta, cudaStream_t st,
                     void (*record)(void*), void* rec_ctx);
 
 }  // namespace mrsr

@@ -16,8 +16,7 @@ import torch
 from . import _lib
 from .arrays import (is_complex_array, jl_empty, jl_reshape, mask_u8, ptr, stack_cmaps, stream_handle, to_jl)
 
-_PREC = {"fp32": _lib.PREC_FP32, "fp16": _lib.PREC_FP16, "fp16-arith": _lib.PREC_FP16_ARITH,
-         "fp16-tc": _lib.PREC_FP16_TC}
+_PREC = {"fp32": _lib.PREC_FP32, "fp16": _lib.PREC_FP16, "fp16-tc": _lib.PREC_FP16_TC}
 
 
 def _prec(precision):

@@ -148,37 +148,3 @@ def test_cg_refined_reaches_float32_residual(mr, cuda):
     print(f"cg_refined: outer {res.iters}, reported {res.resnorm:.2e}, float64 check {rel:.2e}")
     assert res.resnorm <= tol
     assert rel < 2 * tol
-
-
-@pytest.mark.parametrize("img,K,Nc,cplx", [
-    ((64, 64), 5, 4, False),
-    ((128, 128), 4, 3, True),
-    ((256, 64), 4, 2, False),
-    ((192, 192), 3, 2, True),
-    ((64, 64), 8, 2, True),
-])
-def test_half_arith_apply(mr, cuda, img, K, Nc, cplx):
-    """precision="fp16-arith": fp16 FFT butterflies and kernel product (half2 on column / line
-    pairs), float32 coil sums.  11-bit arithmetic through four 2^9-2^10-point transforms:
-    relative error ~1.5e-3; bound 4e-3."""
-    lam, cells, cm, x = _problem(15, img, K, Nc, complex_lam=cplx)
-    cml = [cm[..., c] for c in range(Nc)]
-    A = mr.NFFTNormalOp(img, lam, cells, cmaps=cml, precision="fp16-arith")
-    assert A.precision == 2
-    y = mr.to_host(A @ x)
-    ref = onormal.nfft_normalop_apply(x, onormal.unpack_lambda(lam.astype(np.complex128), K), cells, img, cmaps=cml)
-    err = rel_l2(y, ref)
-    print(f"fp16-arith apply {img} K={K}: rel L2 {err:.2e}")
-    assert err < 4e-3
-
-
-def test_half_arith_refined_reaches_float32_residual(mr, cuda):
-    N, K = 32, 4
-    Lam, km, cml, b = _radial_problem(N=N, K=K, Ncyc=8)
-    packed = onormal.pack_lambda(Lam).astype(np.complex64)
-    A16 = mr.NFFTNormalOp((N, N), packed, km, cmaps=cml, precision="fp16-arith")
-    A32 = mr.NFFTNormalOp((N, N), packed, km, cmaps=cml)
-    bt = A32 @ mr.to_jl(b, torch.complex64)
-    res = mr.cg_refined(A16, A32, bt, inner_iters=30, max_outer=20, tol=1e-4, log=True)
-    print(f"fp16-arith refined: outer {res.iters}, residual {res.resnorm:.2e}")
-    assert res.resnorm <= 1e-4

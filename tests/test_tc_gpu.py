@@ -2,8 +2,7 @@
 pass and of the inverse row pass is a tcgen05 MMA with fp16 operands, per-tile
 power-of-two scales and float32 accumulation; the DFT-8 stages, twiddles, coil maps,
 K x K kernel and coil sums run in float32, and the stack between the passes is float32.
-The forward row pass is the float32 kernel unless MRSR_TC_ROWS_FWD=1 selects its
-tensor-core form (tested in a child process, since the switch is read once).
+The forward row pass is the float32 four-step kernel.
 
 Four fp16 roundings of the operands (one per DFT-64) and the fp16 DFT matrix set the
 error: relative L2 vs the float64 oracle of ``mul!`` (src/NFFTNormalOp.jl:227-267) a few
@@ -47,44 +46,6 @@ def test_tc_apply_matches_oracle(mr, cuda, K, Nc, cplx):
     y32 = mr.to_host(mr.NFFTNormalOp(img, lam, cells, cmaps=cml) @ x)
     print(f"fp16-tc apply K={K} Nc={Nc} cplx={cplx}: rel L2 {err:.2e} (float32 {rel_l2(y32, ref):.2e})")
     assert err < TOL
-
-
-_TC_ROWS_FWD_CHILD = r"""
-import sys
-sys.path.insert(0, {root!r})
-import numpy as np
-import __graft_entry__ as ge
-from oracle import normalop as onormal
-mr = ge.package()
-rng = np.random.default_rng(7)
-img, K, Nc = (256, 256), 3, 4
-G = (512, 512)
-cells = np.flatnonzero(rng.random(G[0] * G[1]) < 0.8) + 1
-lam = (rng.standard_normal((6, cells.size)) + 1j * rng.standard_normal((6, cells.size))).astype(np.complex64)
-cm = (rng.standard_normal(img + (Nc,)) + 1j * rng.standard_normal(img + (Nc,))).astype(np.complex64)
-x = (rng.standard_normal(img + (K,)) + 1j * rng.standard_normal(img + (K,))).astype(np.complex64)
-cml = [cm[..., c] for c in range(Nc)]
-A = mr.NFFTNormalOp(img, lam, cells, cmaps=cml, precision="fp16-tc")
-y = mr.to_host(A @ x)
-ref = onormal.nfft_normalop_apply(x, onormal.unpack_lambda(lam.astype(np.complex128), K), cells, img, cmaps=cml)
-err = np.linalg.norm(y - ref) / np.linalg.norm(ref)
-print("ERR", err)
-assert err < {tol}, err
-"""
-
-
-def test_tc_forward_rows_on_tensor_cores(mr, cuda):
-    """MRSR_TC_ROWS_FWD=1: the forward row pass's DFT-64 on the tensor cores too."""
-    import os
-    import subprocess
-    import sys
-    from pathlib import Path
-    root = str(Path(__file__).resolve().parents[1])
-    env = dict(os.environ, MRSR_TC_ROWS_FWD="1")
-    r = subprocess.run([sys.executable, "-c", _TC_ROWS_FWD_CHILD.format(root=root, tol=TOL)], env=env,
-                       capture_output=True, text=True, timeout=600)
-    assert r.returncode == 0, r.stdout + r.stderr
-    assert "ERR" in r.stdout
 
 
 def test_tc_without_coil_maps(mr, cuda):

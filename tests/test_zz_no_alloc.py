@@ -6,6 +6,9 @@ keeps its work vectors in a static device array of the library instead of
 cudaMalloc'd buffers.  Its results must equal those of mrsr_cg, the regular
 entry point, call after call: the shared array keeps the previous call's
 contents, so a second solve in a row checks that nothing stale leaks in.
+The property it exists for is checked too: across a warm call, the device's
+default memory pool (where every other library buffer comes from, through
+cudaMallocAsync) neither grows nor hands out a single byte.
 Everything goes through the C ABI with ctypes.
 """
 import ctypes as C
@@ -19,6 +22,25 @@ from oracle import trajectories as otraj
 from tests.helpers import rand_c, rel_l2
 
 pytestmark = pytest.mark.gpu
+
+
+# CUmemPool_attribute values (CUDA driver API)
+_RESERVED_MEM_CURRENT, _USED_MEM_CURRENT = 5, 7
+
+
+def _pool_usage():
+    """(reserved, used) bytes of device 0's default memory pool, read through the driver API."""
+    drv = C.CDLL("libcuda.so.1")
+    dev = C.c_int(0)
+    assert drv.cuDeviceGet(C.byref(dev), 0) == 0
+    pool = C.c_void_p()
+    assert drv.cuDeviceGetDefaultMemPool(C.byref(pool), dev) == 0
+    out = []
+    for attr in (_RESERVED_MEM_CURRENT, _USED_MEM_CURRENT):
+        v = C.c_uint64(0)
+        assert drv.cuMemPoolGetAttribute(pool, attr, C.byref(v)) == 0
+        out.append(v.value)
+    return tuple(out)
 
 
 def _solve(lib, entry, A, b, maxiter, reltol):
@@ -50,6 +72,19 @@ def test_cg_noalloc_matches_cg_on_consecutive_calls(mr, cuda):
         assert it_new == it_ref
         assert rel_l2(x_new.cpu().numpy(), x_ref.cpu().numpy()) < 1e-6, f"call {call}"
         assert abs(rn_new - rn_ref) <= 1e-6 * max(rn_ref, 1e-30)
+    # a warm call allocates nothing: the pool's reserved and used bytes stay put
+    b = torch.from_numpy(rand_c(rng, (N * N * K,))).cuda()
+    x = torch.zeros_like(b)
+    torch.cuda.synchronize()  # every stream, the library's own included: pending frees have landed
+    before = _pool_usage()
+    it = C.c_int(0)
+    rn = C.c_double(0.0)
+    st = torch.cuda.current_stream().cuda_stream
+    status = lib.mrsr_cg_noalloc(A.handle, b.data_ptr(), x.data_ptr(), 20, 1e-4, 0.0, C.byref(it), C.byref(rn), st)
+    torch.cuda.synchronize()
+    after = _pool_usage()
+    assert status == 0, lib.mrsr_last_error()
+    assert after == before, f"pool (reserved, used) bytes {before} -> {after}"
 
 
 def test_cg_noalloc_rejects_problems_beyond_its_scratch(mr, cuda):
