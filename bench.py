@@ -180,30 +180,40 @@ def make_inputs(w, seed=42):
 
 
 # -------------------------------------------------------------- CPU arms ---
-def cpu_apply_sample(w, trj, cm, Lam=None, kmask=None, coils=2, reps=2, seed=0):
-    """Time the float32 CPU restatement of the reference apply on a bounded
-    sample (``coils`` of the Nc coils, ``reps`` times); returns (applies/s, cores, sample)."""
-    from oracle import normalop as onormal
+def synthetic_module():
+    """The package's seeded input generators (pure NumPy), loaded by path without the package."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mrsr_synthetic_inputs",
+                                                  ROOT / "mrfingerprintingrecon.jl_gb300" / "synthetic.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def arm_config(args, w, prec):
+    """The ``config`` object both arms print (identical, so the two lines describe one workload)."""
+    return {"workload": args.workload, "img": list(w["img"]), "Nr": w["Nr"], "Ncyc": w["Ncyc"], "Nt": w["Nt"],
+            "Nc": w["Nc"], "K": w["K"], "precision": prec,
+            "operator": "NFFTNormalOp " + {"fp32": "float32", "fp16": "fp16 storage, float32 arithmetic",
+                                           "fp16-tc": "tensor-core Λ and inverse row passes, float32 "
+                                                      "forward row pass"}[prec]
+            + " (real basis, packed real kernel)",
+            "parallelism": f"replicas x{args.gpus}", "l2": "flushed (256 MB write) before every timed step"}
+
+
+def cpu_apply_run(w, Lam, kmask, cm, x, steps, warmup):
+    """Full applies (all Nc coils) of the float32 CPU restatement of the reference apply on
+    the host cores: ``warmup`` untimed, then ``steps`` timed.  Returns (applies/s, cores)."""
     from oracle.cpu_apply import CpuNFFTNormalOp
-    G = tuple(2 * n for n in w["img"])
-    if kmask is None:
-        kmask = onormal.kmask_indcs(G, trj)
-    K = w["K"]
-    if Lam is None:  # values do not change the work of the apply; the kmask does
-        rng = np.random.default_rng(seed)
-        Lp = rng.standard_normal((K * (K + 1) // 2, kmask.size)).astype(np.float32)
-        Lam = onormal.unpack_lambda(Lp.astype(np.complex128), K).astype(np.complex64)
     cores = os.cpu_count()
-    op = CpuNFFTNormalOp(w["img"], Lam, kmask, cm, workers=cores)
-    x = (np.random.default_rng(seed + 1).standard_normal(tuple(w["img"]) + (K,)) + 0j).astype(np.complex64)
-    op.apply(x, coils=[0])  # warm-up
+    op = CpuNFFTNormalOp(w["img"], Lam.astype(np.complex64), kmask, cm, workers=cores)
+    xc = np.asarray(x, dtype=np.complex64)
+    for _ in range(warmup):
+        op.apply(xc)
     t0 = time.perf_counter()
-    for _ in range(reps):
-        op.apply(x, coils=list(range(coils)))
-    dt = (time.perf_counter() - t0) / reps
-    per_apply = dt * w["Nc"] / coils
-    sample = f"{coils} of {w['Nc']} coils x {reps} reps of one apply, scaled to {w['Nc']} coils"
-    return 1.0 / per_apply, cores, sample
+    for _ in range(steps):
+        op.apply(xc)
+    return steps / (time.perf_counter() - t0), cores
 
 
 def reference_arm(args, world, rank):
@@ -218,27 +228,31 @@ def reference_arm(args, world, rank):
                           "restatement is timed on the 2D apply workloads"}), flush=True)
         return
     w = WORKLOADS[args.workload]
-    # inputs from the oracle's own restatements only (no package code on this arm)
+    # The GPU arm's inputs, made on the host without the package: the same seeded trajectory,
+    # basis, phantom and coil maps, and the Toeplitz kernel and kmask of that trajectory from
+    # the oracle (float64 spreading NUFFT point-spread sums, ~1e-7 from the exact sums).
     from oracle import normalop as onormal
     from oracle import trajectories as otraj
+    syn = synthetic_module()
     trj = otraj.traj_2d_radial_goldenratio(w["Nr"], w["Ncyc"], w["Nt"])
-    rng = np.random.default_rng(42)
-    cm = (rng.standard_normal(tuple(w["img"]) + (w["Nc"],)) + 1j * rng.standard_normal(tuple(w["img"]) + (w["Nc"],)))
-    cm = (cm / np.sqrt(np.sum(np.abs(cm) ** 2, axis=-1, keepdims=True))).astype(np.complex64)
-    kmask = onormal.kmask_indcs(tuple(2 * n for n in w["img"]), trj)
-    rates = []
-    for i in range(args.warmup + args.steps):
-        r, cores, sample = cpu_apply_sample(w, trj, cm, kmask=kmask, coils=1, reps=1, seed=i)
-        if i >= args.warmup:
-            rates.append(r)
-    value = statistics.median(rates)
+    D = syn.dictionary(w["Nt"], seed=42)
+    U = syn.basis(D, w["K"])
+    x = syn.phantom(w["img"], D, U, seed=42)
+    cm = syn.coil_maps(w["img"], w["Nc"], seed=42)
+    Lam, kmask = onormal.calculate_kernel_noncartesian(tuple(2 * n for n in w["img"]), trj, U, fast=True)
+    value, cores = cpu_apply_run(w, Lam, kmask, cm, x, args.steps, args.warmup)
+    prec = "fp32" if args.precision in ("fp32", "refined") else ("fp16-tc" if "tc" in args.precision else "fp16")
+    sample = (f"per step: one full apply (all {w['Nc']} coils) of the float32 CPU restatement of "
+              "src/NFFTNormalOp.jl:227-267 on the GPU arm's inputs (trajectory-built kernel and kmask, "
+              "coil maps, phantom)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": args.workload, **{k: (list(v) if isinstance(v, tuple) else v) for k, v in w.items()},
-                       "operator": "NFFTNormalOp float32, restated reference CPU apply"},
-            "cpu_baseline": {"value": value, "unit": "applies/s", "cores": cores, "kind": "port",
-                             "sample": "per step: " + sample},
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+            "data": "synthetic (seeded phantom, dictionary basis, coil maps)",
+            "config": arm_config(args, w, prec),
+            "reference_operator": "float32 CPU restatement of the reference apply (Julia is not available here); "
+                                  "NumPy/SciPy FFTs on all host cores",
+            "cpu_baseline": {"value": value, "unit": "applies/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "applies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -392,19 +406,19 @@ def gb300_arm(args, world, rank, local):
     if rank != 0:
         return
     value = world * 1000.0 / ms
-    base_rate, cores, sample = cpu_apply_sample(w, trj, cm, kmask=mr.to_host(A.kmask_indcs))
+    from oracle import normalop as onormal
+    lam_dev = mr.to_host(A.Λ)
+    Lam_h = onormal.unpack_lambda(lam_dev.astype(np.complex128), K)
+    base_steps = 3
+    base_rate, cores = cpu_apply_run(w, Lam_h, mr.to_host(A.kmask_indcs), cm, x_h, base_steps, 1)
+    sample = (f"{base_steps} full applies (all {Nc} coils, after 1 untimed) of the float32 CPU restatement of "
+              "src/NFFTNormalOp.jl:227-267 on this operator's kernel, kmask, coil maps and x")
     line = {
         "metric": METRIC, "value": value, "unit": "applies/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": {"fp32": "c64", "fp16": "c64 (f16 storage)", "fp16-tc": "c64 (f16 tensor-core operands)"}[prec],
         "data": "synthetic (seeded phantom, dictionary basis, coil maps)",
-        "config": {"workload": args.workload, "img": list(w["img"]), "Nr": w["Nr"], "Ncyc": w["Ncyc"], "Nt": w["Nt"],
-                   "Nc": Nc, "K": K, "precision": prec,
-                   "operator": "NFFTNormalOp " + {"fp32": "float32", "fp16": "fp16 storage, float32 arithmetic",
-                                                  "fp16-tc": "tensor-core Λ and inverse row passes, float32 "
-                                                             "forward row pass"}[prec]
-                   + " (real basis, packed real kernel)",
-                   "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) before every timed step"},
+        "config": arm_config(args, w, prec),
         "e2e": {"value": world * 1000.0 / ms_e2e, "unit": "applies/s", "h2d_bytes_per_step": int(xh.numel() * 8),
                 "d2h_bytes_per_step": int(yh.numel() * 8)},
         "roofline": {"bound": "hbm", "kernel": f"Λ pass ({lam_kernel}: last-axis FFT + K x K kernel + inverse FFT)",

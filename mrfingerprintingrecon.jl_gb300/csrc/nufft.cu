@@ -99,6 +99,11 @@ __device__ __forceinline__ int64_t wrap(int64_t l, int64_t M) {
 
 // --------------------------------------------------------- spreading ---
 
+// one 64-bit fixed-point term: v (already scaled by 2^e) rounded to nearest
+__device__ __forceinline__ void fx_add(long long* q, float v) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(q), (unsigned long long)__float2ll_rn(v));
+}
+
 // one warp per kept sample; lanes cover the w^d taps
 __global__ void __launch_bounds__(256) k_spread_lambda(SpreadLambdaArgs a) {
   const int lane = threadIdx.x & 31;
@@ -106,6 +111,8 @@ __global__ void __launch_bounds__(256) k_spread_lambda(SpreadLambdaArgs a) {
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int d = a.S.d;
   const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
+  const float sc = a.fs->scale;
+  const int64_t chs = (int64_t)a.nq * a.cells;
   for (int64_t n = warp; n < a.S.n; n += nwarps) {
     const int64_t li = sample_lin(a.S, n);
     const int64_t t = li / a.S.ns_pf;
@@ -114,7 +121,7 @@ __global__ void __launch_bounds__(256) k_spread_lambda(SpreadLambdaArgs a) {
     float wt;
     int64_t l0[3] = {0, 0, 0};
     es_lane_weight(kd, a.M, d, lane, &wt, l0);
-    // basis values of this frame
+    // basis values of this frame (the tap weight below carries the 2^e scale)
     float2 u[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -130,6 +137,7 @@ __global__ void __launch_bounds__(256) k_spread_lambda(SpreadLambdaArgs a) {
       const int t1 = tt % kEsWidth, t2 = (tt / kEsWidth) % kEsWidth, t3 = tt / (kEsWidth * kEsWidth);
       float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
       if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
+      w *= sc;
       int64_t cell = wrap(l0[0] + t1, a.M[0]) + a.M[0] * wrap(l0[1] + t2, a.M[1]);
       if (d == 3) cell += a.M[0] * a.M[1] * wrap(l0[2] + t3, a.M[2]);
       int p = 0;
@@ -139,7 +147,9 @@ __global__ void __launch_bounds__(256) k_spread_lambda(SpreadLambdaArgs a) {
         for (int k1 = 0; k1 <= k2; ++k1) {
           if (k2 < a.K && p >= a.p0 && p < a.p0 + a.np) {
             const float2 v = cmulc(u[k2], u[k1]);  // conj(U[t,k1]) * U[t,k2]
-            atomicAdd(&a.grid[(int64_t)(p - a.p0) * a.cells + cell], make_float2(v.x * w, v.y * w));
+            long long* q = a.q + (int64_t)(p - a.p0) * chs + cell;
+            fx_add(q, v.x * w);
+            if (a.nq == 2) fx_add(q + a.cells, v.y * w);
           }
           ++p;
         }
@@ -154,6 +164,7 @@ __global__ void __launch_bounds__(256) k_spread_data(SpreadDataArgs a) {
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int d = a.S.d;
   const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
+  const float sc = a.fs->scale;
   for (int64_t n = warp; n < a.S.n; n += nwarps) {
     const int64_t li = sample_lin(a.S, n);
     const int64_t t = li / a.S.ns_pf;
@@ -176,6 +187,7 @@ __global__ void __launch_bounds__(256) k_spread_data(SpreadDataArgs a) {
       float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
       if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
       w *= dcf;
+      w *= sc;
       int64_t cell = wrap(l0[0] + t1, a.M[0]) + a.M[0] * wrap(l0[1] + t2, a.M[1]);
       if (d == 3) cell += a.M[0] * a.M[1] * wrap(l0[2] + t3, a.M[2]);
       for (int c = 0; c < a.nc; ++c) {
@@ -192,152 +204,26 @@ __global__ void __launch_bounds__(256) k_spread_data(SpreadDataArgs a) {
             const float uu = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
             v = make_float2(y.x * uu, y.y * uu);
           }
-          atomicAdd(&a.grid[((int64_t)c * a.K + k) * a.cells + cell], make_float2(v.x * w, v.y * w));
+          long long* q = a.q + ((int64_t)c * a.K + k) * 2 * a.cells + cell;
+          fx_add(q, v.x * w);
+          fx_add(q + a.cells, v.y * w);
         }
       }
     }
   }
 }
 
-// Channel-last spreading: the grid is [cell][channel] with an even channel
-// count, one warp per sample, and each lane adds two consecutive channels with
-// one float4 atomic, so a warp's atomic instruction covers 64 consecutive
-// channels of one cell (whole cache lines) instead of 32 scattered cells.
-// kCl channel values per lane are kept in registers for all taps.
-constexpr int kClPairs = 4;  // up to 2 * 32 * kClPairs = 256 channels
-template <class VAL>
-__device__ __forceinline__ void spread_cl_sample(const SampleSet& S, const int64_t* M, int64_t li, int nch,
-                                                 float extra_w, VAL val, float2* gcl) {
-  const int lane = threadIdx.x & 31;
-  const int d = S.d;
-  const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
-  float kd[3] = {0.f, 0.f, 0.f};
-  for (int dd = 0; dd < d; ++dd) kd[dd] = S.trj[dd + (int64_t)d * li];
-  float wt;
-  int64_t l0[3] = {0, 0, 0};
-  es_lane_weight(kd, M, d, lane, &wt, l0);
-  float4 v[kClPairs];
-#pragma unroll
-  for (int b = 0; b < kClPairs; ++b) {
-    const int ch = 2 * (lane + 32 * b);
-    float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
-    if (ch < nch) a0 = val(ch);
-    if (ch + 1 < nch) a1 = val(ch + 1);
-    v[b] = make_float4(a0.x * extra_w, a0.y * extra_w, a1.x * extra_w, a1.y * extra_w);
-  }
-  for (int tt = 0; tt < ntap; ++tt) {
-    const int t1 = tt % kEsWidth, t2 = (tt / kEsWidth) % kEsWidth, t3 = tt / (kEsWidth * kEsWidth);
-    float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
-    if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
-    if (w == 0.f) continue;
-    int64_t cell = wrap(l0[0] + t1, M[0]) + M[0] * wrap(l0[1] + t2, M[1]);
-    if (d == 3) cell += M[0] * M[1] * wrap(l0[2] + t3, M[2]);
-    float2* row = gcl + cell * nch;
-#pragma unroll
-    for (int b = 0; b < kClPairs; ++b) {
-      const int ch = 2 * (lane + 32 * b);
-      if (ch < nch)
-        atomicAdd(reinterpret_cast<float4*>(row + ch), make_float4(v[b].x * w, v[b].y * w, v[b].z * w, v[b].w * w));
-    }
-  }
-}
-
-__global__ void __launch_bounds__(256) k_spread_data_cl(SpreadDataArgs a, int nch, float2* gcl) {
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t ns_tot = a.S.ns_pf * a.S.nt;
-  for (int64_t n = warp; n < a.S.n; n += nwarps) {
-    const int64_t li = sample_lin(a.S, n);
-    const int64_t t = li / a.S.ns_pf;
-    float dcf = 1.f;
-    if (a.dcf_kind == MRSR_DCF_RADIAL_3D || a.dcf_kind == MRSR_DCF_RADIAL_2D) {
-      float s2 = 0.f;
-      for (int dd = 0; dd < a.S.d; ++dd) {
-        const float k = a.S.trj[dd + (int64_t)a.S.d * li];
-        s2 = __fadd_rn(s2, __fmul_rn(k, k));
-      }
-      dcf = a.dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
-    } else if (a.dcf_kind == MRSR_DCF_ARRAY) {
-      dcf = a.dcf[n];
-    }
-    spread_cl_sample(a.S, a.M, li, nch, dcf, [&](int ch) -> float2 {
-      if (ch >= a.nc * a.K) return make_float2(0.f, 0.f);  // row padding
-      const int c = ch / a.K, k = ch - c * a.K;
-      const float2 y = a.data[li + ns_tot * (a.c0 + c)];
-      if (a.u_complex) return cmulc(y, reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k]);
-      const float uu = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
-      return make_float2(y.x * uu, y.y * uu);
-    }, gcl);
-  }
-}
-
-__global__ void __launch_bounds__(256) k_spread_lambda_cl(SpreadLambdaArgs a, int nch, float2* gcl) {
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t n = warp; n < a.S.n; n += nwarps) {
-    const int64_t li = sample_lin(a.S, n);
-    const int64_t t = li / a.S.ns_pf;
-    spread_cl_sample(a.S, a.M, li, nch, 1.f, [&](int ch) -> float2 {
-      if (ch >= a.np) return make_float2(0.f, 0.f);  // row padding
-      // packed pair p0 + ch -> (k1, k2), k1 <= k2
-      int p = a.p0 + ch, k2 = 0;
-      while (p > k2) {
-        p -= k2 + 1;
-        ++k2;
-      }
-      const int k1 = p;
-      float2 u1, u2;
-      if (a.u_complex) {
-        u1 = reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k1];
-        u2 = reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k2];
-      } else {
-        u1 = make_float2(reinterpret_cast<const float*>(a.U)[t + a.S.nt * k1], 0.f);
-        u2 = make_float2(reinterpret_cast<const float*>(a.U)[t + a.S.nt * k2], 0.f);
-      }
-      return cmulc(u2, u1);  // conj(U[t,k1]) * U[t,k2]
-    }, gcl);
-  }
-}
-
-// [cell][nch] -> [ch][cell] through 32 x 32 shared-memory tiles
-__global__ void k_cl_to_planes(const float2* gcl, int nch, int nout, int64_t cells, float2* out) {
-  __shared__ float2 tile[32][33];
-  const int64_t c0 = (int64_t)blockIdx.x * 32;
-  const int h0 = blockIdx.y * 32;
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int64_t cell = c0 + r;
-    const int ch = h0 + threadIdx.x;
-    if (cell < cells && ch < nch) tile[r][threadIdx.x] = gcl[cell * nch + ch];
-  }
-  __syncthreads();
-  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
-    const int ch = h0 + r;
-    const int64_t cell = c0 + threadIdx.x;
-    if (cell < cells && ch < nout) out[(int64_t)ch * cells + cell] = tile[threadIdx.x][r];
-  }
+// taps of one sample that can land on the same cell (the w taps wrap around a grid shorter than w)
+static double taps_per_cell(int d, const int64_t* M) {
+  double t = 1.0;
+  for (int i = 0; i < d; ++i) t *= (double)cdiv(kEsWidth, M[i]);
+  return t;
 }
 
 static unsigned spread_blocks(int64_t n) { return (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(n * 32, 256), 1), 152 * 64); }
 
-// channel-last spreading into a scratch [cell][channel] grid, then transposed to a.grid
-static int spread_cl_finish(float2* gcl, int nch, int nout, int64_t cells, float2* grid, cudaStream_t st) {
-  const dim3 g((unsigned)cdiv(cells, 32), (unsigned)cdiv(nout, 32));
-  k_cl_to_planes<<<g, dim3(32, 8), 0, st>>>(gcl, nch, nout, cells, grid);
-  MRSR_LAUNCH_CHECK();
-  return MRSR_OK;
-}
-
 int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
-  if (a.np >= 160 && a.np <= 64 * kClPairs) {  // see spread_data
-    const int nchp = a.np + (a.np & 1);
-    DevBuf gcl;
-    MRSR_TRY(gcl.alloc(sizeof(float2) * a.cells * nchp));
-    MRSR_CHECK_CUDA(cudaMemsetAsync(gcl.p, 0, gcl.bytes, st));
-    k_spread_lambda_cl<<<spread_blocks(a.S.n), 256, 0, st>>>(a, nchp, gcl.as<float2>());
-    MRSR_LAUNCH_CHECK();
-    return spread_cl_finish(gcl.as<float2>(), nchp, a.np, a.cells, a.grid, st);
-  }
   k_spread_lambda<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
@@ -345,19 +231,67 @@ int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
 
 int spread_data(const SpreadDataArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
-  // channel-last pays off for many channels (GB300, 2D radial: 100 channels 8.6 ms vs
-  // 5.7 ms for the scattered kernel, 192 channels 20.5 ms vs 31 ms)
-  const int nch = a.nc * a.K;
-  if (a.U && nch >= 160 && nch <= 64 * kClPairs) {
-    const int nchp = nch + (nch & 1);  // float4 atomics need an even row length
-    DevBuf gcl;
-    MRSR_TRY(gcl.alloc(sizeof(float2) * a.cells * nchp));
-    MRSR_CHECK_CUDA(cudaMemsetAsync(gcl.p, 0, gcl.bytes, st));
-    k_spread_data_cl<<<spread_blocks(a.S.n), 256, 0, st>>>(a, nchp, gcl.as<float2>());
-    MRSR_LAUNCH_CHECK();
-    return spread_cl_finish(gcl.as<float2>(), nchp, nch, a.cells, a.grid, st);
-  }
   k_spread_data<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+// ------------------------------------------------------- fixed point ---
+
+// amax[slot] = max |f[i]| as float bits (non-negative floats order like their bit patterns)
+__global__ void k_absmax(const float* f, int64_t n, unsigned* amax) {
+  float m = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(f[i]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(amax, __float_as_uint(m));
+}
+
+// e = 62 - ceil(log2(nterms * mult * prod amax)); e clamped so 2^e is a normal float
+__global__ void k_fixed_scale(const unsigned* amax, int nf, double mult, double nterms, FixedScale* out) {
+  double b = nterms * mult;
+  for (int i = 0; i < nf; ++i) b *= (double)__uint_as_float(amax[i]);
+  int e = 0;
+  if (b > 0.0) e = 62 - (int)ceil(log2(b));
+  e = max(-120, min(120, e));
+  out->scale = ldexpf(1.f, e);
+  out->pad = 0.f;
+  out->inv = ldexp(1.0, -e);
+}
+
+int fixed_scale(const float* const* f, const int64_t* n, int nf, double mult, double nterms, FixedScale* out,
+                cudaStream_t st) {
+  MRSR_REQUIRE(nf >= 0 && nf <= 3, MRSR_ERR_ARG, "fixed_scale: at most 3 factors");
+  DevBuf am;
+  MRSR_TRY(am.alloc(4 * sizeof(unsigned)));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(am.p, 0, 4 * sizeof(unsigned), st));
+  for (int i = 0; i < nf; ++i) {
+    const unsigned g = (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(n[i], 1024), 1), 152 * 8);
+    k_absmax<<<g, 256, 0, st>>>(f[i], n[i], am.as<unsigned>() + i);
+    MRSR_LAUNCH_CHECK();
+  }
+  k_fixed_scale<<<1, 1, 0, st>>>(am.as<unsigned>(), nf, mult, nterms, out);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+__global__ void k_fixed_to_grid(const long long* q, int nq, int64_t cells, int64_t total, const FixedScale* fs,
+                                float2* out) {
+  const double inv = fs->inv;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ch = e / cells, cell = e - ch * cells;
+    const long long* qc = q + ch * nq * cells + cell;
+    const float re = (float)((double)qc[0] * inv);
+    const float im = nq == 2 ? (float)((double)qc[cells] * inv) : 0.f;
+    out[e] = make_float2(re, im);
+  }
+}
+
+int fixed_to_grid(const long long* q, int nq, int64_t cells, int64_t nch, const FixedScale* fs, float2* out,
+                  cudaStream_t st) {
+  const int64_t total = cells * nch;
+  const unsigned g = (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(total, 256), 1), 152 * 32);
+  k_fixed_to_grid<<<g, 256, 0, st>>>(q, nq, cells, total, fs, out);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
 }
@@ -481,19 +415,33 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
   MRSR_TRY(fG.init(d, G));
   DevBuf ipsi[3];
   for (int i = 0; i < d; ++i) MRSR_TRY(es_inv_psi_table(M[i], -G[i] / 2, G[i] + 1, ipsi[i]));
-  // channel batches bounded to ~2 GB of upsampled grid
+  // channel batches bounded to ~2 GB of upsampled float2 grid (plus its fixed-point accumulator)
   const int64_t max_bytes = 2ll << 30;
   const int pb = (int)std::max<int64_t>(1, std::min<int64_t>(P, max_bytes / (mcells * (int64_t)sizeof(float2))));
-  DevBuf grid, cgrid;
+  const int nq = u_complex ? 2 : 1;  // a real basis spreads real values
+  DevBuf grid, qgrid, cgrid, fsb;
   MRSR_TRY(grid.alloc(sizeof(float2) * mcells * pb));
+  MRSR_TRY(qgrid.alloc(sizeof(long long) * nq * mcells * pb));
   MRSR_TRY(cgrid.alloc(sizeof(float2) * gcells * P));
+  // fixed-point scale: |term| <= (2 if complex) max|U|^2 (the kernel taps are <= 1), and a cell
+  // of the upsampled grid gets at most ceil(w / M) taps per sample and dimension
+  MRSR_TRY(fsb.alloc(sizeof(FixedScale)));
+  {
+    const float* uf = reinterpret_cast<const float*>(U);
+    const int64_t nu = S.nt * (int64_t)K * (u_complex ? 2 : 1);
+    const float* f[2] = {uf, uf};
+    const int64_t n[2] = {nu, nu};
+    MRSR_TRY(fixed_scale(f, n, 2, u_complex ? 2.0 : 1.0, (double)S.n * taps_per_cell(d, M), fsb.as<FixedScale>(), st));
+  }
   MRSR_TRY(packed.alloc((u_complex ? 8 : 4) * (size_t)P * std::max<int64_t>(*nk_out, 1)));
   // channels in batches of pb: spread, inverse DFT on the upsampled grid, deconvolve and fold onto the 2x grid
   for (int p0 = 0; p0 < P; p0 += pb) {
     const int np = std::min(pb, P - p0);
-    MRSR_CHECK_CUDA(cudaMemsetAsync(grid.p, 0, sizeof(float2) * mcells * np, st));
-    SpreadLambdaArgs sa{S, {M[0], M[1], M[2]}, mcells, U, u_complex, K, P, p0, np, grid.as<float2>()};
+    MRSR_CHECK_CUDA(cudaMemsetAsync(qgrid.p, 0, sizeof(long long) * nq * mcells * np, st));
+    SpreadLambdaArgs sa{S, {M[0], M[1], M[2]}, mcells, U, u_complex, K, P, p0, np, nq, qgrid.as<long long>(),
+                        fsb.as<FixedScale>()};
     MRSR_TRY(spread_lambda(sa, st));
+    MRSR_TRY(fixed_to_grid(qgrid.as<long long>(), nq, mcells, np, fsb.as<FixedScale>(), grid.as<float2>(), st));
     MRSR_TRY(fM.run(grid.as<float2>(), np, +1, 1.0f, st));
     FoldArgs fa;
     fa.d = d;
@@ -734,16 +682,42 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
   const int64_t max_bytes = 2ll << 30;
   const int64_t per_coil = (int64_t)K * mcells * (int64_t)sizeof(float2);
   const int cc = (int)std::max<int64_t>(1, std::min<int64_t>(ncoils, max_bytes / std::max<int64_t>(per_coil, 1)));
-  DevBuf grid;
+  DevBuf grid, qgrid, fsb;
   MRSR_TRY(grid.alloc((size_t)per_coil * cc));
+  MRSR_TRY(qgrid.alloc((size_t)per_coil * 2 * cc));  // fixed-point re and im, 8 bytes each
+  // fixed-point scale: |term component| <= max|data| max|U| (x2 for complex U) x dcf bound,
+  // at most ceil(w / M) taps per sample, cell and dimension
+  MRSR_TRY(fsb.alloc(sizeof(FixedScale)));
+  {
+    const float* f[3];
+    int64_t n[3];
+    int nf = 0;
+    double mult = 1.0;
+    f[nf] = data;
+    n[nf++] = 2 * ns_per_frame * nt * (int64_t)ncoils;
+    if (U) {
+      f[nf] = reinterpret_cast<const float*>(U);
+      n[nf++] = nt * (int64_t)K * (u_is_complex ? 2 : 1);
+      if (u_is_complex) mult *= 2.0;
+    }
+    if (dcf_kind == MRSR_DCF_RADIAL_2D) mult *= 0.5 * std::sqrt((double)ndims);  // |k| <= sqrt(d) / 2
+    if (dcf_kind == MRSR_DCF_RADIAL_3D) mult *= 0.25 * ndims;                   // |k|^2 <= d / 4
+    if (dcf_kind == MRSR_DCF_ARRAY) {
+      f[nf] = dcf_array;
+      n[nf++] = sl.set.n;
+    }
+    MRSR_TRY(fixed_scale(f, n, nf, mult, (double)sl.set.n * taps_per_cell(ndims, M), fsb.as<FixedScale>(), st));
+  }
   const int64_t out_elems = nimg * K * (cmaps ? 1 : ncoils);
   if (cmaps) MRSR_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(float2) * out_elems, st));
   for (int c0 = 0; c0 < ncoils; c0 += cc) {
     const int nc = std::min(cc, ncoils - c0);
-    MRSR_CHECK_CUDA(cudaMemsetAsync(grid.p, 0, (size_t)per_coil * nc, st));
+    MRSR_CHECK_CUDA(cudaMemsetAsync(qgrid.p, 0, (size_t)per_coil * 2 * nc, st));
     SpreadDataArgs sa{sl.set, {M[0], M[1], M[2]}, mcells, reinterpret_cast<const float2*>(data), c0, nc, U,
-                      u_is_complex, K, dcf_kind, dcf_array, grid.as<float2>()};
+                      u_is_complex, K, dcf_kind, dcf_array, qgrid.as<long long>(), fsb.as<FixedScale>()};
     MRSR_TRY(spread_data(sa, st));
+    MRSR_TRY(fixed_to_grid(qgrid.as<long long>(), 2, mcells, (int64_t)nc * K, fsb.as<FixedScale>(), grid.as<float2>(),
+                           st));
     MRSR_TRY(fM.run(grid.as<float2>(), (int64_t)nc * K, +1, 1.0f, st));
     BpFoldArgs fa;
     fa.d = ndims;

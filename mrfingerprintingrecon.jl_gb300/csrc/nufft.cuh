@@ -67,7 +67,23 @@ __device__ __forceinline__ void es_lane_weight(const float* kd, const int64_t* M
 // Deconvolution factors 1/psi_hat(j) for j = jmin .. jmin + count - 1 on an upsampled grid of size M.
 int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, DevBuf& out);
 
-// grid[ch][cell] += sum over samples of value(ch, n) * phi taps, cells column-major on dims M.
+// Fixed-point accumulation of the spread grids.  Each tap's term (a float32 product of
+// the sample value and the kernel weights) is scaled by 2^e, rounded to a 64-bit integer
+// and added to the grid with 64-bit integer atomics.  Integer addition is associative, so
+// every cell holds the exact sum of its rounded terms whatever order the samples land in:
+// the grids are bitwise reproducible run to run, and the sum carries no accumulation
+// error (a float32 atomic sum of n terms drifts by ~sqrt(n) float32 roundings of the
+// running total, a float64 one by ~n float64 roundings).  e = 62 - ceil(log2(n_terms *
+// max|term|)) from a device-side bound, so no cell can overflow, and the resolution
+// 2^-e is ~1e-19 of the largest possible cell sum.
+struct FixedScale {
+  float scale;   // 2^e
+  float pad;
+  double inv;    // 2^-e
+};
+
+// grid[ch][part][cell] (part: re, and im for complex grids) += value(ch, n) * phi taps,
+// cells column-major on dims M, in units of 2^-e.
 // value(ch, n): Λ precompute channels (pairs of basis columns) or data channels.
 struct SpreadLambdaArgs {
   SampleSet S;
@@ -76,7 +92,9 @@ struct SpreadLambdaArgs {
   int u_complex, K;
   int P;              // channels: packed pairs k1 <= k2
   int p0, np;         // spread only channels p0 .. p0+np-1
-  float2* grid;       // [np][cells]
+  int nq;             // parts per cell: 1 (real basis: the spread values are real) or 2
+  long long* q;       // [np][nq][cells]
+  const FixedScale* fs;
 };
 int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st);
 
@@ -89,8 +107,19 @@ struct SpreadDataArgs {
   int u_complex, K;
   int dcf_kind;
   const float* dcf;     // per kept sample (dcf_kind == array)
-  float2* grid;         // [(c - c0) * K + k][cells]
+  long long* q;         // [(c - c0) * K + k][2][cells]
+  const FixedScale* fs;
 };
 int spread_data(const SpreadDataArgs& a, cudaStream_t st);
+
+// Scale of a fixed-point grid: every term's components are bounded by `mult` times the
+// product of the largest absolute entries of the nf (<= 3) factor arrays f[i] (n[i]
+// floats each), and a cell sums at most `nterms` terms.
+int fixed_scale(const float* const* f, const int64_t* n, int nf, double mult, double nterms, FixedScale* out,
+                cudaStream_t st);
+
+// out[ch][cell] = complex(q[ch][0][cell], q[ch][1][cell] or 0) * 2^-e, for nch channels.
+int fixed_to_grid(const long long* q, int nq, int64_t cells, int64_t nch, const FixedScale* fs, float2* out,
+                  cudaStream_t st);
 
 }  // namespace mrsr

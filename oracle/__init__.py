@@ -13,14 +13,14 @@ project):
 * ``trajectories`` -- ``src/Trajectories.jl:81-173``
 * ``nudft``        -- exact non-uniform DFTs used as the forward model of the
   reference tests (``test/reconstruct_radial.jl:62-74``) and as the exact
-  replacement of the NonuniformFFTs.jl type-1 transform
+  replacement of the NonuniformFFTs.jl type-1 transform, plus a float64
+  spreading type-1 NUFFT (~1e-7) for benchmark-sized trajectories
 * ``normalop``     -- ``src/NFFTNormalOp.jl:106-267`` (kmask, Toeplitz kernel
   for complex and real bases, apply) and ``src/FFTNormalOp.jl:81-149``
 * ``backprojection`` -- ``src/BackProjection.jl:23-203``
 * ``grog``         -- ``src/GROG.jl:14-102``
 * ``cg``           -- IterativeSolvers.jl 0.9 ``cg`` as called from the
   reference tests (``test/reconstruct_radial.jl:83``)
-* ``synthetic``    -- seeded inputs shaped like the reference tests
 * ``cpu_apply``    -- float32 structure-faithful restatement of the CPU apply
   ``src/NFFTNormalOp.jl:227-267`` used only as the timed CPU baseline
 

@@ -6,10 +6,12 @@ step by step: per coil, zero the 2x oversampled K-stack, copy ``cmap .* b``
 into the low corner, K full FFTs, a per-voxel K x K product on the kmask
 voxels (kL2 zero elsewhere), K inverse FFTs, crop and accumulate
 ``α conj(cmap) .* kL2``.  FFTs run through ``scipy.fft`` with all host threads
-(the reference uses FFTW with ``num_threads``); the per-voxel products are one
-batched matmul.
+(the reference runs its K FFTs on Julia threads); the per-voxel K x K products
+are batched matmuls over voxel chunks on a thread pool of all host cores, as the
+reference's ``@tasks`` loop over voxels (``src/NFFTNormalOp.jl:253-255``).
 """
 import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import scipy.fft as sfft
@@ -27,6 +29,10 @@ class CpuNFFTNormalOp:
         self.workers = workers or os.cpu_count()
         self.kL1 = np.zeros((self.K,) + self.G[::-1], dtype=np.complex64)  # C-order (K, G_d, ..., G_1)
         self.kL2 = np.zeros_like(self.kL1)
+        self.pool = ThreadPoolExecutor(self.workers)
+        nch = 4 * self.workers
+        bounds = np.linspace(0, self.kidx.size, nch + 1).astype(np.int64)
+        self.chunks = [(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
 
     def apply(self, b, coils=None, alpha=1.0):
         """x = alpha * A b for the coils in ``coils`` (default: all); b (img..., K)."""
@@ -45,8 +51,12 @@ class CpuNFFTNormalOp:
             k2 = self.kL2.reshape(self.K, -1)
             k2.fill(0)
             # kmask indices are column-major over the 2x grid = row-major over the reversed C-order axes
-            X = k1[:, self.kidx].T[:, :, None]                  # (Nk, K, 1)
-            k2[:, self.kidx] = np.matmul(self.lamT, X)[:, :, 0].T
+            def voxels(ab, k1=k1, k2=k2):
+                a, b = ab
+                ix = self.kidx[a:b]
+                X = k1[:, ix].T[:, :, None]                     # (n, K, 1)
+                k2[:, ix] = np.matmul(self.lamT[a:b], X)[:, :, 0].T
+            list(self.pool.map(voxels, self.chunks))
             self._fft(self.kL2, axes, +1)
             x += alpha * np.conj(cT[c])[None] * self.kL2[sl]
         return np.moveaxis(x.transpose((0,) + tuple(range(d, 0, -1))), 0, -1)

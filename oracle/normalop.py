@@ -7,6 +7,7 @@ layout, ``ext/MRISubspaceReconCUDAExt/NFFTNormalOp.jl:239``), linear grid
 indices are 1-based and column-major like Julia's ``findall``.
 """
 import numpy as np
+import scipy.fft as sfft
 
 from . import nudft
 
@@ -80,20 +81,27 @@ def _fft_order(n):
     return np.concatenate([np.arange(0, n // 2), np.arange(-(n // 2), 0)])
 
 
+def _psf_sets(G, half_first):
+    sets = [np.arange(0, G[0] // 2 + 1) if half_first else _fft_order(G[0])]
+    return sets + [_fft_order(g) for g in G[1:]]
+
+
 def psf(img_shape_os, pts, w, half_first=False):
     """Exact point-spread sums c[j] = sum_n w_n exp(+2 pi i j.k_n) on the grid in FFT order.
 
     With ``half_first`` the first dimension holds j1 = 0..G1/2 (the half
     spectrum a real-input type-1 transform returns), the others FFT order.
     """
-    G = img_shape_os
-    sets = [np.arange(0, G[0] // 2 + 1) if half_first else _fft_order(G[0])]
-    sets += [_fft_order(g) for g in G[1:]]
-    return nudft.nudft_sum(w, pts, sets, +1.0)
+    return nudft.nudft_sum(w, pts, _psf_sets(img_shape_os, half_first), +1.0)
 
 
-def calculate_kernel_noncartesian(img_shape_os, trj, U, sample_mask=None):
-    """``src/NFFTNormalOp.jl:121-225`` with exact PSFs. Returns (Lam[K,K,Nk], kmask)."""
+def calculate_kernel_noncartesian(img_shape_os, trj, U, sample_mask=None, fast=False):
+    """``src/NFFTNormalOp.jl:121-225`` with exact PSFs. Returns (Lam[K,K,Nk], kmask).
+
+    ``fast``: the point-spread sums come from the float64 spreading NUFFT
+    (``nudft.Nufft1Plan``, ~1e-7 relative) instead of exact sums, for
+    trajectories too large for O(modes x samples).
+    """
     trj = np.asarray(trj, dtype=np.float32)
     if sample_mask is None:
         sample_mask = np.ones(trj.shape[1:], dtype=bool)
@@ -106,11 +114,16 @@ def calculate_kernel_noncartesian(img_shape_os, trj, U, sample_mask=None):
     G = tuple(img_shape_os)
     Lam = np.zeros((K, K, len(kmask)), dtype=np.complex128)
     real_u = not np.iscomplexobj(U)
+    if fast:
+        plan = nudft.Nufft1Plan(pts, _psf_sets(G, real_u), +1.0)
+        psf_of = lambda w, half_first=False: plan(w)  # noqa: E731
+    else:
+        psf_of = lambda w, half_first=False: psf(G, pts, w, half_first=half_first)  # noqa: E731
     for k2 in range(K):
         for k1 in range(k2 + 1):
             if real_u:
                 w = (U[t_of, k1].astype(np.float64) * U[t_of, k2].astype(np.float64))
-                ch = psf(G, pts, w, half_first=True)
+                ch = psf_of(w, half_first=True)
                 axes = tuple(range(1, len(G))) + (0,)
                 s = tuple(G[1:]) + (G[0],)
                 lam = np.fft.irfftn(np.conj(ch), s=s, axes=axes) * np.prod(G)
@@ -119,7 +132,7 @@ def calculate_kernel_noncartesian(img_shape_os, trj, U, sample_mask=None):
                 Lam[k2, k1] = v
             else:
                 w = np.conj(U[t_of, k1].astype(np.complex128)) * U[t_of, k2].astype(np.complex128)
-                c = psf(G, pts, w)
+                c = psf_of(w)
                 lam = np.fft.fftn(c)
                 v = lam.ravel(order="F")[kmask - 1]
                 # statement order of src/NFFTNormalOp.jl:161-162: the mirror first, so the diagonal keeps λ
@@ -176,12 +189,12 @@ def nfft_normalop_apply(x, Lam, kmask, img_shape, cmaps=None, alpha=1.0, beta=0.
     for c in range(S.shape[0]):
         kL1 = np.zeros(G + (K,), dtype=np.complex128)
         kL1[idx] = S[c][..., None] * x
-        kL1 = np.fft.fftn(kL1, axes=tuple(range(d)))
+        kL1 = sfft.fftn(kL1, axes=tuple(range(d)), workers=-1)
         k1r = kL1.reshape(-1, K, order="F")
         k2r = np.zeros_like(k1r)
         k2r[kidx] = np.einsum("jki,ik->ij", Lam, k1r[kidx])
         kL2 = k2r.reshape(G + (K,), order="F")
-        kL2 = np.fft.ifftn(kL2, axes=tuple(range(d)))
+        kL2 = sfft.ifftn(kL2, axes=tuple(range(d)), workers=-1)
         out += alpha * np.conj(S[c])[..., None] * kL2[idx]
     return out
 

@@ -116,25 +116,75 @@ def test_grog_gridding_matches_oracle(mr, cuda, nrep):
         assert rel_l2(got[..., 1], got[..., 0]) < 1e-5
 
 
+def _ellipse_image(N, seed):
+    """A piecewise-constant test image of random ellipses (stands in for Shepp-Logan)."""
+    rng = np.random.default_rng(seed)
+    g = np.meshgrid(np.linspace(-1, 1, N), np.linspace(-1, 1, N), indexing="ij")
+    img = np.zeros((N, N))
+    img[(g[0] / 0.69) ** 2 + (g[1] / 0.92) ** 2 <= 1] = 1.0
+    img[(g[0] / 0.66) ** 2 + ((g[1] + 0.02) / 0.87) ** 2 <= 1] = 0.2
+    for _ in range(6):
+        c = rng.uniform(-0.4, 0.4, 2)
+        ax = rng.uniform(0.05, 0.25, 2)
+        img[((g[0] - c[0]) / ax[0]) ** 2 + ((g[1] - c[1]) / ax[1]) ** 2 <= 1] += rng.uniform(-0.2, 0.3)
+    return img
+
+
 @pytest.mark.gpu
 def test_radial_grog_then_fft_normalop_recon(mr, cuda):
-    """test/grog_recon.jl: GROG-gridded data reconstructs with FFTNormalOp + CG."""
+    """test/grog_recon.jl at its own sizes: 64^2, Nr = 128, rank 4 (two non-zero coefficient
+    images), Nt = 100 frames x 200 golden-angle spokes, 9 Gaussian coil maps.  Both the NUFFT
+    reconstruction (NFFTNormalOp + cg, 20 iterations) and the GROG reconstruction (radial_grog!
+    + FFTNormalOp + cg, 20 iterations, global phase slope removed as in :91-92) match the
+    phantom cropped to the sampled k-space disk within the reference's rtol = 5e-2 (:95-96)."""
     import torch
-    trj, data, Nr, img, maps, x = _grog_data(N=16, Ncyc=8, Nt=20, Nc=8, seed=4)
-    d = mr.to_jl(data, torch.complex64)
+    Nx, Nr, K, Nt, Ncyc, Ncoil = 64, 128, 4, 100, 200, 9
+    img = (Nx, Nx)
+    rng = np.random.default_rng(42)
+    x = np.zeros((Nx, Nx, K), dtype=np.complex64)
+    x[:, :, 0] = _ellipse_image(Nx, 1).T
+    x[: Nx // 2, :, 0] *= np.exp(1j * np.pi / 3)
+    x[:, :, 1] = _ellipse_image(Nx, 2)
+    # Gaussian coil maps centred on a 3 x 3 grid (gauss2 at Nx/8, Nx/2, 7Nx/8, width Nx/1.5)
+    ii, jj = np.meshgrid(np.arange(1, Nx + 1), np.arange(1, Nx + 1), indexing="ij")
+    cm = np.empty((Nx, Nx, Ncoil), dtype=np.complex64)
+    centres = [Nx // 8, Nx // 2, 7 * Nx // 8]
+    for a, ca in enumerate(centres):
+        for b, cb in enumerate(centres):
+            w = Nx // 1.5
+            cm[:, :, 3 * a + b] = np.exp(-4 * np.log(2) * (((ii - ca) / w) ** 2 + ((jj - cb) / w) ** 2))
+    cm /= np.sqrt(np.sum(np.abs(cm) ** 2, axis=-1, keepdims=True))
+    # traj_kooshball(Nr, theta = pi/2, phi = golden angle) restricted to its first two dimensions
+    ag = 2 * np.pi / (1 + np.sqrt(5))
+    phi = (ag * np.arange(Nt * Ncyc)).astype(np.float32).reshape(Ncyc, Nt, order="F")
+    kr = (np.arange(-(Nr - 1) / 2, (Nr - 1) / 2 + 1) / Nr).astype(np.float32)
+    trj = np.empty((2, Nr, Ncyc, Nt), dtype=np.float32)
+    trj[0] = kr[:, None, None] * np.cos(phi)[None]
+    trj[1] = kr[:, None, None] * np.sin(phi)[None]
+    trj = trj.reshape(2, Nr * Ncyc, Nt, order="F")
+    U = np.linalg.svd(rand_c(rng, (Nt, K)), full_matrices=False)[0].astype(np.complex64)
+    cmd = mr.to_jl(cm, torch.complex64)
+    d = mr.forward_model(mr.to_jl(x, torch.complex64), trj, U, cmaps=cmd)
+    cml = [cm[..., c] for c in range(Ncoil)]
+    # ground truth: x cropped to the disk |k| <= Nx/2
+    xc = np.fft.fftshift(np.fft.fft2(x, axes=(0, 1)), axes=(0, 1))
+    xc[(ii - 1 - Nx / 2) ** 2 + (jj - 1 - Nx / 2) ** 2 > (Nx / 2) ** 2] = 0
+    xc = np.fft.ifft2(np.fft.ifftshift(xc, axes=(0, 1)), axes=(0, 1))
+    # NUFFT reconstruction
+    A = mr.NFFTNormalOp(img, trj, U, cmaps=cml)
+    b = mr.calculate_backprojection(d, trj, cml, U=U)
+    xr = mr.to_host(mr.cg(A, b, maxiter=20))
+    # GROG reconstruction
     trj_cart = mr.radial_grog(d, trj, Nr, img)
-    U = np.ones((trj.shape[2], 1), dtype=np.complex64)
-    cml = [maps[..., c] for c in range(maps.shape[-1])]
-    A = mr.FFTNormalOp(img, trj_cart, U, cmaps=cml)
-    b = mr.calculate_backprojection(d, trj_cart, cml, U=U)
-    xr = mr.to_host(mr.cg(A, b, maxiter=20))[..., 0]
-    assert np.all(np.isfinite(xr))
-    # the GROG recon matches the image up to the gridding's global phase slope (test/grog_recon.jl:95)
-    ii, jj = np.meshgrid(np.arange(16), np.arange(16), indexing="ij")
-    xg = xr * -np.exp(1j * np.pi * (ii + jj) / 16)
-    xc = np.fft.fftshift(np.fft.fft2(x))
-    ii2, jj2 = np.meshgrid(np.arange(16), np.arange(16), indexing="ij")
-    xc[(ii2 - 8) ** 2 + (jj2 - 8) ** 2 > 64] = 0
-    xc = np.fft.ifft2(np.fft.ifftshift(xc))
-    err = min(rel_l2(xg, xc), rel_l2(xr, xc))
-    assert err < 0.3
+    Ac = mr.FFTNormalOp(img, trj_cart, U, cmaps=cml)
+    bc = mr.calculate_backprojection(d, trj_cart, cml, U=U)
+    xg = mr.to_host(mr.cg(Ac, bc, maxiter=20))
+    xg = xg * -np.exp(1j * np.pi * ((ii - 1) + (jj - 1)) / Nx)[..., None]
+
+    def isapprox(a, b, rtol):  # Julia's norm-wise isapprox
+        return np.linalg.norm(a - b) <= rtol * max(np.linalg.norm(a), np.linalg.norm(b))
+
+    er, eg = rel_l2(xr, xc), rel_l2(xg, xc)
+    print(f"grog_recon: NUFFT recon vs crop {er:.3e}, GROG recon vs crop {eg:.3e}")
+    assert isapprox(xc, xr, 5e-2)
+    assert isapprox(xc, xg, 5e-2)
