@@ -268,6 +268,23 @@ int mrsr_cg_stacked(mrsr_normalop* op, const float* b, float* x, int maxiter, do
 int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const float* b, float* x, int inner_iters,
                     int max_outer, double tol, int* outer_out, double* relres_out, mrsr_stream_t stream);
 
+/* Relaxed mixed-precision CG (no counterpart in the reference): cg(A, b;
+ * maxiter, reltol, abstol) as mrsr_cg runs it (x0 = 0, IterativeSolvers'
+ * recurrence), whose operator products use the float32 op_hi while
+ * ||r|| > switch_relres * ||b|| and the reduced-precision op_lo (fp16 or
+ * fp16-tc) after that, on the same recurrence (no restart).  Product errors
+ * taken at a large residual move a CG iterate the most, so the first few
+ * iterations stay float32 and the rest run on the faster operator; the iterate
+ * stays close to the float32 / float64 CG iterate of the same iteration count
+ * (switch_relres = 0.05 on 20 iterations: ~5e-4 from float64).  0 runs every
+ * product on op_hi, >= 1 every product on op_lo.  iters_out, hi_iters_out (the
+ * float32 iterations) and resnorm_out are host pointers (may be NULL); the
+ * call synchronises the stream, once per float32 iteration.  op_lo and op_hi
+ * must describe the same operator; the vectors live in op_hi's workspace. */
+int mrsr_cg_relaxed(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const float* b, float* x, int maxiter,
+                    double reltol, double abstol, double switch_relres, int* iters_out, int* hi_iters_out,
+                    double* resnorm_out, mrsr_stream_t stream);
+
 /* ---------------------------------------------------------------------
  * Serving support (no counterpart in the reference).
  *

@@ -7,14 +7,14 @@ no CPU implementation: every call runs on the current CUDA device.
 from . import _lib
 from .normalop import NFFTNormalOp, FFTNormalOp, NormalOperator
 from .backprojection import calculate_backprojection, forward_model
-from .solvers import cg, cg_refined, cg_stacked, CgBatch
+from .solvers import cg, cg_refined, cg_relaxed, cg_stacked, CgBatch
 from .grog import grog_calib, grog_gridding, radial_grog
 from .coilmaps import reconstruct_coilwise, calculate_calibration_kspace, calibration_mask
 from . import trajectories, synthetic
 from .arrays import jl_empty, jl_zeros, jl_reshape, to_jl, to_host
 
 __all__ = ["NFFTNormalOp", "FFTNormalOp", "NormalOperator", "calculate_backprojection", "forward_model", "cg",
-           "cg_refined", "cg_stacked", "CgBatch", "grog_calib", "grog_gridding", "radial_grog", "reconstruct_coilwise",
+           "cg_refined", "cg_relaxed", "cg_stacked", "CgBatch", "grog_calib", "grog_gridding", "radial_grog", "reconstruct_coilwise",
            "calculate_calibration_kspace", "calibration_mask", "trajectories", "synthetic",
            "jl_empty", "jl_zeros", "jl_reshape", "to_jl", "to_host"]
 

@@ -43,6 +43,7 @@ SIGNATURES = {
     "mrsr_cg": [p, p, p, i32, f64, f64, C.POINTER(i32), C.POINTER(f64), p],
     "mrsr_cg_refined": [p, p, p, p, i32, i32, f64, C.POINTER(i32), C.POINTER(f64), p],
     "mrsr_cg_noalloc": [p, p, p, i32, f64, f64, C.POINTER(i32), C.POINTER(f64), p],
+    "mrsr_cg_relaxed": [p, p, p, p, i32, f64, f64, f64, C.POINTER(i32), C.POINTER(i32), C.POINTER(f64), p],
     "mrsr_normalop_stack": [p, i32, p, C.POINTER(p)],
     "mrsr_cg_stacked": [p, p, p, i32, f64, f64, C.POINTER(i32), C.POINTER(f64), p],
     "mrsr_normalop_share": [p, p, i32, i32, p, C.POINTER(p)],

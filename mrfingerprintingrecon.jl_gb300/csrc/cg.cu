@@ -199,7 +199,10 @@ static unsigned vec_blocks(int64_t n) {
 void CgWork::drop_graphs() {
   if (it8) cudaGraphExecDestroy(it8);
   if (it1) cudaGraphExecDestroy(it1);
-  it8 = it1 = nullptr;
+  if (lo8) cudaGraphExecDestroy(lo8);
+  if (lo1) cudaGraphExecDestroy(lo1);
+  it8 = it1 = lo8 = lo1 = nullptr;
+  lo_serial = 0;
 }
 
 CgWork::~CgWork() {
@@ -490,6 +493,97 @@ extern "C" int mrsr_cg_refined(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const
   if (outer_out) *outer_out = outer;
   if (relres_out) *relres_out = relres;
   return MRSR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Relaxed mixed-precision CG.
+//
+// One CG recurrence (IterativeSolvers' iteration, x0 = 0) whose operator products switch
+// from the float32 operator op_hi to the reduced-precision op_lo once the residual has
+// fallen to ||r|| <= switch_relres ||b||.  The deviation of a CG iterate caused by an
+// inexact product grows with the residual at the step where the product was taken
+// (inexact Krylov theory: the tolerable product error at step k scales like 1 / ||r_k||),
+// so the few large-residual steps run on the accurate operator and the many later steps
+// on the fast one, and the iterate stays close to the float32 / float64 CG iterate of the
+// same iteration count.  Restarted refinement (mrsr_cg_refined) instead converges to
+// A_hi^-1 b, which on the kmask-truncated Toeplitz operator is far from a CG-k iterate.
+// The vectors live in op_hi's CG workspace.
+// ---------------------------------------------------------------------------
+extern "C" int mrsr_cg_relaxed(mrsr_normalop* op_lo, mrsr_normalop* op_hi, const float* b, float* x, int maxiter,
+                               double reltol, double abstol, double switch_relres, int* iters_out, int* hi_iters_out,
+                               double* resnorm_out, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
+  MRSR_REQUIRE(op_lo && op_hi && b && x, MRSR_ERR_ARG, "NULL argument to mrsr_cg_relaxed");
+  MRSR_REQUIRE(op_lo != op_hi, MRSR_ERR_ARG, "mrsr_cg_relaxed needs two different operators");
+  MRSR_REQUIRE(op_lo->geo.nimg() == op_hi->geo.nimg() && op_lo->geo.K == op_hi->geo.K, MRSR_ERR_ARG,
+               "operators of different sizes");
+  MRSR_REQUIRE(!lam_is_diag(op_hi->lam_mode) && !lam_is_diag(op_lo->lam_mode), MRSR_ERR_ARG,
+               "mrsr_cg_relaxed solves one system; use mrsr_cg_stacked for stacked operators");
+  MRSR_REQUIRE((const void*)b != (const void*)x, MRSR_ERR_ARG, "b and x must not alias");
+  MRSR_REQUIRE(maxiter >= 0, MRSR_ERR_ARG, "maxiter must be >= 0");
+  MRSR_REQUIRE(switch_relres >= 0.0, MRSR_ERR_ARG, "switch_relres must be >= 0");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  OpUse use_lo{op_lo, st}, use_hi{op_hi, st};
+  CgWork& w = op_hi->cg;
+  const int64_t n = op_hi->geo.nimg() * op_hi->geo.K;
+  MRSR_TRY(w.ensure(n, 1));
+  if (!w.xw.p) MRSR_TRY(w.xw.alloc(sizeof(float2) * n));
+  CgState* s = w.state.as<CgState>();
+  const unsigned nb = vec_blocks(n);
+  k_cg_init<<<nb, kCgThreads, 0, st>>>(reinterpret_cast<const float2*>(b), w.xw.as<float2>(), w.r.as<float2>(),
+                                       w.u.as<float2>(), n, reltol, abstol, maxiter, s, w.partial.as<double2>());
+  MRSR_LAUNCH_CHECK();
+  CgState h;
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  const double bnorm = h.res;
+  // phase 1: float32 products, one iteration at a time, the residual read back after each
+  int done_its = 0, hi_its = 0;
+  if (maxiter > 0 && h.res > switch_relres * bnorm && !h.done && !w.it1) MRSR_TRY(cg_capture(op_hi, w, 1, &w.it1));
+  while (done_its < maxiter && !h.done && h.res > switch_relres * bnorm) {
+    MRSR_CHECK_CUDA(cudaGraphLaunch(w.it1, st));
+    ++done_its;
+    ++hi_its;
+    MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+    MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  }
+  // phase 2: reduced-precision products on the same recurrence, graphs of 8 and 1 iterations
+  if (done_its < maxiter && !h.done) {
+    if (w.lo_serial != op_lo->serial) {
+      if (w.lo8) cudaGraphExecDestroy(w.lo8);
+      if (w.lo1) cudaGraphExecDestroy(w.lo1);
+      w.lo8 = w.lo1 = nullptr;
+      w.lo_serial = op_lo->serial;
+    }
+    const int rest = maxiter - done_its;
+    if (rest >= 8 && !w.lo8) MRSR_TRY(cg_capture(op_lo, w, 8, &w.lo8));
+    if (rest % 8 != 0 && !w.lo1) MRSR_TRY(cg_capture(op_lo, w, 1, &w.lo1));
+    const bool check = reltol > 0.0 || abstol > 0.0;
+    while (done_its < maxiter) {
+      const int nit = std::min(8, maxiter - done_its);
+      if (nit == 8)
+        MRSR_CHECK_CUDA(cudaGraphLaunch(w.lo8, st));
+      else
+        for (int k = 0; k < nit; ++k) MRSR_CHECK_CUDA(cudaGraphLaunch(w.lo1, st));
+      done_its += nit;
+      if (check && done_its < maxiter) {
+        MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+        MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+        if (h.done) break;
+      }
+    }
+  }
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(x, w.xw.p, sizeof(float2) * n, cudaMemcpyDeviceToDevice, st));
+  int err_hi = 0, err_lo = 0;
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(&h, s, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(&err_hi, op_hi->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(&err_lo, op_lo->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MRSR_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (iters_out) *iters_out = h.it;
+  if (hi_iters_out) *hi_iters_out = std::min(hi_its, h.it);
+  if (resnorm_out) *resnorm_out = h.res;
+  MRSR_TRY(device_error_status(op_hi, err_hi, st));
+  return device_error_status(op_lo, err_lo, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -16,6 +16,10 @@ struct CgWork {
   // cg_run's iterations recorded once per workspace as CUDA graphs of 8 and of 1
   // iteration (they touch only this workspace and the operator's own buffers)
   cudaGraphExec_t it8 = nullptr, it1 = nullptr;
+  // the same iterations applying another operator (the reduced-precision one of a relaxed
+  // solve) to this workspace's vectors; recorded for the operator whose serial is lo_serial
+  cudaGraphExec_t lo8 = nullptr, lo1 = nullptr;
+  uint64_t lo_serial = 0;
   cudaStream_t cap = nullptr;  // private stream the graphs are captured on
   int ensure(int64_t n, int nseg = 1);
   void drop_graphs();

@@ -103,8 +103,8 @@ __device__ __forceinline__ float2 twl(const float2* tw, int m, int) {
 // x[R2 n1 + n2] (n1 < nload) through ld(lo, li, n), applies the R1-point DFT
 // and the twiddle, and writes slot(lo, li, f1, n2).  nload = R1 or R1/2
 // (lower-half input, zero-padded embedding).
-template <class SP, int S, class LD>
-__device__ __forceinline__ void step_a(float2* sm, const Slots& sl, int NO, const float2* tw, int nload, LD ld) {
+template <class SP, int S, class SL, class LD>
+__device__ __forceinline__ void step_a(float2* sm, const SL& sl, int NO, const float2* tw, int nload, LD ld) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   const int ntask = (NO * R2) << sl.tcs;
   for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
@@ -127,8 +127,8 @@ __device__ __forceinline__ void step_a(float2* sm, const Slots& sl, int NO, cons
 // Step A with the task loop software-pipelined: the inputs of the thread's next task are
 // loaded before the current task's DFT, so their latency overlaps it.  NLOAD inputs per
 // task are read (the rest are zero), which costs NLOAD extra registers.
-template <class SP, int S, int NLOAD, class LD>
-__device__ __forceinline__ void step_a_pf(float2* sm, const Slots& sl, int NO, const float2* tw, LD ld) {
+template <class SP, int S, int NLOAD, class SL, class LD>
+__device__ __forceinline__ void step_a_pf(float2* sm, const SL& sl, int NO, const float2* tw, LD ld) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   const int ntask = (NO * R2) << sl.tcs;
   auto load = [&](int t, float2* v) {
@@ -161,8 +161,8 @@ __device__ __forceinline__ void step_a_pf(float2* sm, const Slots& sl, int NO, c
 
 // Step B.  Task (lo, li, f1) reads slot(lo, li, f1, n2) for all n2, applies
 // the R2-point DFT and hands X[f1 + R1 f2] for f2 < nkeep to st(lo, li, f1, f2, v).
-template <class SP, int S, class ST>
-__device__ __forceinline__ void step_b(float2* sm, const Slots& sl, int NO, int nkeep, ST st) {
+template <class SP, int S, class SL, class ST>
+__device__ __forceinline__ void step_b(float2* sm, const SL& sl, int NO, int nkeep, ST st) {
   constexpr int R1 = SP::R1, R2 = SP::R2;
   const int ntask = (NO * R1) << sl.tcs;
   for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
@@ -183,8 +183,8 @@ __device__ __forceinline__ void step_b(float2* sm, const Slots& sl, int NO, int 
 // Inverse transform of a spectrum held in the slot layout with frequency
 // f = f1 + R1 f2 at slot(lo, li, f1, f2).  Step A': task (lo, li, f1) runs
 // the R2-point inverse DFT over f2 (-> g1), twiddle W_L^{+f1 g1}, in place.
-template <class SP>
-__device__ __forceinline__ void inv_step_a_slots(float2* sm, const Slots& sl, int NO, const float2* tw) {
+template <class SP, class SL>
+__device__ __forceinline__ void inv_step_a_slots(float2* sm, const SL& sl, int NO, const float2* tw) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   const int ntask = (NO * R1) << sl.tcs;
   for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
@@ -204,8 +204,8 @@ __device__ __forceinline__ void inv_step_a_slots(float2* sm, const Slots& sl, in
 
 // Step B': task (lo, li, g1) runs the R1-point inverse DFT over f1 (-> g2)
 // and hands y[g1 + R2 g2] for g2 < nkeep to st(lo, li, n, v).
-template <class SP, class ST>
-__device__ __forceinline__ void inv_step_b_slots(float2* sm, const Slots& sl, int NO, int nkeep, ST st) {
+template <class SP, class SL, class ST>
+__device__ __forceinline__ void inv_step_b_slots(float2* sm, const SL& sl, int NO, int nkeep, ST st) {
   constexpr int R1 = SP::R1, R2 = SP::R2;
   const int ntask = (NO * R2) << sl.tcs;
   for (int t = threadIdx.x; t < ntask; t += blockDim.x) {

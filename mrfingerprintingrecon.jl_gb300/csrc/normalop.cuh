@@ -1,5 +1,6 @@
 // Internal state of a subspace Toeplitz normal operator handle.
 #pragma once
+#include <atomic>
 #include <memory>
 
 #include "cg.cuh"
@@ -66,6 +67,13 @@ struct mrsr_normalop {
   int FC = 1;     // Λ chunk length along the last dim
   int Cg = 1;     // coils per group
   int launches = 0;
+  // process-unique id (never reused, unlike the address): CG workspaces key the graphs they
+  // recorded with another operator's apply by it
+  uint64_t serial = next_serial();
+  static uint64_t next_serial() {
+    static std::atomic<uint64_t> n{0};
+    return ++n;
+  }
   std::shared_ptr<mrsr::LamStore> store;
   mrsr::DevBuf& kmask;
   mrsr::DevBuf& lam;

@@ -2,9 +2,11 @@
 
 ``cg`` mirrors IterativeSolvers.jl 0.9 ``cg(A, b; maxiter, reltol, abstol)``
 as the reference calls it (``test/reconstruct_radial.jl:83``, x0 = 0).
-``cg_refined`` is the mixed-precision iterative refinement (no counterpart in
-the reference): inner CG on an fp16-storage operator, outer residual with the
-float32 operator.
+``cg_relaxed`` is the same CG with its operator products switched from the
+float32 operator to a reduced-precision one once the residual is small, and
+``cg_refined`` the restarted mixed-precision iterative refinement (inner CG on a
+reduced-precision operator, outer residual with the float32 operator); neither
+has a counterpart in the reference.
 """
 import ctypes as C
 
@@ -60,6 +62,36 @@ def cg_stacked(A, b, maxiter=None, reltol=DEFAULT_RELTOL, abstol=0.0, log=False,
     if log:
         return CgResult(x, list(its), list(rns))
     return x
+
+
+class RelaxedResult(CgResult):
+    def __init__(self, x, iters, hi_iters, resnorm):
+        super().__init__(x, iters, resnorm)
+        self.hi_iters = hi_iters
+
+
+def cg_relaxed(A_lo, A_hi, b, maxiter=None, reltol=DEFAULT_RELTOL, abstol=0.0, switch=0.05, log=False, stream=None):
+    """``cg(A, vec(b); maxiter, reltol, abstol)`` with the products on the float32 ``A_hi``
+    while ||r|| > switch ||b|| and on the reduced-precision ``A_lo`` after that (one
+    recurrence, no restart).  ``log=True`` also returns the iterations, how many of them
+    ran on ``A_hi``, and the final residual norm."""
+    lib = _lib.load()
+    bi = A_hi._as_image(b)
+    x = jl_empty(bi.shape, torch.complex64)
+    if maxiter is None:
+        maxiter = A_hi.shape[1]
+    it = C.c_int(0)
+    hi = C.c_int(0)
+    rn = C.c_double(0.0)
+    _lib.check(lib.mrsr_cg_relaxed(A_lo.handle, A_hi.handle, ptr(bi), ptr(x), int(maxiter), float(reltol),
+                                   float(abstol), float(switch), C.byref(it), C.byref(hi), C.byref(rn),
+                                   stream_handle(stream)))
+    out = x
+    if isinstance(b, torch.Tensor) and b.dim() == 1:
+        out = x.permute(*reversed(range(x.dim()))).reshape(-1)
+    if log:
+        return RelaxedResult(out, it.value, hi.value, rn.value)
+    return out
 
 
 def cg_refined(A_lo, A_hi, b, inner_iters=20, max_outer=10, tol=1e-4, log=False, stream=None):

@@ -10,7 +10,7 @@ import pytest
 import scipy.linalg as sla
 
 from oracle import cbuild, grog as ogrog, nudft, trajectories as otraj
-from tests.helpers import rand_c, rel_l2
+from tests.helpers import rand_c, rel_l2, shepp_logan
 
 
 def _grog_data(N=16, Ncyc=3, Nt=40, Nc=8, seed=0):
@@ -116,24 +116,10 @@ def test_grog_gridding_matches_oracle(mr, cuda, nrep):
         assert rel_l2(got[..., 1], got[..., 0]) < 1e-5
 
 
-def _ellipse_image(N, seed):
-    """A piecewise-constant test image of random ellipses (stands in for Shepp-Logan)."""
-    rng = np.random.default_rng(seed)
-    g = np.meshgrid(np.linspace(-1, 1, N), np.linspace(-1, 1, N), indexing="ij")
-    img = np.zeros((N, N))
-    img[(g[0] / 0.69) ** 2 + (g[1] / 0.92) ** 2 <= 1] = 1.0
-    img[(g[0] / 0.66) ** 2 + ((g[1] + 0.02) / 0.87) ** 2 <= 1] = 0.2
-    for _ in range(6):
-        c = rng.uniform(-0.4, 0.4, 2)
-        ax = rng.uniform(0.05, 0.25, 2)
-        img[((g[0] - c[0]) / ax[0]) ** 2 + ((g[1] - c[1]) / ax[1]) ** 2 <= 1] += rng.uniform(-0.2, 0.3)
-    return img
-
-
 @pytest.mark.gpu
 def test_radial_grog_then_fft_normalop_recon(mr, cuda):
     """test/grog_recon.jl at its own sizes: 64^2, Nr = 128, rank 4 (two non-zero coefficient
-    images), Nt = 100 frames x 200 golden-angle spokes, 9 Gaussian coil maps.  Both the NUFFT
+    images: the modified Shepp-Logan phantom), Nt = 100 frames x 200 golden-angle spokes, 9 Gaussian coil maps.  Both the NUFFT
     reconstruction (NFFTNormalOp + cg, 20 iterations) and the GROG reconstruction (radial_grog!
     + FFTNormalOp + cg, 20 iterations, global phase slope removed as in :91-92) match the
     phantom cropped to the sampled k-space disk within the reference's rtol = 5e-2 (:95-96)."""
@@ -142,9 +128,10 @@ def test_radial_grog_then_fft_normalop_recon(mr, cuda):
     img = (Nx, Nx)
     rng = np.random.default_rng(42)
     x = np.zeros((Nx, Nx, K), dtype=np.complex64)
-    x[:, :, 0] = _ellipse_image(Nx, 1).T
+    sl = shepp_logan(Nx, oversample=4)  # the modified Shepp-Logan phantom, anti-aliased
+    x[:, :, 0] = sl.T
     x[: Nx // 2, :, 0] *= np.exp(1j * np.pi / 3)
-    x[:, :, 1] = _ellipse_image(Nx, 2)
+    x[:, :, 1] = sl
     # Gaussian coil maps centred on a 3 x 3 grid (gauss2 at Nx/8, Nx/2, 7Nx/8, width Nx/1.5)
     ii, jj = np.meshgrid(np.arange(1, Nx + 1), np.arange(1, Nx + 1), indexing="ij")
     cm = np.empty((Nx, Nx, Ncoil), dtype=np.complex64)
@@ -157,11 +144,8 @@ def test_radial_grog_then_fft_normalop_recon(mr, cuda):
     # traj_kooshball(Nr, theta = pi/2, phi = golden angle) restricted to its first two dimensions
     ag = 2 * np.pi / (1 + np.sqrt(5))
     phi = (ag * np.arange(Nt * Ncyc)).astype(np.float32).reshape(Ncyc, Nt, order="F")
-    kr = (np.arange(-(Nr - 1) / 2, (Nr - 1) / 2 + 1) / Nr).astype(np.float32)
-    trj = np.empty((2, Nr, Ncyc, Nt), dtype=np.float32)
-    trj[0] = kr[:, None, None] * np.cos(phi)[None]
-    trj[1] = kr[:, None, None] * np.sin(phi)[None]
-    trj = trj.reshape(2, Nr * Ncyc, Nt, order="F")
+    theta = np.full_like(phi, np.float32(np.pi / 2))
+    trj = np.ascontiguousarray(otraj.traj_kooshball(Nr, theta, phi)[:2]).astype(np.float32)
     U = np.linalg.svd(rand_c(rng, (Nt, K)), full_matrices=False)[0].astype(np.complex64)
     cmd = mr.to_jl(cm, torch.complex64)
     d = mr.forward_model(mr.to_jl(x, torch.complex64), trj, U, cmaps=cmd)
