@@ -38,6 +38,7 @@ DEFAULT_WORKLOAD = "radial2d_256_nt1000_nc20_k5"
 SERVED = "served_mixed_500"
 PIPE3D = "radial3d_128_nt800_nc16_k5"
 PIPEGROG = "grog_cart256_nt500_nc32_k6"
+PIPE2D = "radial2d_256_nt1000_nc20_k5_stages"
 L2_FLUSH_BYTES = 256 << 20   # > 129 MB L2
 
 
@@ -47,7 +48,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SERVED, PIPE3D, PIPEGROG])
+    p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SERVED, PIPE3D, PIPEGROG, PIPE2D])
     p.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "fp16-tc", "refined", "refined-tc"],
                    help="operator storage: fp32, fp16 (per-tile scaled half stacks and kernel); "
                         "refined (served workload only: fp16 inner CG + float32 residual steps)")
@@ -240,7 +241,7 @@ def reference_arm(args, world, rank):
         print(json.dumps({"impl": "reference", "unavailable": "the reference package has no request server; "
                           "its per-reconstruction CPU path is timed by the apply workloads"}), flush=True)
         return
-    if args.workload in (PIPE3D, PIPEGROG):
+    if args.workload in (PIPE3D, PIPEGROG, PIPE2D):
         print(json.dumps({"impl": "reference", "unavailable": "stage timings of the GPU pipeline only; the CPU "
                           "restatement is timed on the 2D apply workloads"}), flush=True)
         return
@@ -646,6 +647,10 @@ def pipeline_arm(args, world, rank, local):
       apply (float32 and fp16 storage), 20 CG iterations, refinement.  `value` = float32
       applies/s; the fp16 operator's applies/s and its difference from the float32 apply
       on the phantom are reported beside it.
+    radial2d_256_nt1000_nc20_k5_stages: the benchmark workload's other stages: Λ/kmask
+      precompute, forward model, backprojection (20 coils), 20 CG iterations.  `value` =
+      backprojections/s; the Λ/kmask stage's and the backprojection's spreading rates
+      (samples x channels per second) are reported beside it.
     grog_cart256_nt500_nc32_k6: 256^2 radial, Nt=500 x 2 spokes x 512 samples, 32 coils,
       K=6.  Stages: grog_calib, grog_gridding!, the coil-wise calibration reconstruction of
       calculate_coil_maps (32^2 region, 32 coils x 100 CG iterations), FFTNormalOp from the gridded trajectory,
@@ -702,6 +707,30 @@ def pipeline_arm(args, world, rank, local):
                  "refined_relres_after_2x20": res.resnorm, "apply_roofline": _apply_roofline(b3, ms32)}
         cfg = {"workload": PIPE3D, "img": list(img), "Nr": Nr, "Ncyc": Ncyc, "Nt": Nt, "Nc": Nc, "K": K,
                "trajectory": "koosh-ball golden means", "samples": Nr * Ncyc * Nt}
+    elif args.workload == PIPE2D:
+        N, Nr, Ncyc, Nt, Nc, K = 256, 512, 1, 1000, 20, 5
+        img = (N, N)
+        trj = mr.to_jl(tr.traj_2d_radial_goldenratio(Nr, Ncyc, Nt), torch.float32)
+        D = syn.dictionary(Nt, seed=42 + rank)
+        U = mr.to_jl(syn.basis(D, K), torch.float32)
+        cm = mr.to_jl(syn.coil_maps(img, Nc, seed=42 + rank), torch.complex64)
+        x = mr.to_jl(syn.phantom(img, D, mr.to_host(U), seed=42 + rank), torch.complex64)
+        A = mr.NFFTNormalOp(img, trj, U, cmaps=cm)                      # untimed first call
+        st["lambda_kmask"] = _wall_ms(lambda: mr.NFFTNormalOp(img, trj, U, cmaps=cm).close(), reps)
+        data = mr.forward_model(x, trj, U, cmaps=cm)
+        st["forward_model"] = _events_ms(lambda: mr.forward_model(x, trj, U, cmaps=cm), reps, stream)
+        data = syn.add_noise(data, 0.01)
+        b = mr.calculate_backprojection(data, trj, cm, U=U)
+        st["backprojection"] = _events_ms(lambda: mr.calculate_backprojection(data, trj, cm, U=U), reps, stream)
+        mr.cg(A, b, maxiter=20, reltol=0.0)
+        st["cg20"] = _events_ms(lambda: mr.cg(A, b, maxiter=20, reltol=0.0), reps, stream)
+        value, unit = 1000.0 / st["backprojection"], "backprojections/s"
+        ns = Nr * Ncyc * Nt
+        P = K * (K + 1) // 2
+        extra = {"spread_rate": {"lambda_kmask_samples_x_channels_per_s": ns * P / (st["lambda_kmask"] * 1e-3),
+                                 "backprojection_samples_x_channels_per_s": ns * Nc * K / (st["backprojection"] * 1e-3)}}
+        cfg = {"workload": PIPE2D, "img": list(img), "Nr": Nr, "Ncyc": Ncyc, "Nt": Nt, "Nc": Nc, "K": K,
+               "samples": ns}
     else:
         N, Nr, Ncyc, Nt, Nc, K = 256, 512, 2, 500, 32, 6
         img = (N, N)
@@ -766,7 +795,7 @@ def main():
         reference_arm(args, world, rank)
     elif args.workload == SERVED:
         served_arm(args, world, rank, local)
-    elif args.workload in (PIPE3D, PIPEGROG):
+    elif args.workload in (PIPE3D, PIPEGROG, PIPE2D):
         pipeline_arm(args, world, rank, local)
     else:
         gb300_arm(args, world, rank, local)
