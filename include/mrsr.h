@@ -215,6 +215,24 @@ int mrsr_grog_gridding(int ndims, const int64_t* img_shape, int64_t nr, int64_t 
                        int32_t* trj_cart_out, mrsr_stream_t stream);
 
 /* ---------------------------------------------------------------------
+ * ESPIRiT coil sensitivities: espirit(kbp, img_shape, kernel_size;
+ * eigThresh_1, eigThresh_2, nmaps) of MRICoilSensitivities.jl as
+ * calculate_coil_maps calls it (src/CoilMaps.jl:55-57, :89-91); the reference's
+ * GPU extension copies kbp to the host for it (ext/MRISubspaceReconCUDAExt/
+ * CoilMaps.jl:29-31), this runs on the device.
+ * kbp: centred calibration k-space (calib_shape..., ncoils) ComplexF32, DC at
+ * calib / 2; maps_out (img_shape..., ncoils, nmaps) ComplexF32; eig_out
+ * (img_shape..., nmaps) Float32 or NULL.  Signal subspace: singular vectors of
+ * the calibration matrix with sigma >= eig_thresh_1 * sigma_max; maps: leading
+ * eigenvectors of the image-space ESPIRiT operator, zero where the eigenvalue is
+ * below eig_thresh_2, coil 1 real and non-negative.  2D, 1..32 coils,
+ * nmaps 1..2 (else MRSR_ERR_UNSUPPORTED).  Synchronises the stream once per
+ * Jacobi sweep of the calibration SVD; asynchronous after that. */
+int mrsr_espirit(int ndims, const int64_t* img_shape, const int64_t* calib_shape, int ncoils, const float* kbp,
+                 const int64_t* kernel_size, double eig_thresh_1, double eig_thresh_2, int nmaps, float* maps_out,
+                 float* eig_out, mrsr_stream_t stream);
+
+/* ---------------------------------------------------------------------
  * cg(A, b; maxiter, reltol, abstol) with x0 = 0 as IterativeSolvers.jl 0.9
  * runs it on the LinearOperator (call sites test/*.jl, src/CoilMaps.jl:136).
  * Vectors ComplexF32; each thread sums its few elements' products in float32,

@@ -39,6 +39,7 @@ SIGNATURES = {
     "mrsr_backprojection_cartesian": [i32, i64p, i64, i64, i32, i32, p, p, p, p, i32, i32, p, p, p],
     "mrsr_forward_model": [i32, i64p, i64, i64, i32, p, p, p, i32, i32, p, p, p],
     "mrsr_grog_calib": [i32, i64, i64, i64, i32, i32, p, p, p, p],
+    "mrsr_espirit": [i32, i64p, i64p, i32, p, i64p, f64, f64, i32, p, p, p],
     "mrsr_grog_gridding": [i32, i64p, i64, i64, i64, i32, i32, p, p, p, p, p],
     "mrsr_cg": [p, p, p, i32, f64, f64, C.POINTER(i32), C.POINTER(f64), p],
     "mrsr_cg_refined": [p, p, p, p, i32, i32, f64, C.POINTER(i32), C.POINTER(f64), p],

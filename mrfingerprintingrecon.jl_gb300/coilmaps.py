@@ -11,15 +11,18 @@ and CG step is one launch for all coils, while each coil keeps its own CG iterat
 
 ``calculate_calibration_kspace`` is ``calculate_coil_maps`` up to the ESPIRiT call:
 the calibration mask and the rescaled trajectory, the coil-wise reconstruction and
-``fftshift(fft(fftshift(x)))``.  ESPIRiT itself (MRICoilSensitivities) is not part
-of this library; the reference's GPU extension also hands this k-space to it on the
-host (``espirit(Array(kbp), ...)``, ext/.../CoilMaps.jl:30), so it is returned as a
-host array.
+``fftshift(fft(fftshift(x)))``.  ``espirit`` runs ESPIRiT (MRICoilSensitivities'
+``espirit``, which the reference's GPU extension calls on the host,
+``espirit(Array(kbp), ...)``, ext/.../CoilMaps.jl:30) on the device, and
+``calculate_coil_maps`` chains the two without leaving the device.
 """
 import numpy as np
 import torch
 
-from .arrays import jl_reshape, jl_zeros, mask_u8, to_host, to_jl
+import ctypes as C
+
+from . import _lib
+from .arrays import jl_empty, jl_reshape, jl_zeros, mask_u8, ptr, stream_handle, to_host, to_jl
 from .backprojection import _is_int_traj, calculate_backprojection
 from .normalop import FFTNormalOp, NFFTNormalOp
 from .solvers import DEFAULT_RELTOL, CgBatch, cg, cg_stacked
@@ -171,3 +174,65 @@ def calculate_calibration_kspace(data, trj, img_shape, U=None, sample_mask=None,
     axes = tuple(range(len(calib_size)))
     k = np.fft.fftshift(np.fft.fftn(np.fft.fftshift(x, axes=axes), axes=axes), axes=axes)
     return k.astype(np.complex64)
+
+
+def _centred_fft(x, ndim):
+    """fftshift(fft(fftshift(x, 1:d), 1:d), 1:d) of a (calib..., Nc) device tensor."""
+    axes = tuple(range(ndim))
+    return torch.fft.fftshift(torch.fft.fftn(torch.fft.fftshift(x, dim=axes), dim=axes), dim=axes)
+
+
+def calibration_kspace_device(data, trj, img_shape, U=None, sample_mask=None, calib_size=None, Niter_cg=None,
+                              stream=None):
+    """``calculate_calibration_kspace`` without leaving the device: (calib..., Nc) complex64."""
+    if getattr(data, "ndim", None) == 4 or (isinstance(data, torch.Tensor) and data.dim() == 4):
+        data = to_jl(data, torch.complex64)
+        data = jl_reshape(data, (-1, data.shape[2], data.shape[3]))
+        t = to_host(trj) if isinstance(trj, torch.Tensor) else np.asarray(trj)
+        trj = t.reshape(t.shape[0], -1, t.shape[3], order="F")
+        if sample_mask is not None:
+            sm = to_host(sample_mask) if isinstance(sample_mask, torch.Tensor) else np.asarray(sample_mask)
+            sample_mask = sm.reshape(-1, sm.shape[-1], order="F")
+    mask, trj_c, calib_size = calibration_mask(trj, img_shape, calib_size, sample_mask)
+    x = reconstruct_coilwise(data, trj_c, calib_size, U=U, sample_mask=mask, Niter_cg=Niter_cg, stream=stream)
+    k = _centred_fft(x, len(calib_size))
+    return to_jl(k, torch.complex64)
+
+
+def espirit(kbp, img_shape, kernel_size=None, eigThresh_1=0.01, eigThresh_2=0.9, nmaps=1, eigenvalues=False,
+            stream=None):
+    """ESPIRiT maps (img..., Nc, nmaps) on the device from the centred calibration k-space
+    ``kbp`` (calib..., Nc); ``eigenvalues=True`` also returns the (img..., nmaps) eigenvalues."""
+    lib = _lib.load()
+    k = to_jl(kbp, torch.complex64)
+    img_shape = tuple(int(s) for s in img_shape)
+    d = len(img_shape)
+    calib = tuple(int(s) for s in k.shape[:d])
+    nc = int(k.shape[d])
+    if kernel_size is None:
+        kernel_size = (6,) * d
+    maps = jl_empty(img_shape + (nc, int(nmaps)), torch.complex64)
+    eig = jl_empty(img_shape + (int(nmaps),), torch.float32)
+    shp = (C.c_int64 * d)(*img_shape)
+    cal = (C.c_int64 * d)(*calib)
+    ks = (C.c_int64 * d)(*[int(v) for v in kernel_size])
+    _lib.check(lib.mrsr_espirit(d, shp, cal, nc, ptr(k), ks, float(eigThresh_1), float(eigThresh_2), int(nmaps),
+                                ptr(maps), ptr(eig), stream_handle(stream)))
+    return (maps, eig) if eigenvalues else maps
+
+
+def calculate_coil_maps(data, trj, img_shape, U=None, sample_mask=None, kernel_size=None, calib_size=None,
+                        eigThresh_1=0.01, eigThresh_2=0.9, nmaps=1, Niter_cg=None, stream=None):
+    """``calculate_coil_maps`` (src/CoilMaps.jl:32-63, :66-96; GPU ext/.../CoilMaps.jl:1-34) on
+    the device: calibration region, coil-wise reconstruction, centred FFT, ESPIRiT.  Returns
+    the reference's ``Vector`` of maps: one (img...) device array per coil (nmaps == 1) or
+    per (coil, map)."""
+    img_shape = tuple(int(s) for s in img_shape)
+    kbp = calibration_kspace_device(data, trj, img_shape, U=U, sample_mask=sample_mask, calib_size=calib_size,
+                                    Niter_cg=Niter_cg, stream=stream)
+    maps = espirit(kbp, img_shape, kernel_size=kernel_size, eigThresh_1=eigThresh_1, eigThresh_2=eigThresh_2,
+                   nmaps=nmaps, stream=stream)
+    nc = int(maps.shape[len(img_shape)])
+    if nmaps == 1:
+        return [maps[..., c, 0] for c in range(nc)]
+    return [maps[..., c, m] for c in range(nc) for m in range(int(nmaps))]

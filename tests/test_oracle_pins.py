@@ -170,3 +170,33 @@ def test_package_trajectories_match_oracle(mr):
     g1, g2 = tr.calculate_golden_means()
     o1, o2 = otraj.calculate_golden_means()
     assert abs(g1 - o1) < 1e-14 and abs(g2 - o2) < 1e-14
+
+
+def _espirit_consistent_calibration(N=64, Nc=8, calib=24, seed=0):
+    """Calibration k-space of smooth coil maps times an object, and the true maps."""
+    g = np.meshgrid(np.linspace(-1, 1, N), np.linspace(-1, 1, N), indexing="ij")
+    m = ((g[0] / 0.7) ** 2 + (g[1] / 0.85) ** 2 <= 1).astype(float) * (1 + 0.3 * g[0])
+    S = np.empty((N, N, Nc), complex)
+    for c in range(Nc):
+        a = 2 * np.pi * c / Nc
+        S[..., c] = (np.exp(-((g[0] - 1.3 * np.cos(a)) ** 2 + (g[1] - 1.3 * np.sin(a)) ** 2) / 2.0)
+                     * np.exp(1j * np.pi * 0.3 * (np.cos(a) * g[0] + np.sin(a) * g[1])))
+    S /= np.sqrt(np.sum(np.abs(S) ** 2, -1, keepdims=True))
+    X = np.fft.fftshift(np.fft.fft2(np.fft.fftshift(S * m[..., None], axes=(0, 1)), axes=(0, 1)), axes=(0, 1))
+    c0 = N // 2 - calib // 2
+    return X[c0:c0 + calib, c0:c0 + calib], S, m
+
+
+def test_espirit_oracle_recovers_known_maps():
+    """ESPIRiT's defining property (Uecker et al. 2014): on consistent calibration data the
+    true sensitivities, normalised to unit root-sum-of-squares, are eigenvalue-1
+    eigenvectors of the image-space operator, so the maps reproduce them (up to a
+    per-pixel phase, fixed here by coil 1)."""
+    from oracle import espirit as oesp
+    kbp, S, m = _espirit_consistent_calibration()
+    maps, lam = oesp.espirit(kbp, (64, 64), (6, 6))
+    obj = m > 0
+    assert lam[obj, 0].min() > 0.99
+    Sn = S * (np.conj(S[..., 0:1]) / np.abs(S[..., 0:1]))
+    err = np.linalg.norm((maps[..., 0] - Sn)[obj]) / np.linalg.norm(Sn[obj])
+    assert err < 1e-2
