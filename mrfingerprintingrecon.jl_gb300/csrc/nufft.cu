@@ -222,8 +222,316 @@ static double taps_per_cell(int d, const int64_t* M) {
 
 static unsigned spread_blocks(int64_t n) { return (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(n * 32, 256), 1), 152 * 64); }
 
+// ------------------------------------------------- tile-sorted (2D) ---
+//
+// 2D grids are spread tile by tile.  Samples are counting-sorted by the 16 x 16 tile that
+// holds their first tap; a work item is a chunk of up to kTileChunk samples of one tile
+// and one group of channels.  A CTA accumulates its item into a shared-memory window of
+// (16 + w - 1)^2 cells of 64-bit fixed-point values (shared 64-bit integer atomics are
+// native and keep their rate under contention, unlike float ones), then adds every
+// nonzero window cell to the grid with one global 64-bit atomic, a row of the window at a
+// time (coalesced).  The terms are the global kernels' terms, computed in the same order,
+// and integer sums do not depend on the order of their terms, so the grids are
+// reproducible run to run like theirs, with ~50x fewer global atomics.  A persistent grid
+// takes items from a device counter, so nothing waits for the host.
+constexpr int kTile = 16;
+constexpr int kWin = kTile + kEsWidth - 1;       // 23
+constexpr int kWinCells = kWin * kWin;           // 529
+constexpr int kTileChunk = 1024;                 // samples per work item
+constexpr int kTiledThreads = 256;
+constexpr int kTiledSmem = 8 * 2 * kWinCells * 8;  // 8 complex or 16 real channels: 67.7 KB
+
+struct TileWork {
+  int ntx, ntiles;
+  const int* order;    // sample indices sorted by tile
+  const int4* items;   // (tile, first sorted position, count, -)
+  const int* nitems;   // device: number of chunks
+  int* next;           // device work counter (zeroed before the launch)
+  int ngroups, cg;     // channel groups and channels per group
+};
+
+// home tile of every kept sample: the tile holding its first tap (l0 of es_lane_weight)
+__global__ void k_tile_home(SampleSet S, int64_t M0, int64_t M1, int ntx, int* tile_of, int* counts) {
+  const int hw = kEsWidth / 2;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < S.n; n += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t li = sample_lin(S, n);
+    int64_t l0[2];
+    const int64_t M[2] = {M0, M1};
+    for (int dd = 0; dd < 2; ++dd) {
+      const float m = (float)M[dd];
+      const float kd = S.trj[dd + 2 * li];
+      const float uh = __fmul_rn(kd, m);   // the arithmetic of es_lane_weight, operation for operation
+      const float ul = fmaf(kd, m, -uh);
+      const float f = floorf(uh);
+      const float r = __fadd_rn(__fsub_rn(uh, f), ul);
+      l0[dd] = wrap((int64_t)f - hw + (r > 0.f ? 1 : 0), M[dd]);
+    }
+    const int t = (int)(l0[0] / kTile) + ntx * (int)(l0[1] / kTile);
+    tile_of[n] = t;
+    atomicAdd(&counts[t], 1);
+  }
+}
+
+// one block: offsets of the tiles' sample lists and of their chunks; items per tile
+__global__ void __launch_bounds__(1024) k_tile_scan(const int* counts, int ntiles, int* offset, int* choff,
+                                                    int* nitems) {
+  __shared__ int s_n[1024], s_c[1024];
+  const int per = (ntiles + blockDim.x - 1) / blockDim.x;
+  const int t0 = threadIdx.x * per, t1 = min(ntiles, t0 + per);
+  int sn = 0, sc = 0;
+  for (int t = t0; t < t1; ++t) {
+    sn += counts[t];
+    sc += (counts[t] + kTileChunk - 1) / kTileChunk;
+  }
+  s_n[threadIdx.x] = sn;
+  s_c[threadIdx.x] = sc;
+  __syncthreads();
+  for (int o = 1; o < (int)blockDim.x; o <<= 1) {  // inclusive Hillis-Steele scan
+    const int an = threadIdx.x >= (unsigned)o ? s_n[threadIdx.x - o] : 0;
+    const int ac = threadIdx.x >= (unsigned)o ? s_c[threadIdx.x - o] : 0;
+    __syncthreads();
+    s_n[threadIdx.x] += an;
+    s_c[threadIdx.x] += ac;
+    __syncthreads();
+  }
+  int on = s_n[threadIdx.x] - sn, oc = s_c[threadIdx.x] - sc;
+  for (int t = t0; t < t1; ++t) {
+    offset[t] = on;
+    choff[t] = oc;
+    on += counts[t];
+    oc += (counts[t] + kTileChunk - 1) / kTileChunk;
+  }
+  if (threadIdx.x == blockDim.x - 1) *nitems = s_c[threadIdx.x];
+}
+
+__global__ void k_tile_scatter(int64_t n, const int* tile_of, const int* offset, int* cursor, int* order) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int t = tile_of[i];
+    order[offset[t] + atomicAdd(&cursor[t], 1)] = (int)i;
+  }
+}
+
+__global__ void k_tile_items(const int* counts, const int* offset, const int* choff, int ntiles, int4* items) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
+    const int c = counts[t];
+    for (int j = 0; j * kTileChunk < c; ++j)
+      items[choff[t] + j] = make_int4(t, offset[t] + j * kTileChunk, min(kTileChunk, c - j * kTileChunk), 0);
+  }
+}
+
+// Sorting and item lists of a 2D sample set on grid M0 x M1 (buffers owned by the caller).
+struct TileSort {
+  DevBuf counts, offset, choff, cursor, tile_of, order, items, nitems, next;
+  int ntx = 0, ntiles = 0;
+  int build(const SampleSet& S, int64_t M0, int64_t M1, cudaStream_t st) {
+    MRSR_REQUIRE(S.n < (1ll << 31), MRSR_ERR_UNSUPPORTED, "tiled spreading: too many samples");
+    ntx = (int)cdiv(M0, kTile);
+    ntiles = ntx * (int)cdiv(M1, kTile);
+    const int64_t maxitems = ntiles + cdiv(S.n, kTileChunk);
+    MRSR_TRY(counts.alloc(sizeof(int) * ntiles));
+    MRSR_TRY(offset.alloc(sizeof(int) * ntiles));
+    MRSR_TRY(choff.alloc(sizeof(int) * ntiles));
+    MRSR_TRY(cursor.alloc(sizeof(int) * ntiles));
+    MRSR_TRY(tile_of.alloc(sizeof(int) * S.n));
+    MRSR_TRY(order.alloc(sizeof(int) * S.n));
+    MRSR_TRY(items.alloc(sizeof(int4) * maxitems));
+    MRSR_TRY(nitems.alloc(sizeof(int)));
+    MRSR_TRY(next.alloc(sizeof(int)));
+    MRSR_CHECK_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int) * ntiles, st));
+    MRSR_CHECK_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int) * ntiles, st));
+    const unsigned gb = (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(S.n, 256), 1), 152 * 16);
+    k_tile_home<<<gb, 256, 0, st>>>(S, M0, M1, ntx, tile_of.as<int>(), counts.as<int>());
+    MRSR_LAUNCH_CHECK();
+    k_tile_scan<<<1, 1024, 0, st>>>(counts.as<int>(), ntiles, offset.as<int>(), choff.as<int>(), nitems.as<int>());
+    MRSR_LAUNCH_CHECK();
+    k_tile_scatter<<<gb, 256, 0, st>>>(S.n, tile_of.as<int>(), offset.as<int>(), cursor.as<int>(), order.as<int>());
+    MRSR_LAUNCH_CHECK();
+    const unsigned gt = (unsigned)std::max<int64_t>(cdiv(ntiles, 256), 1);
+    k_tile_items<<<gt, 256, 0, st>>>(counts.as<int>(), offset.as<int>(), choff.as<int>(), ntiles, items.as<int4>());
+    MRSR_LAUNCH_CHECK();
+    return MRSR_OK;
+  }
+  TileWork work(int ngroups, int cg, cudaStream_t st) {
+    cudaMemsetAsync(next.p, 0, sizeof(int), st);
+    return TileWork{ntx, ntiles, order.as<int>(), items.as<int4>(), nitems.as<int>(), next.as<int>(), ngroups, cg};
+  }
+};
+
+// Item loop shared by the Λ and data kernels: prep(n, li) loads what a kept sample's
+// terms need, term(ctx, channel, tap weight, out[NQ]) gives a channel's scaled term (NQ
+// parts: re, and im for complex grids); the window and flush are done here.
+template <int NQ, class Prep, class Term>
+__device__ __forceinline__ void tiled_items(const TileWork& tw, const SampleSet& S, const int64_t* M, int nch_total,
+                                            long long* gq, int64_t cells, Prep prep, Term term) {
+  extern __shared__ long long win[];  // [cg][NQ][kWinCells]
+  __shared__ int s_item;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int total = *tw.nitems * tw.ngroups;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(tw.next, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= total) break;
+    const int4 item = tw.items[it / tw.ngroups];
+    const int grp = it % tw.ngroups;
+    const int ch0 = grp * tw.cg, ncg = min(tw.cg, nch_total - ch0);
+    const int tx = item.x % tw.ntx, ty = item.x / tw.ntx;
+    const int64_t ox = (int64_t)tx * kTile, oy = (int64_t)ty * kTile;
+    for (int i = threadIdx.x; i < ncg * NQ * kWinCells; i += blockDim.x) win[i] = 0;
+    __syncthreads();
+    for (int s = warp; s < item.z; s += nwarps) {
+      const int64_t n = tw.order[item.y + s];
+      const int64_t li = sample_lin(S, n);
+      float kd[3] = {S.trj[2 * li], S.trj[2 * li + 1], 0.f};
+      float wt;
+      int64_t l0[3] = {0, 0, 0};
+      es_lane_weight(kd, M, 2, lane, &wt, l0);
+      const int lx0 = (int)(wrap(l0[0], M[0]) - ox), ly0 = (int)(wrap(l0[1], M[1]) - oy);
+      // the sort placed the first tap in this tile; a sample outside the window (which the
+      // shared arithmetic rules out) would go straight to the grid rather than out of bounds
+      const bool inwin = lx0 >= 0 && lx0 < kTile && ly0 >= 0 && ly0 < kTile;
+      auto ctx = prep(n, li);
+      for (int tt = lane; tt < kEsWidth * kEsWidth; tt += 32) {
+        const int t1 = tt % kEsWidth, t2 = tt / kEsWidth;
+        const float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
+        const int cell = (ly0 + t2) * kWin + (lx0 + t1);
+        for (int c = 0; c < ncg; ++c) {
+          float vals[NQ];
+          term(ctx, ch0 + c, w, vals);
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) {
+            const unsigned long long v = (unsigned long long)__float2ll_rn(vals[q]);
+            if (inwin)
+              atomicAdd(reinterpret_cast<unsigned long long*>(&win[(c * NQ + q) * kWinCells + cell]), v);
+            else
+              atomicAdd(reinterpret_cast<unsigned long long*>(
+                            &gq[((int64_t)(ch0 + c) * NQ + q) * cells + wrap(l0[0] + t1, M[0]) +
+                                M[0] * wrap(l0[1] + t2, M[1])]),
+                        v);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < ncg * NQ * kWinCells; i += blockDim.x) {
+      const long long v = win[i];
+      if (v == 0) continue;
+      const int cell = i % kWinCells, cq = i / kWinCells;
+      const int c = cq / NQ, q = cq - c * NQ;
+      const int64_t gx = wrap(ox + cell % kWin, M[0]), gy = wrap(oy + cell / kWin, M[1]);
+      atomicAdd(reinterpret_cast<unsigned long long*>(&gq[((int64_t)(ch0 + c) * NQ + q) * cells + gx + M[0] * gy]),
+                (unsigned long long)v);
+    }
+    __syncthreads();
+  }
+}
+
+struct LamCtx {
+  float2 u[8];
+};
+
+// the terms of k_spread_lambda: conj(U[t,k1]) U[t,k2] times (wx wy) 2^e, pairs p0 + channel
+template <int NQ>
+__global__ void __launch_bounds__(kTiledThreads) k_spread_lambda_tiled(SpreadLambdaArgs a, TileWork tw) {
+  const float sc = a.fs->scale;
+  tiled_items<NQ>(
+      tw, a.S, a.M, a.np, a.q, a.cells,
+      [&](int64_t, int64_t li) {
+        LamCtx c;
+        const int64_t t = li / a.S.ns_pf;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          c.u[k] = make_float2(0.f, 0.f);
+          if (k < a.K) {
+            if (a.u_complex)
+              c.u[k] = reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k];
+            else
+              c.u[k].x = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
+          }
+        }
+        return c;
+      },
+      [&](const LamCtx& c, int ch, float w, float* out) {
+        int p = a.p0 + ch, k2 = 0;
+        while (p > k2) {
+          p -= k2 + 1;
+          ++k2;
+        }
+        float2 u1 = make_float2(0.f, 0.f), u2 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          if (k == p) u1 = c.u[k];
+          if (k == k2) u2 = c.u[k];
+        }
+        const float ws = w * sc;
+        const float2 v = cmulc(u2, u1);  // conj(U[t,k1]) * U[t,k2]
+        out[0] = v.x * ws;
+        if (NQ == 2) out[NQ - 1] = v.y * ws;
+      });
+}
+
+struct DataCtx {
+  int64_t li, t;
+  float dcf;
+};
+
+// the terms of k_spread_data: y_c conj(U[t,k]) times (wx wy) dcf 2^e, channel = (c - c0) K + k
+__global__ void __launch_bounds__(kTiledThreads) k_spread_data_tiled(SpreadDataArgs a, TileWork tw) {
+  const float sc = a.fs->scale;
+  const int64_t ns_tot = a.S.ns_pf * a.S.nt;
+  tiled_items<2>(
+      tw, a.S, a.M, a.nc * a.K, a.q, a.cells,
+      [&](int64_t n, int64_t li) {
+        DataCtx c{li, li / a.S.ns_pf, 1.f};
+        if (a.dcf_kind == MRSR_DCF_RADIAL_3D || a.dcf_kind == MRSR_DCF_RADIAL_2D) {
+          float s2 = 0.f;
+          for (int dd = 0; dd < 2; ++dd) {
+            const float k = a.S.trj[dd + 2 * li];
+            s2 = __fadd_rn(s2, __fmul_rn(k, k));
+          }
+          c.dcf = a.dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
+        } else if (a.dcf_kind == MRSR_DCF_ARRAY) {
+          c.dcf = a.dcf[n];
+        }
+        return c;
+      },
+      [&](const DataCtx& c, int ch, float w0, float* out) {
+        float w = w0;
+        w *= c.dcf;
+        w *= sc;
+        const int cc = ch / a.K, k = ch - cc * a.K;
+        const float2 y = a.data[c.li + ns_tot * (a.c0 + cc)];
+        float2 v;
+        if (a.u_complex) {
+          v = cmulc(y, reinterpret_cast<const float2*>(a.U)[c.t + a.S.nt * k]);  // y * conj(U)
+        } else {
+          const float uu = reinterpret_cast<const float*>(a.U)[c.t + a.S.nt * k];
+          v = make_float2(y.x * uu, y.y * uu);
+        }
+        out[0] = v.x * w;
+        out[1] = v.y * w;
+      });
+}
+
+static int tiled_grid() { return 152 * 3; }
+
 int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
+  if (a.S.d == 2 && a.K <= 8) {
+    TileSort ts;
+    MRSR_TRY(ts.build(a.S, a.M[0], a.M[1], st));
+    const int cg = a.nq == 2 ? 8 : 16;
+    const TileWork tw = ts.work((int)cdiv(a.np, cg), cg, st);
+    if (a.nq == 2) {
+      MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_spread_lambda_tiled<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmem));
+      k_spread_lambda_tiled<2><<<tiled_grid(), kTiledThreads, kTiledSmem, st>>>(a, tw);
+    } else {
+      MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_spread_lambda_tiled<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmem));
+      k_spread_lambda_tiled<1><<<tiled_grid(), kTiledThreads, kTiledSmem, st>>>(a, tw);
+    }
+    MRSR_LAUNCH_CHECK();
+    return MRSR_OK;
+  }
   k_spread_lambda<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
@@ -231,6 +539,16 @@ int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
 
 int spread_data(const SpreadDataArgs& a, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
+  if (a.S.d == 2 && a.U) {  // an identity basis (U = I(nt)) has one channel per frame: global path
+    TileSort ts;
+    MRSR_TRY(ts.build(a.S, a.M[0], a.M[1], st));
+    const int cg = 8;
+    const TileWork tw = ts.work((int)cdiv((int64_t)a.nc * a.K, cg), cg, st);
+    MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_spread_data_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmem));
+    k_spread_data_tiled<<<tiled_grid(), kTiledThreads, kTiledSmem, st>>>(a, tw);
+    MRSR_LAUNCH_CHECK();
+    return MRSR_OK;
+  }
   k_spread_data<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;

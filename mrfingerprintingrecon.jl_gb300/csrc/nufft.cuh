@@ -48,10 +48,10 @@ __device__ __forceinline__ void es_lane_weight(const float* kd, const int64_t* M
   for (int dd = 0; dd < 3; ++dd) {
     if (dd < d) {
       const float m = (float)M[dd];
-      const float uh = kd[dd] * m;
-      const float ul = fmaf(kd[dd], m, -uh);
+      const float uh = __fmul_rn(kd[dd], m);   // intrinsics: no contraction, so every kernel
+      const float ul = fmaf(kd[dd], m, -uh);   // that locates a sample's first tap agrees
       const float f = floorf(uh);
-      const float r = (uh - f) + ul;
+      const float r = __fadd_rn(__fsub_rn(uh, f), ul);
       const int c = r > 0.f ? 1 : 0;
       l0[dd] = (int64_t)f - hw + c;
       if (lane / kEsWidth == dd) {
