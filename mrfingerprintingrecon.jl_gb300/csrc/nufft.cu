@@ -99,9 +99,9 @@ __device__ __forceinline__ int64_t wrap(int64_t l, int64_t M) {
 
 // --------------------------------------------------------- spreading ---
 
-// one 64-bit fixed-point term: v (already scaled by 2^e) rounded to nearest
-__device__ __forceinline__ void fx_add(long long* q, float v) {
-  atomicAdd(reinterpret_cast<unsigned long long*>(q), (unsigned long long)__float2ll_rn(v));
+// one fixed-point term: a = value * 2^(e - 21), added as round(a * 2^21)
+__device__ __forceinline__ void fx_add(long long* q, float a) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(q), (unsigned long long)fx_term(a));
 }
 
 // one warp per kept sample; lanes cover the w^d taps
@@ -225,54 +225,56 @@ static unsigned spread_blocks(int64_t n) { return (unsigned)std::min<int64_t>(st
 // ------------------------------------------------- tile-sorted (2D) ---
 //
 // 2D grids are spread tile by tile.  Samples are counting-sorted by the 16 x 16 tile that
-// holds their first tap; a work item is a chunk of up to kTileChunk samples of one tile
-// and one group of channels.  A CTA accumulates its item into a shared-memory window of
-// (16 + w - 1)^2 cells of 64-bit fixed-point values (shared 64-bit integer atomics are
-// native and keep their rate under contention, unlike float ones), then adds every
-// nonzero window cell to the grid with one global 64-bit atomic, a row of the window at a
-// time (coalesced).  The terms are the global kernels' terms, computed in the same order,
-// and integer sums do not depend on the order of their terms, so the grids are
-// reproducible run to run like theirs, with ~50x fewer global atomics.  A persistent grid
-// takes items from a device counter, so nothing waits for the host.
+// holds their first tap; a work item is a chunk of up to kChunk samples of one tile and a
+// group of P accumulator parts (a part is the real or the imaginary plane of a channel).
+// A CTA sums its item into a shared-memory window of (16 + w - 1)^2 cells x P parts, then
+// adds every nonzero window cell to the grid with one global 64-bit atomic, the lanes of a
+// warp on consecutive cells of a window row (one coalesced flush per window row and part).
+//
+// Lanes own parts, not taps: a sample's value for each part is formed once, and its 64
+// terms are that value times the separable tap weights, each added at a window offset
+// fixed at compile time.  The terms are the fixed-point terms of the global kernels
+// (|term| < 2^40) and enter the window as their two fx_split limbs, round(a) and the
+// 21-bit remainder: 32-bit shared atomics run at ~5x the rate of 64-bit ones, and the
+// limb sums of at most kChunk terms cannot overflow (|low sums| <= 2^30, |high sums| <
+// 2^30).  The flush rebuilds each window cell's exact 64-bit sum from its limbs, so every
+// grid cell is the exact integer sum of its rounded terms, whatever order the samples and
+// items land in: the grids are reproducible run to run.
 constexpr int kTile = 16;
-constexpr int kWin = kTile + kEsWidth - 1;       // 23
-constexpr int kWinCells = kWin * kWin;           // 529
-constexpr int kTileChunk = 1024;                 // samples per work item
-constexpr int kTiledThreads = 256;
-constexpr int kTiledSmem = 8 * 2 * kWinCells * 8;  // 8 complex or 16 real channels: 67.7 KB
+constexpr int kWin = kTile + kEsWidth - 1;  // 23
+constexpr int kWinCells = kWin * kWin;      // 529: odd, so the part stride is bank-conflict free
+constexpr int kChunk = 1024;                // samples per work item
+constexpr int kTiledThreads = 512;
+static_assert(kChunk * (1ll << (kFxLoBits - 1)) < (1ll << 31), "low limb sums must fit in 31 bits");
+static_assert(kChunk * (1ll << (kFxTermBits - kFxLoBits)) < (1ll << 31), "high limb sums must fit in 31 bits");
 
-struct TileWork {
-  int ntx, ntiles;
-  const int* order;    // sample indices sorted by tile
-  const int4* items;   // (tile, first sorted position, count, -)
-  const int* nitems;   // device: number of chunks
-  int* next;           // device work counter (zeroed before the launch)
-  int ngroups, cg;     // channel groups and channels per group
-};
+template <int P>
+constexpr int tiled_smem_bytes() { return 2 * P * kWinCells * (int)sizeof(int); }
 
 // home tile of every kept sample: the tile holding its first tap (l0 of es_lane_weight)
-__global__ void k_tile_home(SampleSet S, int64_t M0, int64_t M1, int ntx, int* tile_of, int* counts) {
+__global__ void k_tile_home(SampleSet S, int M0, int M1, int ntx, int* tile_of, int* counts) {
   const int hw = kEsWidth / 2;
+  const int M[2] = {M0, M1};
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < S.n; n += (int64_t)gridDim.x * blockDim.x) {
     const int64_t li = sample_lin(S, n);
-    int64_t l0[2];
-    const int64_t M[2] = {M0, M1};
+    int l0[2];
     for (int dd = 0; dd < 2; ++dd) {
       const float m = (float)M[dd];
       const float kd = S.trj[dd + 2 * li];
-      const float uh = __fmul_rn(kd, m);   // the arithmetic of es_lane_weight, operation for operation
+      const float uh = __fmul_rn(kd, m);  // the arithmetic of es_lane_weight, operation for operation
       const float ul = fmaf(kd, m, -uh);
       const float f = floorf(uh);
       const float r = __fadd_rn(__fsub_rn(uh, f), ul);
-      l0[dd] = wrap((int64_t)f - hw + (r > 0.f ? 1 : 0), M[dd]);
+      int l = ((int)f - hw + (r > 0.f ? 1 : 0)) % M[dd];
+      l0[dd] = l < 0 ? l + M[dd] : l;
     }
-    const int t = (int)(l0[0] / kTile) + ntx * (int)(l0[1] / kTile);
+    const int t = l0[0] / kTile + ntx * (l0[1] / kTile);
     tile_of[n] = t;
     atomicAdd(&counts[t], 1);
   }
 }
 
-// one block: offsets of the tiles' sample lists and of their chunks; items per tile
+// one block: offsets of the tiles' sample lists and of their chunks, and the chunk count
 __global__ void __launch_bounds__(1024) k_tile_scan(const int* counts, int ntiles, int* offset, int* choff,
                                                     int* nitems) {
   __shared__ int s_n[1024], s_c[1024];
@@ -281,7 +283,7 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const int* counts, int ntile
   int sn = 0, sc = 0;
   for (int t = t0; t < t1; ++t) {
     sn += counts[t];
-    sc += (counts[t] + kTileChunk - 1) / kTileChunk;
+    sc += (counts[t] + kChunk - 1) / kChunk;
   }
   s_n[threadIdx.x] = sn;
   s_c[threadIdx.x] = sc;
@@ -299,7 +301,7 @@ __global__ void __launch_bounds__(1024) k_tile_scan(const int* counts, int ntile
     offset[t] = on;
     choff[t] = oc;
     on += counts[t];
-    oc += (counts[t] + kTileChunk - 1) / kTileChunk;
+    oc += (counts[t] + kChunk - 1) / kChunk;
   }
   if (threadIdx.x == blockDim.x - 1) *nitems = s_c[threadIdx.x];
 }
@@ -314,240 +316,257 @@ __global__ void k_tile_scatter(int64_t n, const int* tile_of, const int* offset,
 __global__ void k_tile_items(const int* counts, const int* offset, const int* choff, int ntiles, int4* items) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles; t += gridDim.x * blockDim.x) {
     const int c = counts[t];
-    for (int j = 0; j * kTileChunk < c; ++j)
-      items[choff[t] + j] = make_int4(t, offset[t] + j * kTileChunk, min(kTileChunk, c - j * kTileChunk), 0);
+    for (int j = 0; j * kChunk < c; ++j)
+      items[choff[t] + j] = make_int4(t, offset[t] + j * kChunk, min(kChunk, c - j * kChunk), 0);
   }
 }
 
-// Sorting and item lists of a 2D sample set on grid M0 x M1 (buffers owned by the caller).
-struct TileSort {
-  DevBuf counts, offset, choff, cursor, tile_of, order, items, nitems, next;
-  int ntx = 0, ntiles = 0;
-  int build(const SampleSet& S, int64_t M0, int64_t M1, cudaStream_t st) {
-    MRSR_REQUIRE(S.n < (1ll << 31), MRSR_ERR_UNSUPPORTED, "tiled spreading: too many samples");
-    ntx = (int)cdiv(M0, kTile);
-    ntiles = ntx * (int)cdiv(M1, kTile);
-    const int64_t maxitems = ntiles + cdiv(S.n, kTileChunk);
-    MRSR_TRY(counts.alloc(sizeof(int) * ntiles));
-    MRSR_TRY(offset.alloc(sizeof(int) * ntiles));
-    MRSR_TRY(choff.alloc(sizeof(int) * ntiles));
-    MRSR_TRY(cursor.alloc(sizeof(int) * ntiles));
-    MRSR_TRY(tile_of.alloc(sizeof(int) * S.n));
-    MRSR_TRY(order.alloc(sizeof(int) * S.n));
-    MRSR_TRY(items.alloc(sizeof(int4) * maxitems));
-    MRSR_TRY(nitems.alloc(sizeof(int)));
-    MRSR_TRY(next.alloc(sizeof(int)));
-    MRSR_CHECK_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int) * ntiles, st));
-    MRSR_CHECK_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int) * ntiles, st));
-    const unsigned gb = (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(S.n, 256), 1), 152 * 16);
-    k_tile_home<<<gb, 256, 0, st>>>(S, M0, M1, ntx, tile_of.as<int>(), counts.as<int>());
-    MRSR_LAUNCH_CHECK();
-    k_tile_scan<<<1, 1024, 0, st>>>(counts.as<int>(), ntiles, offset.as<int>(), choff.as<int>(), nitems.as<int>());
-    MRSR_LAUNCH_CHECK();
-    k_tile_scatter<<<gb, 256, 0, st>>>(S.n, tile_of.as<int>(), offset.as<int>(), cursor.as<int>(), order.as<int>());
-    MRSR_LAUNCH_CHECK();
-    const unsigned gt = (unsigned)std::max<int64_t>(cdiv(ntiles, 256), 1);
-    k_tile_items<<<gt, 256, 0, st>>>(counts.as<int>(), offset.as<int>(), choff.as<int>(), ntiles, items.as<int4>());
-    MRSR_LAUNCH_CHECK();
-    return MRSR_OK;
+int TileSort::build(const SampleSet& S, int64_t M0, int64_t M1, cudaStream_t st) {
+  MRSR_REQUIRE(S.d == 2 && S.n < (1ll << 31) && M0 < (1ll << 24) && M1 < (1ll << 24), MRSR_ERR_UNSUPPORTED,
+               "tile-sorted spreading: 2D, < 2^31 samples, grid < 2^24 per dimension");
+  ntx = (int)cdiv(M0, kTile);
+  ntiles = ntx * (int)cdiv(M1, kTile);
+  m0 = (int)M0;
+  m1 = (int)M1;
+  const int64_t maxitems = ntiles + cdiv(S.n, kChunk);
+  MRSR_TRY(counts.alloc(sizeof(int) * ntiles));
+  MRSR_TRY(offset.alloc(sizeof(int) * ntiles));
+  MRSR_TRY(choff.alloc(sizeof(int) * ntiles));
+  MRSR_TRY(cursor.alloc(sizeof(int) * ntiles));
+  MRSR_TRY(tile_of.alloc(sizeof(int) * std::max<int64_t>(S.n, 1)));
+  MRSR_TRY(order.alloc(sizeof(int) * std::max<int64_t>(S.n, 1)));
+  MRSR_TRY(items.alloc(sizeof(int4) * maxitems));
+  MRSR_TRY(nitems.alloc(sizeof(int)));
+  MRSR_TRY(next.alloc(sizeof(int)));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int) * ntiles, st));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int) * ntiles, st));
+  const unsigned gb = (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(S.n, 256), 1), 152 * 16);
+  k_tile_home<<<gb, 256, 0, st>>>(S, m0, m1, ntx, tile_of.as<int>(), counts.as<int>());
+  MRSR_LAUNCH_CHECK();
+  k_tile_scan<<<1, 1024, 0, st>>>(counts.as<int>(), ntiles, offset.as<int>(), choff.as<int>(), nitems.as<int>());
+  MRSR_LAUNCH_CHECK();
+  k_tile_scatter<<<gb, 256, 0, st>>>(S.n, tile_of.as<int>(), offset.as<int>(), cursor.as<int>(), order.as<int>());
+  MRSR_LAUNCH_CHECK();
+  const unsigned gt = (unsigned)std::max<int64_t>(cdiv(ntiles, 256), 1);
+  k_tile_items<<<gt, 256, 0, st>>>(counts.as<int>(), offset.as<int>(), choff.as<int>(), ntiles, items.as<int4>());
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+struct TiledArgs {
+  SampleSet S;
+  int M0, M1;
+  int64_t cells;
+  int nparts;              // parts to spread (grid planes)
+  long long* q;            // [nparts][cells]
+  const FixedScale* fs;
+  int ntx;
+  const int* order;        // kept-sample indices sorted by home tile
+  const int4* items;       // (tile, first sorted position, count, -)
+  const int* nitems;
+  int* next;               // work counter, zeroed before the launch
+};
+
+// Part p of the Λ precompute: pair p0 + p / nq (k1 <= k2, packed k2 (k2 + 1) / 2 + k1), plane
+// p % nq; value conj(U[t,k1]) U[t,k2] 2^e (k_spread_lambda's value).
+struct LamParts {
+  const void* U;
+  int u_complex, nq, p0;
+  int64_t nt, ns_pf;
+  struct Lane {
+    int k1, k2, q;
+  };
+  __device__ Lane bind(int part) const {
+    const int ch = part / nq, q = part - ch * nq, p = p0 + ch;
+    int k2 = 0;
+    while ((k2 + 1) * (k2 + 2) / 2 <= p) ++k2;
+    return Lane{p - k2 * (k2 + 1) / 2, k2, q};
   }
-  TileWork work(int ngroups, int cg, cudaStream_t st) {
-    cudaMemsetAsync(next.p, 0, sizeof(int), st);
-    return TileWork{ntx, ntiles, order.as<int>(), items.as<int4>(), nitems.as<int>(), next.as<int>(), ngroups, cg};
+  __device__ float value(const Lane& L, int64_t, int64_t li, const float*) const {
+    const int64_t t = li / ns_pf;
+    if (u_complex) {
+      const float2* u = reinterpret_cast<const float2*>(U);
+      const float2 v = cmulc(u[t + nt * L.k2], u[t + nt * L.k1]);  // conj(U[t,k1]) * U[t,k2]
+      return L.q ? v.y : v.x;
+    }
+    const float* u = reinterpret_cast<const float*>(U);
+    return u[t + nt * L.k2] * u[t + nt * L.k1];
   }
 };
 
-// Item loop shared by the Λ and data kernels: prep(n, li) loads what a kept sample's
-// terms need, term(ctx, channel, tap weight, out[NQ]) gives a channel's scaled term (NQ
-// parts: re, and im for complex grids); the window and flush are done here.
-template <int NQ, class Prep, class Term>
-__device__ __forceinline__ void tiled_items(const TileWork& tw, const SampleSet& S, const int64_t* M, int nch_total,
-                                            long long* gq, int64_t cells, Prep prep, Term term) {
-  extern __shared__ long long win[];  // [cg][NQ][kWinCells]
+// Part p of the backprojection: channel p / 2 = (coil c0 + c) K + k, plane p % 2; value
+// y_c conj(U[t,k]) dcf (k_spread_data's value).
+struct DataParts {
+  const float2* data;
+  const void* U;
+  int u_complex, K, c0, dcf_kind;
+  const float* dcf;
+  int64_t nt, ns_pf, ns_tot;
+  struct Lane {
+    int c, k, q;
+  };
+  __device__ Lane bind(int part) const {
+    const int ch = part >> 1, c = ch / K;
+    return Lane{c, ch - c * K, part & 1};
+  }
+  __device__ float value(const Lane& L, int64_t n, int64_t li, const float* kd) const {
+    const int64_t t = li / ns_pf;
+    float w = 1.f;
+    if (dcf_kind == MRSR_DCF_RADIAL_3D || dcf_kind == MRSR_DCF_RADIAL_2D) {
+      const float s2 = __fadd_rn(__fmul_rn(kd[0], kd[0]), __fmul_rn(kd[1], kd[1]));
+      w = dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
+    } else if (dcf_kind == MRSR_DCF_ARRAY) {
+      w = dcf[n];
+    }
+    const float2 y = data[li + ns_tot * (c0 + L.c)];
+    float2 v;
+    if (u_complex) {
+      v = cmulc(y, reinterpret_cast<const float2*>(U)[t + nt * L.k]);  // y * conj(U)
+    } else {
+      const float uu = reinterpret_cast<const float*>(U)[t + nt * L.k];
+      v = make_float2(y.x * uu, y.y * uu);
+    }
+    return (L.q ? v.y : v.x) * w;
+  }
+};
+
+__device__ __forceinline__ int wrap32(int l, int M) {
+  l %= M;
+  return l < 0 ? l + M : l;
+}
+
+__device__ __noinline__ void spread_direct(long long* g, int M0, int M1, int lx0, int ly0, float v, const float* wx,
+                                           const float* wy) {
+  for (int t2 = 0; t2 < kEsWidth; ++t2) {
+    const int64_t row = (int64_t)M0 * wrap32(ly0 + t2, M1);
+    for (int t1 = 0; t1 < kEsWidth; ++t1)
+      atomicAdd(reinterpret_cast<unsigned long long*>(g + row + wrap32(lx0 + t1, M0)),
+                (unsigned long long)fx_term(v * wy[t2] * wx[t1]));
+  }
+}
+
+// Items are taken group-major (all tiles of part group 0, then group 1, ...) from a device
+// counter, so the CTAs in flight work on neighbouring tiles of one group and their flushes
+// share L2 lines.
+template <int P, class Parts>
+__global__ void __launch_bounds__(kTiledThreads, P == 16 ? 2 : 1) k_spread_tiled(TiledArgs a, Parts parts) {
+  extern __shared__ __align__(16) int win[];  // [2][P][kWinCells]: low limbs, then high limbs
+  int* wlo = win;
+  int* whi = win + P * kWinCells;
   __shared__ int s_item;
+  constexpr int SPW = 32 / P;  // samples per warp step
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int total = *tw.nitems * tw.ngroups;
+  const int slot = lane / P, part = lane % P;
+  const int nitems = *a.nitems;
+  const int ngroups = (a.nparts + P - 1) / P;
+  const int total = nitems * ngroups;
+  const int64_t M[2] = {a.M0, a.M1};
+  const float sc = a.fs->scale;
   for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(tw.next, 1);
+    if (threadIdx.x == 0) s_item = atomicAdd(a.next, 1);
     __syncthreads();
     const int it = s_item;
     if (it >= total) break;
-    const int4 item = tw.items[it / tw.ngroups];
-    const int grp = it % tw.ngroups;
-    const int ch0 = grp * tw.cg, ncg = min(tw.cg, nch_total - ch0);
-    const int tx = item.x % tw.ntx, ty = item.x / tw.ntx;
-    const int64_t ox = (int64_t)tx * kTile, oy = (int64_t)ty * kTile;
-    for (int i = threadIdx.x; i < ncg * NQ * kWinCells; i += blockDim.x) win[i] = 0;
+    const int grp = it / nitems;
+    const int4 item = a.items[it - grp * nitems];
+    const int gpart = grp * P + part;
+    const bool live_part = gpart < a.nparts;
+    const typename Parts::Lane L = parts.bind(live_part ? gpart : 0);
+    const int ox = (item.x % a.ntx) * kTile, oy = (item.x / a.ntx) * kTile;
+    int4* w4 = reinterpret_cast<int4*>(win);
+    for (int i = threadIdx.x; i < P * kWinCells / 2; i += blockDim.x) w4[i] = make_int4(0, 0, 0, 0);
     __syncthreads();
-    for (int s = warp; s < item.z; s += nwarps) {
-      const int64_t n = tw.order[item.y + s];
-      const int64_t li = sample_lin(S, n);
-      float kd[3] = {S.trj[2 * li], S.trj[2 * li + 1], 0.f};
+    for (int s0 = warp * SPW; s0 < item.z; s0 += nwarps * SPW) {
+      const bool live_s = s0 + slot < item.z;
+      const int64_t n = a.order[item.y + min(s0 + slot, item.z - 1)];
+      const int64_t li = sample_lin(a.S, n);
+      const float kd[3] = {a.S.trj[2 * li], a.S.trj[2 * li + 1], 0.f};
       float wt;
       int64_t l0[3] = {0, 0, 0};
-      es_lane_weight(kd, M, 2, lane, &wt, l0);
-      const int lx0 = (int)(wrap(l0[0], M[0]) - ox), ly0 = (int)(wrap(l0[1], M[1]) - oy);
-      // the sort placed the first tap in this tile; a sample outside the window (which the
-      // shared arithmetic rules out) would go straight to the grid rather than out of bounds
-      const bool inwin = lx0 >= 0 && lx0 < kTile && ly0 >= 0 && ly0 < kTile;
-      auto ctx = prep(n, li);
-      for (int tt = lane; tt < kEsWidth * kEsWidth; tt += 32) {
-        const int t1 = tt % kEsWidth, t2 = tt / kEsWidth;
-        const float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
-        const int cell = (ly0 + t2) * kWin + (lx0 + t1);
-        for (int c = 0; c < ncg; ++c) {
-          float vals[NQ];
-          term(ctx, ch0 + c, w, vals);
+      es_lane_weight(kd, M, 2, lane & 15, &wt, l0);
+      float wx[kEsWidth], wy[kEsWidth];
 #pragma unroll
-          for (int q = 0; q < NQ; ++q) {
-            const unsigned long long v = (unsigned long long)__float2ll_rn(vals[q]);
-            if (inwin)
-              atomicAdd(reinterpret_cast<unsigned long long*>(&win[(c * NQ + q) * kWinCells + cell]), v);
-            else
-              atomicAdd(reinterpret_cast<unsigned long long*>(
-                            &gq[((int64_t)(ch0 + c) * NQ + q) * cells + wrap(l0[0] + t1, M[0]) +
-                                M[0] * wrap(l0[1] + t2, M[1])]),
-                        v);
+      for (int j = 0; j < kEsWidth; ++j) {
+        wx[j] = __shfl_sync(0xffffffffu, wt, slot * P + j);
+        wy[j] = __shfl_sync(0xffffffffu, wt, slot * P + kEsWidth + j);
+      }
+      if (!(live_s && live_part)) continue;
+      const float v = parts.value(L, n, li, kd) * sc;
+      const int lx0 = wrap32((int)l0[0], a.M0), ly0 = wrap32((int)l0[1], a.M1);
+      const int lx = lx0 - ox, ly = ly0 - oy;
+      if ((unsigned)lx < (unsigned)kTile && (unsigned)ly < (unsigned)kTile) {
+        int* pl = wlo + part * kWinCells + ly * kWin + lx;
+        int* ph = whi + part * kWinCells + ly * kWin + lx;
+#pragma unroll
+        for (int t2 = 0; t2 < kEsWidth; ++t2) {
+          const float vy = v * wy[t2];
+#pragma unroll
+          for (int t1 = 0; t1 < kEsWidth; ++t1) {
+            int hi, lo;
+            fx_split(vy * wx[t1], hi, lo);
+            atomicAdd(pl + t2 * kWin + t1, lo);
+            atomicAdd(ph + t2 * kWin + t1, hi);
           }
         }
+      } else {
+        // the sort put the first tap in this tile (the same float arithmetic); a sample
+        // outside it would go straight to the grid rather than out of the window
+        spread_direct(a.q + (int64_t)gpart * a.cells, a.M0, a.M1, lx0, ly0, v, wx, wy);
       }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < ncg * NQ * kWinCells; i += blockDim.x) {
-      const long long v = win[i];
-      if (v == 0) continue;
-      const int cell = i % kWinCells, cq = i / kWinCells;
-      const int c = cq / NQ, q = cq - c * NQ;
-      const int64_t gx = wrap(ox + cell % kWin, M[0]), gy = wrap(oy + cell / kWin, M[1]);
-      atomicAdd(reinterpret_cast<unsigned long long*>(&gq[((int64_t)(ch0 + c) * NQ + q) * cells + gx + M[0] * gy]),
-                (unsigned long long)v);
+    const int gx = wrap32(ox + lane, a.M0);
+    for (int task = warp; task < P * kWin; task += nwarps) {
+      const int p = task / kWin, row = task - p * kWin;
+      const int gp = grp * P + p;
+      if (gp >= a.nparts || lane >= kWin) continue;
+      const int c = p * kWinCells + row * kWin + lane;
+      const long long v = (long long)whi[c] * (1ll << kFxLoBits) + (long long)wlo[c];
+      if (v != 0)
+        atomicAdd(reinterpret_cast<unsigned long long*>(a.q + (int64_t)gp * a.cells + gx +
+                                                        (int64_t)a.M0 * wrap32(oy + row, a.M1)),
+                  (unsigned long long)v);
     }
     __syncthreads();
   }
 }
 
-struct LamCtx {
-  float2 u[8];
-};
-
-// the terms of k_spread_lambda: conj(U[t,k1]) U[t,k2] times (wx wy) 2^e, pairs p0 + channel
-template <int NQ>
-__global__ void __launch_bounds__(kTiledThreads) k_spread_lambda_tiled(SpreadLambdaArgs a, TileWork tw) {
-  const float sc = a.fs->scale;
-  tiled_items<NQ>(
-      tw, a.S, a.M, a.np, a.q, a.cells,
-      [&](int64_t, int64_t li) {
-        LamCtx c;
-        const int64_t t = li / a.S.ns_pf;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          c.u[k] = make_float2(0.f, 0.f);
-          if (k < a.K) {
-            if (a.u_complex)
-              c.u[k] = reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k];
-            else
-              c.u[k].x = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
-          }
-        }
-        return c;
-      },
-      [&](const LamCtx& c, int ch, float w, float* out) {
-        int p = a.p0 + ch, k2 = 0;
-        while (p > k2) {
-          p -= k2 + 1;
-          ++k2;
-        }
-        float2 u1 = make_float2(0.f, 0.f), u2 = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          if (k == p) u1 = c.u[k];
-          if (k == k2) u2 = c.u[k];
-        }
-        const float ws = w * sc;
-        const float2 v = cmulc(u2, u1);  // conj(U[t,k1]) * U[t,k2]
-        out[0] = v.x * ws;
-        if (NQ == 2) out[NQ - 1] = v.y * ws;
-      });
+template <int P, class Parts>
+static int launch_tiled(const TiledArgs& a, const Parts& parts, cudaStream_t st) {
+  constexpr int smem = tiled_smem_bytes<P>();
+  MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_spread_tiled<P, Parts>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(a.next, 0, sizeof(int), st));
+  k_spread_tiled<P, Parts><<<152 * (P == 16 ? 2 : 1), kTiledThreads, smem, st>>>(a, parts);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
 }
 
-struct DataCtx {
-  int64_t li, t;
-  float dcf;
-};
-
-// the terms of k_spread_data: y_c conj(U[t,k]) times (wx wy) dcf 2^e, channel = (c - c0) K + k
-__global__ void __launch_bounds__(kTiledThreads) k_spread_data_tiled(SpreadDataArgs a, TileWork tw) {
-  const float sc = a.fs->scale;
-  const int64_t ns_tot = a.S.ns_pf * a.S.nt;
-  tiled_items<2>(
-      tw, a.S, a.M, a.nc * a.K, a.q, a.cells,
-      [&](int64_t n, int64_t li) {
-        DataCtx c{li, li / a.S.ns_pf, 1.f};
-        if (a.dcf_kind == MRSR_DCF_RADIAL_3D || a.dcf_kind == MRSR_DCF_RADIAL_2D) {
-          float s2 = 0.f;
-          for (int dd = 0; dd < 2; ++dd) {
-            const float k = a.S.trj[dd + 2 * li];
-            s2 = __fadd_rn(s2, __fmul_rn(k, k));
-          }
-          c.dcf = a.dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
-        } else if (a.dcf_kind == MRSR_DCF_ARRAY) {
-          c.dcf = a.dcf[n];
-        }
-        return c;
-      },
-      [&](const DataCtx& c, int ch, float w0, float* out) {
-        float w = w0;
-        w *= c.dcf;
-        w *= sc;
-        const int cc = ch / a.K, k = ch - cc * a.K;
-        const float2 y = a.data[c.li + ns_tot * (a.c0 + cc)];
-        float2 v;
-        if (a.u_complex) {
-          v = cmulc(y, reinterpret_cast<const float2*>(a.U)[c.t + a.S.nt * k]);  // y * conj(U)
-        } else {
-          const float uu = reinterpret_cast<const float*>(a.U)[c.t + a.S.nt * k];
-          v = make_float2(y.x * uu, y.y * uu);
-        }
-        out[0] = v.x * w;
-        out[1] = v.y * w;
-      });
+template <class Parts>
+static int spread_tiled(const SampleSet& S, const int64_t* M, int64_t cells, int nparts, long long* q,
+                        const FixedScale* fs, const TileSort& ts, const Parts& parts, cudaStream_t st) {
+  MRSR_REQUIRE(ts.m0 == (int)M[0] && ts.m1 == (int)M[1], MRSR_ERR_STATE, "tile sort built for another grid");
+  const TiledArgs a{S, ts.m0, ts.m1, cells, nparts, q, fs, ts.ntx,
+                    ts.order.as<int>(), ts.items.as<int4>(), ts.nitems.as<int>(), ts.next.as<int>()};
+  return nparts <= 16 ? launch_tiled<16>(a, parts, st) : launch_tiled<32>(a, parts, st);
 }
 
-static int tiled_grid() { return 152 * 3; }
-
-int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st) {
+int spread_lambda(const SpreadLambdaArgs& a, const TileSort* ts, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
-  if (a.S.d == 2 && a.K <= 8) {
-    TileSort ts;
-    MRSR_TRY(ts.build(a.S, a.M[0], a.M[1], st));
-    const int cg = a.nq == 2 ? 8 : 16;
-    const TileWork tw = ts.work((int)cdiv(a.np, cg), cg, st);
-    if (a.nq == 2) {
-      MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_spread_lambda_tiled<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmem));
-      k_spread_lambda_tiled<2><<<tiled_grid(), kTiledThreads, kTiledSmem, st>>>(a, tw);
-    } else {
-      MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_spread_lambda_tiled<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmem));
-      k_spread_lambda_tiled<1><<<tiled_grid(), kTiledThreads, kTiledSmem, st>>>(a, tw);
-    }
-    MRSR_LAUNCH_CHECK();
-    return MRSR_OK;
+  if (ts) {
+    const LamParts parts{a.U, a.u_complex, a.nq, a.p0, a.S.nt, a.S.ns_pf};
+    return spread_tiled(a.S, a.M, a.cells, a.np * a.nq, a.q, a.fs, *ts, parts, st);
   }
   k_spread_lambda<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
 }
 
-int spread_data(const SpreadDataArgs& a, cudaStream_t st) {
+int spread_data(const SpreadDataArgs& a, const TileSort* ts, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
-  if (a.S.d == 2 && a.U) {  // an identity basis (U = I(nt)) has one channel per frame: global path
-    TileSort ts;
-    MRSR_TRY(ts.build(a.S, a.M[0], a.M[1], st));
-    const int cg = 8;
-    const TileWork tw = ts.work((int)cdiv((int64_t)a.nc * a.K, cg), cg, st);
-    MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_spread_data_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, kTiledSmem));
-    k_spread_data_tiled<<<tiled_grid(), kTiledThreads, kTiledSmem, st>>>(a, tw);
-    MRSR_LAUNCH_CHECK();
-    return MRSR_OK;
+  if (ts && a.U) {
+    const DataParts parts{a.data, a.U, a.u_complex, a.K, a.c0, a.dcf_kind, a.dcf,
+                          a.S.nt, a.S.ns_pf, a.S.ns_pf * a.S.nt};
+    return spread_tiled(a.S, a.M, a.cells, 2 * a.nc * a.K, a.q, a.fs, *ts, parts, st);
   }
   k_spread_data<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
@@ -565,16 +584,16 @@ __global__ void k_absmax(const float* f, int64_t n, unsigned* amax) {
   if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(amax, __float_as_uint(m));
 }
 
-// e = 62 - ceil(log2(nterms * mult * prod amax)); e clamped so 2^e is a normal float
+// e = min(62 - ceil(log2(nterms * bound)), 40 - ceil(log2(bound))), bound = mult * prod
+// amax; e clamped so that 2^(e - 21) and 2^-e are normal floats
 __global__ void k_fixed_scale(const unsigned* amax, int nf, double mult, double nterms, FixedScale* out) {
-  double b = nterms * mult;
-  for (int i = 0; i < nf; ++i) b *= (double)__uint_as_float(amax[i]);
+  double bound = mult;
+  for (int i = 0; i < nf; ++i) bound *= (double)__uint_as_float(amax[i]);
   int e = 0;
-  if (b > 0.0) e = 62 - (int)ceil(log2(b));
-  e = max(-120, min(120, e));
-  out->scale = ldexpf(1.f, e);
-  out->pad = 0.f;
-  out->inv = ldexp(1.0, -e);
+  if (bound > 0.0) e = min(62 - (int)ceil(log2(nterms * bound)), kFxTermBits - (int)ceil(log2(bound)));
+  e = max(-100, min(120, e));
+  out->scale = ldexpf(1.f, e - kFxLoBits);
+  out->inv = ldexpf(1.f, -e);
 }
 
 int fixed_scale(const float* const* f, const int64_t* n, int nf, double mult, double nterms, FixedScale* out,
@@ -593,15 +612,21 @@ int fixed_scale(const float* const* f, const int64_t* n, int nf, double mult, do
   return MRSR_OK;
 }
 
+// int64 -> float32 without the float64 pipe: v = hi * 2^32 + lo with lo in [-2^31, 2^31)
+// (so a small negative v is lo alone, with no cancellation), each half converted in float32
+// and joined by one fma (within ~2 float32 roundings of v), then scaled by 2^-e
 __global__ void k_fixed_to_grid(const long long* q, int nq, int64_t cells, int64_t total, const FixedScale* fs,
                                 float2* out) {
-  const double inv = fs->inv;
+  const float inv = fs->inv;
+  auto cvt = [inv](long long v) {
+    const long long hi = (v + (1ll << 31)) >> 32;
+    const int lo = (int)(v - hi * 4294967296ll);
+    return __fmaf_rn((float)(int)hi, 4294967296.f, (float)lo) * inv;
+  };
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t ch = e / cells, cell = e - ch * cells;
     const long long* qc = q + ch * nq * cells + cell;
-    const float re = (float)((double)qc[0] * inv);
-    const float im = nq == 2 ? (float)((double)qc[cells] * inv) : 0.f;
-    out[e] = make_float2(re, im);
+    out[e] = make_float2(cvt(qc[0]), nq == 2 ? cvt(qc[cells]) : 0.f);
   }
 }
 
@@ -733,10 +758,10 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
   MRSR_TRY(fG.init(d, G));
   DevBuf ipsi[3];
   for (int i = 0; i < d; ++i) MRSR_TRY(es_inv_psi_table(M[i], -G[i] / 2, G[i] + 1, ipsi[i]));
-  // channel batches bounded to ~2 GB of upsampled float2 grid (plus its fixed-point accumulator)
+  // channel batches of ~2 GB of upsampled float2 grid
+  const int nq = u_complex ? 2 : 1;  // a real basis spreads real values
   const int64_t max_bytes = 2ll << 30;
   const int pb = (int)std::max<int64_t>(1, std::min<int64_t>(P, max_bytes / (mcells * (int64_t)sizeof(float2))));
-  const int nq = u_complex ? 2 : 1;  // a real basis spreads real values
   DevBuf grid, qgrid, cgrid, fsb;
   MRSR_TRY(grid.alloc(sizeof(float2) * mcells * pb));
   MRSR_TRY(qgrid.alloc(sizeof(long long) * nq * mcells * pb));
@@ -751,6 +776,8 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
     const int64_t n[2] = {nu, nu};
     MRSR_TRY(fixed_scale(f, n, 2, u_complex ? 2.0 : 1.0, (double)S.n * taps_per_cell(d, M), fsb.as<FixedScale>(), st));
   }
+  TileSort ts;
+  if (d == 2) MRSR_TRY(ts.build(S, M[0], M[1], st));
   MRSR_TRY(packed.alloc((u_complex ? 8 : 4) * (size_t)P * std::max<int64_t>(*nk_out, 1)));
   // channels in batches of pb: spread, inverse DFT on the upsampled grid, deconvolve and fold onto the 2x grid
   for (int p0 = 0; p0 < P; p0 += pb) {
@@ -758,7 +785,7 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
     MRSR_CHECK_CUDA(cudaMemsetAsync(qgrid.p, 0, sizeof(long long) * nq * mcells * np, st));
     SpreadLambdaArgs sa{S, {M[0], M[1], M[2]}, mcells, U, u_complex, K, P, p0, np, nq, qgrid.as<long long>(),
                         fsb.as<FixedScale>()};
-    MRSR_TRY(spread_lambda(sa, st));
+    MRSR_TRY(spread_lambda(sa, d == 2 ? &ts : nullptr, st));
     MRSR_TRY(fixed_to_grid(qgrid.as<long long>(), nq, mcells, np, fsb.as<FixedScale>(), grid.as<float2>(), st));
     MRSR_TRY(fM.run(grid.as<float2>(), np, +1, 1.0f, st));
     FoldArgs fa;
@@ -997,6 +1024,7 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
   MRSR_TRY(fM.init(ndims, M));
   DevBuf ipsi[3];
   for (int i = 0; i < ndims; ++i) MRSR_TRY(es_inv_psi_table(M[i], -(N[i] / 2), N[i], ipsi[i]));
+  // coil batches of ~2 GB of float2 grid
   const int64_t max_bytes = 2ll << 30;
   const int64_t per_coil = (int64_t)K * mcells * (int64_t)sizeof(float2);
   const int cc = (int)std::max<int64_t>(1, std::min<int64_t>(ncoils, max_bytes / std::max<int64_t>(per_coil, 1)));
@@ -1006,6 +1034,7 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
   // fixed-point scale: |term component| <= max|data| max|U| (x2 for complex U) x dcf bound,
   // at most ceil(w / M) taps per sample, cell and dimension
   MRSR_TRY(fsb.alloc(sizeof(FixedScale)));
+  const bool tiled = ndims == 2 && U != nullptr;  // an identity basis gives every sample one channel
   {
     const float* f[3];
     int64_t n[3];
@@ -1026,6 +1055,8 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
     }
     MRSR_TRY(fixed_scale(f, n, nf, mult, (double)sl.set.n * taps_per_cell(ndims, M), fsb.as<FixedScale>(), st));
   }
+  TileSort ts;
+  if (tiled) MRSR_TRY(ts.build(sl.set, M[0], M[1], st));
   const int64_t out_elems = nimg * K * (cmaps ? 1 : ncoils);
   if (cmaps) MRSR_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(float2) * out_elems, st));
   for (int c0 = 0; c0 < ncoils; c0 += cc) {
@@ -1033,7 +1064,7 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
     MRSR_CHECK_CUDA(cudaMemsetAsync(qgrid.p, 0, (size_t)per_coil * 2 * nc, st));
     SpreadDataArgs sa{sl.set, {M[0], M[1], M[2]}, mcells, reinterpret_cast<const float2*>(data), c0, nc, U,
                       u_is_complex, K, dcf_kind, dcf_array, qgrid.as<long long>(), fsb.as<FixedScale>()};
-    MRSR_TRY(spread_data(sa, st));
+    MRSR_TRY(spread_data(sa, tiled ? &ts : nullptr, st));
     MRSR_TRY(fixed_to_grid(qgrid.as<long long>(), 2, mcells, (int64_t)nc * K, fsb.as<FixedScale>(), grid.as<float2>(),
                            st));
     MRSR_TRY(fM.run(grid.as<float2>(), (int64_t)nc * K, +1, 1.0f, st));

@@ -68,19 +68,42 @@ __device__ __forceinline__ void es_lane_weight(const float* kd, const int64_t* M
 int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, DevBuf& out);
 
 // Fixed-point accumulation of the spread grids.  Each tap's term (a float32 product of
-// the sample value and the kernel weights) is scaled by 2^e, rounded to a 64-bit integer
-// and added to the grid with 64-bit integer atomics.  Integer addition is associative, so
-// every cell holds the exact sum of its rounded terms whatever order the samples land in:
-// the grids are bitwise reproducible run to run, and the sum carries no accumulation
-// error (a float32 atomic sum of n terms drifts by ~sqrt(n) float32 roundings of the
-// running total, a float64 one by ~n float64 roundings).  e = 62 - ceil(log2(n_terms *
-// max|term|)) from a device-side bound, so no cell can overflow, and the resolution
-// 2^-e is ~1e-19 of the largest possible cell sum.
+// the sample value and the kernel weights) is scaled by 2^e, rounded to an integer and
+// added to a 64-bit grid with integer atomics.  Integer addition is associative, so every
+// cell holds the exact sum of its rounded terms whatever order the samples land in: the
+// grids are bitwise reproducible run to run, and the sum carries no accumulation error (a
+// float32 atomic sum of n terms drifts by ~sqrt(n) float32 roundings of the running total,
+// a float64 one by ~n float64 roundings).  e = min(62 - ceil(log2(n_terms max|term|)),
+// 40 - ceil(log2(max|term|))) from a device-side bound: no cell sum can leave 63 bits, no
+// term reaches 2^40 (a resolution of 2^-40 of the largest term, far below float32's).
+//
+// A term is never converted to int64 by the float-to-int64 instruction, which runs on this
+// GPU's narrow float64 pipe (~0.4 T/s, it bounded the spreading kernels).  With a = term *
+// 2^-21 (|a| < 2^19) it is split as round(a) * 2^21 + round((a - round(a)) * 2^21), both
+// parts rounded by adding 1.5 * 2^23 in float32 (the sum's low mantissa bits are then the
+// rounded integer), which takes two float adds, one fma and two integer subtractions.
+constexpr int kFxLoBits = 21;
+constexpr int kFxTermBits = 40;
+
 struct FixedScale {
-  float scale;   // 2^e
-  float pad;
-  double inv;    // 2^-e
+  float scale;   // 2^(e - kFxLoBits): value * scale = a
+  float inv;     // 2^-e
 };
+
+__device__ __forceinline__ void fx_split(float a, int& hi, int& lo) {
+  constexpr float kMagic = 12582912.f;  // 1.5 * 2^23
+  constexpr int kMagicBits = 0x4B400000;
+  const float s1 = __fadd_rn(a, kMagic);
+  hi = __float_as_int(s1) - kMagicBits;                    // round(a), |a| < 2^22
+  const float d = __fsub_rn(a, __fsub_rn(s1, kMagic));     // a - round(a), exact, |d| <= 1/2
+  lo = __float_as_int(__fmaf_rn(d, (float)(1 << kFxLoBits), kMagic)) - kMagicBits;  // |lo| <= 2^20
+}
+
+__device__ __forceinline__ long long fx_term(float a) {
+  int hi, lo;
+  fx_split(a, hi, lo);
+  return (long long)hi * (1ll << kFxLoBits) + lo;
+}
 
 // grid[ch][part][cell] (part: re, and im for complex grids) += value(ch, n) * phi taps,
 // cells column-major on dims M, in units of 2^-e.
@@ -96,7 +119,18 @@ struct SpreadLambdaArgs {
   long long* q;       // [np][nq][cells]
   const FixedScale* fs;
 };
-int spread_lambda(const SpreadLambdaArgs& a, cudaStream_t st);
+// Samples of a 2D set counting-sorted by the 16 x 16 tile of the grid M0 x M1 that holds
+// their first tap, in chunks of at most 1024 samples (the work items of the tile-sorted
+// spreading kernels).  Built once per sample set and grid, shared by every spread of it.
+struct TileSort {
+  DevBuf counts, offset, choff, cursor, tile_of, order, items, nitems, next;
+  int ntx = 0, ntiles = 0, m0 = 0, m1 = 0;
+  int build(const SampleSet& S, int64_t M0, int64_t M1, cudaStream_t st);
+};
+
+// ts: tile sort of a.S on a.M (2D), or null for the global kernel (one warp per sample,
+// every term a global atomic; used for 3D).
+int spread_lambda(const SpreadLambdaArgs& a, const TileSort* ts, cudaStream_t st);
 
 struct SpreadDataArgs {
   SampleSet S;
@@ -110,7 +144,7 @@ struct SpreadDataArgs {
   long long* q;         // [(c - c0) * K + k][2][cells]
   const FixedScale* fs;
 };
-int spread_data(const SpreadDataArgs& a, cudaStream_t st);
+int spread_data(const SpreadDataArgs& a, const TileSort* ts, cudaStream_t st);
 
 // Scale of a fixed-point grid: every term's components are bounded by `mult` times the
 // product of the largest absolute entries of the nf (<= 3) factor arrays f[i] (n[i]
