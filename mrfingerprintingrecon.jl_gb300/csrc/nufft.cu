@@ -4,7 +4,10 @@
 //  * calculate_backprojection (src/BackProjection.jl:23-102, ext/.../BackProjection.jl:1-71)
 //  * the forward model of the reference tests (test/reconstruct_radial.jl:62-74)
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "normalop.cuh"
@@ -15,6 +18,11 @@ namespace mrsr {
 // ------------------------------------------------------------ samples ---
 
 __device__ __forceinline__ int64_t sample_lin(const SampleSet& S, int64_t i) { return S.list ? S.list[i] - 1 : i; }
+
+// frame of linear sample index li (32-bit division when the operands allow)
+__device__ __forceinline__ int64_t frame_of(int64_t li, int64_t ns_pf) {
+  return (li | ns_pf) < (1ll << 31) ? (int64_t)((unsigned)li / (unsigned)ns_pf) : li / ns_pf;
+}
 
 __global__ void k_mask_to_flags(const uint8_t* mask, int64_t n, uint8_t* flags) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -75,20 +83,45 @@ static void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w
   }
 }
 
-// psi_hat(j) = (w/2) int_{-1}^{1} phi(z) cos(pi j w z / M) dz
-int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, DevBuf& out) {
-  static std::vector<double> gx, gw;
-  if (gx.empty()) gauss_legendre(200, gx, gw);
+// psi_hat(j) = (w/2) int_{-1}^{1} phi(z) cos(pi j w z / M) dz.  The tables are cached per
+// (device, M, jmin, count) for the life of the process (a few KB each, never freed): one
+// costs count x 200 host cosines, and every kernel build, backprojection and forward model
+// needs d of them.
+int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, const float** out) {
+  static std::mutex mu;
+  static std::map<std::array<int64_t, 4>, float*> cache;
+  static std::vector<double> gx, gw, gphi;
+  int dev = 0;
+  MRSR_CHECK_CUDA(cudaGetDevice(&dev));
+  const std::array<int64_t, 4> key{dev, M, jmin, count};
+  std::lock_guard<std::mutex> lock(mu);
+  const auto it = cache.find(key);
+  if (it != cache.end()) {
+    *out = it->second;
+    return MRSR_OK;
+  }
+  if (gx.empty()) {
+    gauss_legendre(200, gx, gw);
+    gphi.resize(gx.size());
+    for (size_t q = 0; q < gx.size(); ++q) gphi[q] = gw[q] * es_phi_host(gx[q]);
+  }
   std::vector<float> h(count);
   const double hw = 0.5 * kEsWidth;
   for (int64_t i = 0; i < count; ++i) {
     const double j = (double)(jmin + i);
     double s = 0.0;
-    for (size_t q = 0; q < gx.size(); ++q) s += gw[q] * es_phi_host(gx[q]) * std::cos(M_PI * j * kEsWidth * gx[q] / (double)M);
+    for (size_t q = 0; q < gx.size(); ++q) s += gphi[q] * std::cos(M_PI * j * kEsWidth * gx[q] / (double)M);
     h[i] = (float)(1.0 / (hw * s));
   }
-  MRSR_TRY(out.alloc(sizeof(float) * count));
-  MRSR_TRY(copy_h2d(out.p, h.data(), sizeof(float) * count));
+  float* d = nullptr;
+  MRSR_CHECK_CUDA(cudaMalloc(&d, sizeof(float) * std::max<int64_t>(count, 1)));
+  const cudaError_t e = cudaMemcpy(d, h.data(), sizeof(float) * count, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    MRSR_CHECK_CUDA(e);
+  }
+  cache[key] = d;
+  *out = d;
   return MRSR_OK;
 }
 
@@ -104,109 +137,122 @@ __device__ __forceinline__ void fx_add(long long* q, float a) {
   atomicAdd(reinterpret_cast<unsigned long long*>(q), (unsigned long long)fx_term(a));
 }
 
-// one warp per kept sample; lanes cover the w^d taps
-__global__ void __launch_bounds__(256) k_spread_lambda(SpreadLambdaArgs a) {
+__device__ __forceinline__ int wrap32(int l, int M) {
+  l %= M;
+  return l < 0 ? l + M : l;
+}
+
+// Taps of one sample owned by a lane of its warp: lane = t1 + 8 * t2a (t1 < 8, t2a < 4), and
+// its J = w^d / 32 taps are t2 = t2a + 4 (j & 1), t3 = j >> 1.  Weights (times `sc`) and
+// grid cells (< 2^32, checked by the launchers) are formed once per sample, with 32-bit wraps.
+template <int J>
+__device__ __forceinline__ void lane_taps(const SampleSet& S, const int64_t* M, int64_t li, int lane, float sc,
+                                          float* w, unsigned* cell) {
+  constexpr int d = J == 2 ? 2 : 3;
+  float kd[3] = {0.f, 0.f, 0.f};
+  for (int dd = 0; dd < d; ++dd) kd[dd] = S.trj[dd + (int64_t)d * li];
+  float wt;
+  int64_t l0[3] = {0, 0, 0};
+  es_lane_weight(kd, M, d, lane, &wt, l0);
+  const int t1 = lane & 7, t2a = lane >> 3;
+  const float wx = __shfl_sync(0xffffffffu, wt, t1) * sc;
+  const unsigned x = wrap32((int)l0[0] + t1, (int)M[0]);
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const int t2 = t2a + 4 * (j & 1), t3 = j >> 1;
+    float wj = wx * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
+    unsigned c = x + (unsigned)M[0] * (unsigned)wrap32((int)l0[1] + t2, (int)M[1]);
+    if (d == 3) {
+      wj *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
+      c += (unsigned)(M[0] * M[1]) * (unsigned)wrap32((int)l0[2] + t3, (int)M[2]);
+    }
+    w[j] = wj;
+    cell[j] = c;
+  }
+}
+
+// One warp per kept sample (the 3D grids; tile-sorted kernels below do 2D).  A channel's
+// value is formed once per sample; its terms go to the grid as 64-bit atomics.
+template <int J>
+__global__ void __launch_bounds__(256, 2) k_spread_lambda(SpreadLambdaArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int d = a.S.d;
-  const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
   const float sc = a.fs->scale;
   const int64_t chs = (int64_t)a.nq * a.cells;
   for (int64_t n = warp; n < a.S.n; n += nwarps) {
     const int64_t li = sample_lin(a.S, n);
-    const int64_t t = li / a.S.ns_pf;
-    float kd[3] = {0.f, 0.f, 0.f};
-    for (int dd = 0; dd < d; ++dd) kd[dd] = a.S.trj[dd + (int64_t)d * li];
-    float wt;
-    int64_t l0[3] = {0, 0, 0};
-    es_lane_weight(kd, a.M, d, lane, &wt, l0);
-    // basis values of this frame (the tap weight below carries the 2^e scale)
-    float2 u[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      u[k] = make_float2(0.f, 0.f);
-      if (k < a.K) {
-        if (a.u_complex)
-          u[k] = reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k];
-        else
-          u[k].x = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
+    const int64_t t = frame_of(li, a.S.ns_pf);
+    float w[J];
+    unsigned cell[J];
+    lane_taps<J>(a.S, a.M, li, lane, sc, w, cell);
+    for (int ch = 0; ch < a.np; ++ch) {
+      const int p = a.p0 + ch;
+      int k2 = 0;
+      while ((k2 + 1) * (k2 + 2) / 2 <= p) ++k2;
+      const int k1 = p - k2 * (k2 + 1) / 2;
+      float2 v;  // conj(U[t,k1]) * U[t,k2]
+      if (a.u_complex) {
+        const float2* u = reinterpret_cast<const float2*>(a.U);
+        v = cmulc(u[t + a.S.nt * k2], u[t + a.S.nt * k1]);
+      } else {
+        const float* u = reinterpret_cast<const float*>(a.U);
+        v = make_float2(u[t + a.S.nt * k2] * u[t + a.S.nt * k1], 0.f);
       }
-    }
-    for (int tt = lane; tt < ntap; tt += 32) {
-      const int t1 = tt % kEsWidth, t2 = (tt / kEsWidth) % kEsWidth, t3 = tt / (kEsWidth * kEsWidth);
-      float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
-      if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
-      w *= sc;
-      int64_t cell = wrap(l0[0] + t1, a.M[0]) + a.M[0] * wrap(l0[1] + t2, a.M[1]);
-      if (d == 3) cell += a.M[0] * a.M[1] * wrap(l0[2] + t3, a.M[2]);
-      int p = 0;
+      long long* q = a.q + (int64_t)ch * chs;
 #pragma unroll
-      for (int k2 = 0; k2 < 8; ++k2) {
-#pragma unroll
-        for (int k1 = 0; k1 <= k2; ++k1) {
-          if (k2 < a.K && p >= a.p0 && p < a.p0 + a.np) {
-            const float2 v = cmulc(u[k2], u[k1]);  // conj(U[t,k1]) * U[t,k2]
-            long long* q = a.q + (int64_t)(p - a.p0) * chs + cell;
-            fx_add(q, v.x * w);
-            if (a.nq == 2) fx_add(q + a.cells, v.y * w);
-          }
-          ++p;
-        }
+      for (int j = 0; j < J; ++j) {
+        fx_add(q + cell[j], v.x * w[j]);
+        if (a.nq == 2) fx_add(q + a.cells + cell[j], v.y * w[j]);
       }
     }
   }
 }
 
-__global__ void __launch_bounds__(256) k_spread_data(SpreadDataArgs a) {
+template <int J>
+__global__ void __launch_bounds__(256, 2) k_spread_data(SpreadDataArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int d = a.S.d;
-  const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
+  const int d = J == 2 ? 2 : 3;
   const float sc = a.fs->scale;
+  const int64_t ns_tot = a.S.ns_pf * a.S.nt;
   for (int64_t n = warp; n < a.S.n; n += nwarps) {
     const int64_t li = sample_lin(a.S, n);
-    const int64_t t = li / a.S.ns_pf;
-    float kd[3] = {0.f, 0.f, 0.f};
-    for (int dd = 0; dd < d; ++dd) kd[dd] = a.S.trj[dd + (int64_t)d * li];
+    const int64_t t = frame_of(li, a.S.ns_pf);
     float dcf = 1.f;
     if (a.dcf_kind == MRSR_DCF_RADIAL_3D || a.dcf_kind == MRSR_DCF_RADIAL_2D) {
       float s2 = 0.f;
-      for (int dd = 0; dd < d; ++dd) s2 = __fadd_rn(s2, __fmul_rn(kd[dd], kd[dd]));
+      for (int dd = 0; dd < d; ++dd) {
+        const float k = a.S.trj[dd + (int64_t)d * li];
+        s2 = __fadd_rn(s2, __fmul_rn(k, k));
+      }
       dcf = a.dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
     } else if (a.dcf_kind == MRSR_DCF_ARRAY) {
       dcf = a.dcf[n];
     }
-    float wt;
-    int64_t l0[3] = {0, 0, 0};
-    es_lane_weight(kd, a.M, d, lane, &wt, l0);
-    const int64_t ns_tot = a.S.ns_pf * a.S.nt;
-    for (int tt = lane; tt < ntap; tt += 32) {
-      const int t1 = tt % kEsWidth, t2 = (tt / kEsWidth) % kEsWidth, t3 = tt / (kEsWidth * kEsWidth);
-      float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
-      if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
-      w *= dcf;
-      w *= sc;
-      int64_t cell = wrap(l0[0] + t1, a.M[0]) + a.M[0] * wrap(l0[1] + t2, a.M[1]);
-      if (d == 3) cell += a.M[0] * a.M[1] * wrap(l0[2] + t3, a.M[2]);
-      for (int c = 0; c < a.nc; ++c) {
-        const float2 y = a.data[li + ns_tot * (a.c0 + c)];
-        const int kb = a.U ? 0 : (int)t;               // U = I(nt): only coefficient t
-        const int ke = a.U ? a.K : (int)t + 1;
-        for (int k = kb; k < ke; ++k) {
-          float2 v;
-          if (!a.U) {
-            v = y;
-          } else if (a.u_complex) {
-            v = cmulc(y, reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k]);  // y * conj(U)
-          } else {
-            const float uu = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
-            v = make_float2(y.x * uu, y.y * uu);
-          }
-          long long* q = a.q + ((int64_t)c * a.K + k) * 2 * a.cells + cell;
-          fx_add(q, v.x * w);
-          fx_add(q + a.cells, v.y * w);
+    float w[J];
+    unsigned cell[J];
+    lane_taps<J>(a.S, a.M, li, lane, sc * dcf, w, cell);
+    const int kb = a.U ? 0 : (int)t;  // U = I(nt): only coefficient t
+    const int ke = a.U ? a.K : (int)t + 1;
+    for (int c = 0; c < a.nc; ++c) {
+      const float2 y = a.data[li + ns_tot * (a.c0 + c)];
+      for (int k = kb; k < ke; ++k) {
+        float2 v;
+        if (!a.U) {
+          v = y;
+        } else if (a.u_complex) {
+          v = cmulc(y, reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k]);  // y * conj(U)
+        } else {
+          const float uu = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
+          v = make_float2(y.x * uu, y.y * uu);
+        }
+        long long* q = a.q + ((int64_t)c * a.K + k) * 2 * a.cells;
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+          fx_add(q + cell[j], v.x * w[j]);
+          fx_add(q + a.cells + cell[j], v.y * w[j]);
         }
       }
     }
@@ -224,10 +270,10 @@ static unsigned spread_blocks(int64_t n) { return (unsigned)std::min<int64_t>(st
 
 // ------------------------------------------------- tile-sorted (2D) ---
 //
-// 2D grids are spread tile by tile.  Samples are counting-sorted by the 16 x 16 tile that
+// 2D grids are spread tile by tile.  Samples are counting-sorted by the 12 x 12 tile that
 // holds their first tap; a work item is a chunk of up to kChunk samples of one tile and a
 // group of P accumulator parts (a part is the real or the imaginary plane of a channel).
-// A CTA sums its item into a shared-memory window of (16 + w - 1)^2 cells x P parts, then
+// A CTA sums its item into a shared-memory window of (12 + w - 1)^2 cells x P parts, then
 // adds every nonzero window cell to the grid with one global 64-bit atomic, the lanes of a
 // warp on consecutive cells of a window row (one coalesced flush per window row and part).
 //
@@ -240,9 +286,9 @@ static unsigned spread_blocks(int64_t n) { return (unsigned)std::min<int64_t>(st
 // 2^30).  The flush rebuilds each window cell's exact 64-bit sum from its limbs, so every
 // grid cell is the exact integer sum of its rounded terms, whatever order the samples and
 // items land in: the grids are reproducible run to run.
-constexpr int kTile = 16;
-constexpr int kWin = kTile + kEsWidth - 1;  // 23
-constexpr int kWinCells = kWin * kWin;      // 529: odd, so the part stride is bank-conflict free
+constexpr int kTile = 12;
+constexpr int kWin = kTile + kEsWidth - 1;  // 19
+constexpr int kWinCells = kWin * kWin;      // 361: odd, so the part stride is bank-conflict free
 constexpr int kChunk = 1024;                // samples per work item
 constexpr int kTiledThreads = 512;
 static_assert(kChunk * (1ll << (kFxLoBits - 1)) < (1ll << 31), "low limb sums must fit in 31 bits");
@@ -383,7 +429,7 @@ struct LamParts {
     return Lane{p - k2 * (k2 + 1) / 2, k2, q};
   }
   __device__ float value(const Lane& L, int64_t, int64_t li, const float*) const {
-    const int64_t t = li / ns_pf;
+    const int64_t t = frame_of(li, ns_pf);
     if (u_complex) {
       const float2* u = reinterpret_cast<const float2*>(U);
       const float2 v = cmulc(u[t + nt * L.k2], u[t + nt * L.k1]);  // conj(U[t,k1]) * U[t,k2]
@@ -410,7 +456,7 @@ struct DataParts {
     return Lane{c, ch - c * K, part & 1};
   }
   __device__ float value(const Lane& L, int64_t n, int64_t li, const float* kd) const {
-    const int64_t t = li / ns_pf;
+    const int64_t t = frame_of(li, ns_pf);
     float w = 1.f;
     if (dcf_kind == MRSR_DCF_RADIAL_3D || dcf_kind == MRSR_DCF_RADIAL_2D) {
       const float s2 = __fadd_rn(__fmul_rn(kd[0], kd[0]), __fmul_rn(kd[1], kd[1]));
@@ -430,10 +476,6 @@ struct DataParts {
   }
 };
 
-__device__ __forceinline__ int wrap32(int l, int M) {
-  l %= M;
-  return l < 0 ? l + M : l;
-}
 
 __device__ __noinline__ void spread_direct(long long* g, int M0, int M1, int lx0, int ly0, float v, const float* wx,
                                            const float* wy) {
@@ -449,7 +491,7 @@ __device__ __noinline__ void spread_direct(long long* g, int M0, int M1, int lx0
 // counter, so the CTAs in flight work on neighbouring tiles of one group and their flushes
 // share L2 lines.
 template <int P, class Parts>
-__global__ void __launch_bounds__(kTiledThreads, P == 16 ? 2 : 1) k_spread_tiled(TiledArgs a, Parts parts) {
+__global__ void __launch_bounds__(kTiledThreads, 2) k_spread_tiled(TiledArgs a, Parts parts) {
   extern __shared__ __align__(16) int win[];  // [2][P][kWinCells]: low limbs, then high limbs
   int* wlo = win;
   int* whi = win + P * kWinCells;
@@ -503,7 +545,7 @@ __global__ void __launch_bounds__(kTiledThreads, P == 16 ? 2 : 1) k_spread_tiled
 #pragma unroll
           for (int t1 = 0; t1 < kEsWidth; ++t1) {
             int hi, lo;
-            fx_split(vy * wx[t1], hi, lo);
+            fx_split_prod(vy, wx[t1], hi, lo);
             atomicAdd(pl + t2 * kWin + t1, lo);
             atomicAdd(ph + t2 * kWin + t1, hi);
           }
@@ -536,7 +578,7 @@ static int launch_tiled(const TiledArgs& a, const Parts& parts, cudaStream_t st)
   constexpr int smem = tiled_smem_bytes<P>();
   MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_spread_tiled<P, Parts>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   MRSR_CHECK_CUDA(cudaMemsetAsync(a.next, 0, sizeof(int), st));
-  k_spread_tiled<P, Parts><<<152 * (P == 16 ? 2 : 1), kTiledThreads, smem, st>>>(a, parts);
+  k_spread_tiled<P, Parts><<<152 * 2, kTiledThreads, smem, st>>>(a, parts);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
 }
@@ -556,7 +598,11 @@ int spread_lambda(const SpreadLambdaArgs& a, const TileSort* ts, cudaStream_t st
     const LamParts parts{a.U, a.u_complex, a.nq, a.p0, a.S.nt, a.S.ns_pf};
     return spread_tiled(a.S, a.M, a.cells, a.np * a.nq, a.q, a.fs, *ts, parts, st);
   }
-  k_spread_lambda<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+  MRSR_REQUIRE(a.cells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "spreading grid of 2^32 cells or more");
+  if (a.S.d == 2)
+    k_spread_lambda<2><<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+  else
+    k_spread_lambda<16><<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
 }
@@ -568,7 +614,11 @@ int spread_data(const SpreadDataArgs& a, const TileSort* ts, cudaStream_t st) {
                           a.S.nt, a.S.ns_pf, a.S.ns_pf * a.S.nt};
     return spread_tiled(a.S, a.M, a.cells, 2 * a.nc * a.K, a.q, a.fs, *ts, parts, st);
   }
-  k_spread_data<<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+  MRSR_REQUIRE(a.cells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "spreading grid of 2^32 cells or more");
+  if (a.S.d == 2)
+    k_spread_data<2><<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+  else
+    k_spread_data<16><<<spread_blocks(a.S.n), 256, 0, st>>>(a);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
 }
@@ -642,27 +692,44 @@ int fixed_to_grid(const long long* q, int nq, int64_t cells, int64_t nch, const 
 // ----------------------------------------------------------- kmask ---
 
 // Gaussian-footprint mask: cells i0-3 .. i0+4 (mod G) per dimension around
-// i0 = floor(fl32(-k * G)) for every kept sample (src/NFFTNormalOp.jl:106-118).
-__global__ void k_kmask_mark(SampleSet S, int64_t G0, int64_t G1, int64_t G2, uint8_t* flags) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+// i0 = floor(fl32(-k * G)) for every kept sample (src/NFFTNormalOp.jl:106-118).  The union
+// of the boxes is the seed set {i0} dilated by the box: cell j is marked iff some seed lies
+// in j-4 .. j+3 along every dimension.  One byte store per sample marks the seeds, then one
+// pass per dimension ORs each cell's 8 neighbours along it (separable, exact for boolean
+// masks), instead of 8^d scattered byte stores per sample.
+__global__ void k_kmask_seed(SampleSet S, int64_t G0, int64_t G1, int64_t G2, uint8_t* seeds) {
   const int d = S.d;
-  const int ntap = d == 2 ? 64 : 512;
-  const int64_t G[3] = {G0, G1, G2};
-  for (int64_t n = warp; n < S.n; n += nwarps) {
+  const int G[3] = {(int)G0, (int)G1, (int)G2};
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < S.n; n += (int64_t)gridDim.x * blockDim.x) {
     const int64_t li = sample_lin(S, n);
-    int64_t i0[3] = {0, 0, 0};
+    int64_t cell = 0, stride = 1;
     for (int dd = 0; dd < d; ++dd) {
       const float p = __fmul_rn(-S.trj[dd + (int64_t)d * li], (float)G[dd]);
-      i0[dd] = (int64_t)floorf(p);
+      int l = (int)floorf(p) % G[dd];
+      if (l < 0) l += G[dd];
+      cell += (int64_t)l * stride;
+      stride *= G[dd];
     }
-    for (int tt = lane; tt < ntap; tt += 32) {
-      const int t1 = tt % 8, t2 = (tt / 8) % 8, t3 = tt / 64;
-      int64_t cell = wrap(i0[0] - 3 + t1, G0) + G0 * wrap(i0[1] - 3 + t2, G1);
-      if (d == 3) cell += G0 * G1 * wrap(i0[2] - 3 + t3, G2);
-      flags[cell] = 1;
+    seeds[cell] = 1;
+  }
+}
+
+// out[j] = OR of in[j + s], s = -4 .. 3 (mod G) along dimension `axis`
+__global__ void k_kmask_dilate(const uint8_t* in, int64_t G0, int64_t G1, int64_t G2, int axis, uint8_t* out) {
+  const int64_t total = G0 * G1 * G2;
+  const int64_t stride = axis == 0 ? 1 : (axis == 1 ? G0 : G0 * G1);
+  const int64_t Ga = axis == 0 ? G0 : (axis == 1 ? G1 : G2);
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = (c / stride) % Ga;
+    const int64_t base = c - j * stride;
+    uint8_t v = 0;
+#pragma unroll
+    for (int s = -4; s <= 3; ++s) {
+      int64_t k = (j + s) % Ga;
+      if (k < 0) k += Ga;
+      v |= in[base + k * stride];
     }
+    out[c] = v ? 1 : 0;
   }
 }
 
@@ -742,12 +809,22 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
   MRSR_REQUIRE(S.n > 0, MRSR_ERR_ARG, "AssertionError: Mask removes all samples, cannot compute kernel.");
   // kmask
   {
-    DevBuf flags;
+    DevBuf flags, tmp;
     MRSR_TRY(flags.alloc(gcells));
+    MRSR_TRY(tmp.alloc(gcells));
     MRSR_CHECK_CUDA(cudaMemsetAsync(flags.p, 0, gcells, st));
-    k_kmask_mark<<<spread_blocks(S.n), 256, 0, st>>>(S, G[0], G[1], d == 3 ? G[2] : 1, flags.as<uint8_t>());
+    const int64_t G2 = d == 3 ? G[2] : 1;
+    k_kmask_seed<<<(unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(S.n, 256), 1), 152 * 64), 256, 0, st>>>(
+        S, G[0], G[1], G2, flags.as<uint8_t>());
     MRSR_LAUNCH_CHECK();
-    MRSR_TRY(compact_nonzero(flags.as<uint8_t>(), gcells, kmask, nk_out, st));
+    uint8_t* src = flags.as<uint8_t>();
+    uint8_t* dst = tmp.as<uint8_t>();
+    for (int ax = 0; ax < d; ++ax) {
+      k_kmask_dilate<<<grid1d(gcells), 256, 0, st>>>(src, G[0], G[1], G2, ax, dst);
+      MRSR_LAUNCH_CHECK();
+      std::swap(src, dst);
+    }
+    MRSR_TRY(compact_nonzero(src, gcells, kmask, nk_out, st));
   }
   const int P = K * (K + 1) / 2;
   int64_t M[3] = {1, 1, 1};
@@ -756,8 +833,8 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
   FftNd fM, fG;
   MRSR_TRY(fM.init(d, M));
   MRSR_TRY(fG.init(d, G));
-  DevBuf ipsi[3];
-  for (int i = 0; i < d; ++i) MRSR_TRY(es_inv_psi_table(M[i], -G[i] / 2, G[i] + 1, ipsi[i]));
+  const float* ipsi[3] = {nullptr, nullptr, nullptr};
+  for (int i = 0; i < d; ++i) MRSR_TRY(es_inv_psi_table(M[i], -G[i] / 2, G[i] + 1, &ipsi[i]));
   // channel batches of ~2 GB of upsampled float2 grid
   const int nq = u_complex ? 2 : 1;  // a real basis spreads real values
   const int64_t max_bytes = 2ll << 30;
@@ -793,7 +870,7 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
     for (int i = 0; i < 3; ++i) {
       fa.G[i] = i < d ? G[i] : 1;
       fa.M[i] = M[i];
-      fa.ipsi[i] = i < d ? ipsi[i].as<float>() : nullptr;
+      fa.ipsi[i] = ipsi[i];
     }
     fa.gcells = gcells;
     fa.mcells = mcells;
@@ -899,54 +976,86 @@ struct InterpArgs {
   float2* data;          // (ns_pf, nt, ncoils)
 };
 
+// The w tap weights and wrapped tap indices of one sample along one dimension, in the
+// arithmetic of es_lane_weight (every tap of one thread).
+__device__ __forceinline__ void es_axis(float k, int M, float* w, int* idx) {
+  const int hw = kEsWidth / 2;
+  const float m = (float)M;
+  const float uh = __fmul_rn(k, m);
+  const float ul = fmaf(k, m, -uh);
+  const float f = floorf(uh);
+  const float r = __fadd_rn(__fsub_rn(uh, f), ul);
+  const int c = r > 0.f ? 1 : 0;
+  int l = ((int)f - hw + c) % M;
+  if (l < 0) l += M;
+#pragma unroll
+  for (int t = 0; t < kEsWidth; ++t) {
+    const float z = ((float)(c - hw + t) - r) * (1.f / hw);
+    w[t] = (fabsf(z) < 1.f) ? expf(kEsBeta * (sqrtf(1.f - z * z) - 1.f)) : 0.f;
+    idx[t] = l;
+    l = l + 1 == M ? 0 : l + 1;
+  }
+}
+
+// One thread per kept sample: the w^d taps of the K gridded planes, summed in the thread
+// (no cross-lane reduction); the 32 samples of a warp are consecutive along the trajectory,
+// so their taps share cache lines.
 __global__ void __launch_bounds__(256) k_interp(InterpArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int d = a.S.d;
-  const int ntap = d == 2 ? kEsWidth * kEsWidth : kEsWidth * kEsWidth * kEsWidth;
   const int64_t ns_tot = a.S.ns_pf * a.S.nt;
-  for (int64_t n = warp; n < a.S.n; n += nwarps) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < a.S.n; n += (int64_t)gridDim.x * blockDim.x) {
     const int64_t li = sample_lin(a.S, n);
-    const int64_t t = li / a.S.ns_pf;
-    float kd[3] = {0.f, 0.f, 0.f};
-    for (int dd = 0; dd < d; ++dd) kd[dd] = a.S.trj[dd + (int64_t)d * li];
-    float wt;
-    int64_t l0[3] = {0, 0, 0};
-    es_lane_weight(kd, a.M, d, lane, &wt, l0);
+    const int64_t t = frame_of(li, a.S.ns_pf);
+    float wx[kEsWidth], wy[kEsWidth], wz[kEsWidth];
+    int ix[kEsWidth], iy[kEsWidth], iz[kEsWidth];
+    es_axis(a.S.trj[(int64_t)d * li], (int)a.M[0], wx, ix);
+    es_axis(a.S.trj[1 + (int64_t)d * li], (int)a.M[1], wy, iy);
+    if (d == 3) {
+      es_axis(a.S.trj[2 + (int64_t)d * li], (int)a.M[2], wz, iz);
+    } else {
+#pragma unroll
+      for (int j = 0; j < kEsWidth; ++j) {
+        wz[j] = j == 0 ? 1.f : 0.f;
+        iz[j] = 0;
+      }
+    }
     float2 z[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) z[k] = make_float2(0.f, 0.f);
-    for (int tt = lane; tt < ntap; tt += 32) {
-      const int t1 = tt % kEsWidth, t2 = (tt / kEsWidth) % kEsWidth, t3 = tt / (kEsWidth * kEsWidth);
-      float w = __shfl_sync(0xffffffffu, wt, t1) * __shfl_sync(0xffffffffu, wt, kEsWidth + t2);
-      if (d == 3) w *= __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + t3);
-      int64_t cell = wrap(l0[0] + t1, a.M[0]) + a.M[0] * wrap(l0[1] + t2, a.M[1]);
-      if (d == 3) cell += a.M[0] * a.M[1] * wrap(l0[2] + t3, a.M[2]);
+    const int nz = d == 3 ? kEsWidth : 1;
+#pragma unroll 1
+    for (int t3 = 0; t3 < nz; ++t3) {
+      const int64_t base3 = (int64_t)iz[t3] * a.M[0] * a.M[1];
+      const float w3 = wz[t3];
 #pragma unroll
-      for (int k = 0; k < 8; ++k)
-        if (k < a.K) {
-          const float2 gv = a.g[(int64_t)k * a.mcells + cell];
-          z[k].x += w * gv.x;
-          z[k].y += w * gv.y;
+      for (int t2 = 0; t2 < kEsWidth; ++t2) {
+        const float w23 = wy[t2] * w3;
+        const float2* row = a.g + base3 + (int64_t)iy[t2] * a.M[0];
+#pragma unroll
+        for (int t1 = 0; t1 < kEsWidth; ++t1) {
+          const float w = w23 * wx[t1];
+          const float2* cell = row + ix[t1];
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            if (k < a.K) {
+              const float2 gv = __ldg(cell + (int64_t)k * a.mcells);
+              z[k].x = fmaf(w, gv.x, z[k].x);
+              z[k].y = fmaf(w, gv.y, z[k].y);
+            }
         }
+      }
     }
     float2 y = make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       if (k < a.K) {
-        float2 v = z[k];
-        for (int o = 16; o > 0; o >>= 1) {
-          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
-        }
         if (a.u_complex)
-          y = cadd(y, cmul(reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k], v));
+          y = cadd(y, cmul(reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k], z[k]));
         else
-          y = cadd(y, cscale(v, reinterpret_cast<const float*>(a.U)[t + a.S.nt * k]));
+          y = cadd(y, cscale(z[k], reinterpret_cast<const float*>(a.U)[t + a.S.nt * k]));
       }
     }
-    if (lane == 0) a.data[li + ns_tot * a.c] = y;
+    a.data[li + ns_tot * a.c] = y;
   }
 }
 
@@ -1022,8 +1131,8 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
   MRSR_REQUIRE(sl.set.n > 0, MRSR_ERR_ARG, "AssertionError: Sample mask removes all samples, cannot compute backprojection.");
   FftNd fM;
   MRSR_TRY(fM.init(ndims, M));
-  DevBuf ipsi[3];
-  for (int i = 0; i < ndims; ++i) MRSR_TRY(es_inv_psi_table(M[i], -(N[i] / 2), N[i], ipsi[i]));
+  const float* ipsi[3] = {nullptr, nullptr, nullptr};
+  for (int i = 0; i < ndims; ++i) MRSR_TRY(es_inv_psi_table(M[i], -(N[i] / 2), N[i], &ipsi[i]));
   // coil batches of ~2 GB of float2 grid
   const int64_t max_bytes = 2ll << 30;
   const int64_t per_coil = (int64_t)K * mcells * (int64_t)sizeof(float2);
@@ -1073,7 +1182,7 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
     for (int i = 0; i < 3; ++i) {
       fa.N[i] = N[i];
       fa.M[i] = M[i];
-      fa.ipsi[i] = i < ndims ? ipsi[i].as<float>() : nullptr;
+      fa.ipsi[i] = ipsi[i];
     }
     fa.nimg = nimg;
     fa.mcells = mcells;
@@ -1111,8 +1220,8 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
   MRSR_TRY(sl.init(ndims, trj, ns_per_frame, nt, nullptr, st));
   FftNd fM;
   MRSR_TRY(fM.init(ndims, M));
-  DevBuf ipsi[3];
-  for (int i = 0; i < ndims; ++i) MRSR_TRY(es_inv_psi_table(M[i], -(N[i] / 2), N[i], ipsi[i]));
+  const float* ipsi[3] = {nullptr, nullptr, nullptr};
+  for (int i = 0; i < ndims; ++i) MRSR_TRY(es_inv_psi_table(M[i], -(N[i] / 2), N[i], &ipsi[i]));
   DevBuf grid;
   MRSR_TRY(grid.alloc(sizeof(float2) * K * mcells));
   for (int c = 0; c < ncoils; ++c) {
@@ -1122,7 +1231,7 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
     for (int i = 0; i < 3; ++i) {
       pa.N[i] = N[i];
       pa.M[i] = M[i];
-      pa.ipsi[i] = i < ndims ? ipsi[i].as<float>() : nullptr;
+      pa.ipsi[i] = ipsi[i];
     }
     pa.nimg = nimg;
     pa.mcells = mcells;
@@ -1136,7 +1245,7 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
     MRSR_TRY(fM.run(grid.as<float2>(), K, -1, 1.0f, st));
     InterpArgs ia{sl.set, {M[0], M[1], M[2]}, mcells, K, c, u_is_complex, U, grid.as<float2>(),
                   reinterpret_cast<float2*>(data_out)};
-    k_interp<<<spread_blocks(sl.set.n), 256, 0, st>>>(ia);
+    k_interp<<<(unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(sl.set.n, 256), 1), 152 * 64), 256, 0, st>>>(ia);
     MRSR_LAUNCH_CHECK();
   }
   return MRSR_OK;  // asynchronous on `st`

@@ -64,8 +64,9 @@ __device__ __forceinline__ void es_lane_weight(const float* kd, const int64_t* M
   *wt_out = wt;
 }
 
-// Deconvolution factors 1/psi_hat(j) for j = jmin .. jmin + count - 1 on an upsampled grid of size M.
-int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, DevBuf& out);
+// Deconvolution factors 1/psi_hat(j) for j = jmin .. jmin + count - 1 on an upsampled grid
+// of size M: a device table of the current device, cached for the life of the process.
+int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, const float** out);
 
 // Fixed-point accumulation of the spread grids.  Each tap's term (a float32 product of
 // the sample value and the kernel weights) is scaled by 2^e, rounded to an integer and
@@ -99,6 +100,16 @@ __device__ __forceinline__ void fx_split(float a, int& hi, int& lo) {
   lo = __float_as_int(__fmaf_rn(d, (float)(1 << kFxLoBits), kMagic)) - kMagicBits;  // |lo| <= 2^20
 }
 
+// fx_split of the product a = x * y, the first rounding fused into the product
+__device__ __forceinline__ void fx_split_prod(float x, float y, int& hi, int& lo) {
+  constexpr float kMagic = 12582912.f;
+  constexpr int kMagicBits = 0x4B400000;
+  const float s1 = __fmaf_rn(x, y, kMagic);
+  hi = __float_as_int(s1) - kMagicBits;                          // round(x y)
+  const float d = __fmaf_rn(x, y, -__fsub_rn(s1, kMagic));       // x y - round(x y), |d| <= 1/2
+  lo = __float_as_int(__fmaf_rn(d, (float)(1 << kFxLoBits), kMagic)) - kMagicBits;
+}
+
 __device__ __forceinline__ long long fx_term(float a) {
   int hi, lo;
   fx_split(a, hi, lo);
@@ -119,7 +130,7 @@ struct SpreadLambdaArgs {
   long long* q;       // [np][nq][cells]
   const FixedScale* fs;
 };
-// Samples of a 2D set counting-sorted by the 16 x 16 tile of the grid M0 x M1 that holds
+// Samples of a 2D set counting-sorted by the 12 x 12 tile of the grid M0 x M1 that holds
 // their first tap, in chunks of at most 1024 samples (the work items of the tile-sorted
 // spreading kernels).  Built once per sample set and grid, shared by every spread of it.
 struct TileSort {
