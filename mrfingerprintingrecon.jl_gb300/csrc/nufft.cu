@@ -174,13 +174,14 @@ __device__ __forceinline__ void lane_taps(const SampleSet& S, const int64_t* M, 
 // One warp per kept sample (the 3D grids; tile-sorted kernels below do 2D).  A channel's
 // value is formed once per sample; its terms go to the grid as 64-bit atomics.
 template <int J>
-__global__ void __launch_bounds__(256, 2) k_spread_lambda(SpreadLambdaArgs a) {
+__global__ void __launch_bounds__(256, 2) k_spread_lambda(SpreadLambdaArgs a, const int* order) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const float sc = a.fs->scale;
   const int64_t chs = (int64_t)a.nq * a.cells;
-  for (int64_t n = warp; n < a.S.n; n += nwarps) {
+  for (int64_t i = warp; i < a.S.n; i += nwarps) {
+    const int64_t n = order ? (int64_t)order[i] : i;
     const int64_t li = sample_lin(a.S, n);
     const int64_t t = frame_of(li, a.S.ns_pf);
     float w[J];
@@ -210,14 +211,15 @@ __global__ void __launch_bounds__(256, 2) k_spread_lambda(SpreadLambdaArgs a) {
 }
 
 template <int J>
-__global__ void __launch_bounds__(256, 2) k_spread_data(SpreadDataArgs a) {
+__global__ void __launch_bounds__(256, 2) k_spread_data(SpreadDataArgs a, const int* order) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int d = J == 2 ? 2 : 3;
   const float sc = a.fs->scale;
   const int64_t ns_tot = a.S.ns_pf * a.S.nt;
-  for (int64_t n = warp; n < a.S.n; n += nwarps) {
+  for (int64_t i = warp; i < a.S.n; i += nwarps) {
+    const int64_t n = order ? (int64_t)order[i] : i;
     const int64_t li = sample_lin(a.S, n);
     const int64_t t = frame_of(li, a.S.ns_pf);
     float dcf = 1.f;
@@ -395,6 +397,56 @@ int TileSort::build(const SampleSet& S, int64_t M0, int64_t M1, cudaStream_t st)
   MRSR_LAUNCH_CHECK();
   const unsigned gt = (unsigned)std::max<int64_t>(cdiv(ntiles, 256), 1);
   k_tile_items<<<gt, 256, 0, st>>>(counts.as<int>(), offset.as<int>(), choff.as<int>(), ntiles, items.as<int4>());
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+constexpr int kTile3 = 8;
+
+// 3D home tile (kTile3^3) of every kept sample's first tap
+__global__ void k_tile_home3(SampleSet S, int M0, int M1, int M2, int* tile_of, int* counts) {
+  const int hw = kEsWidth / 2;
+  const int M[3] = {M0, M1, M2};
+  const int ntx = (M0 + kTile3 - 1) / kTile3, nty = (M1 + kTile3 - 1) / kTile3;
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < S.n; n += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t li = sample_lin(S, n);
+    int l0[3];
+    for (int dd = 0; dd < 3; ++dd) {
+      const float m = (float)M[dd];
+      const float kd = S.trj[dd + 3 * li];
+      const float uh = __fmul_rn(kd, m);
+      const float ul = fmaf(kd, m, -uh);
+      const float f = floorf(uh);
+      const float r = __fadd_rn(__fsub_rn(uh, f), ul);
+      int l = ((int)f - hw + (r > 0.f ? 1 : 0)) % M[dd];
+      l0[dd] = l < 0 ? l + M[dd] : l;
+    }
+    const int t = l0[0] / kTile3 + ntx * (l0[1] / kTile3 + nty * (l0[2] / kTile3));
+    tile_of[n] = t;
+    atomicAdd(&counts[t], 1);
+  }
+}
+
+int TileSort::build3(const SampleSet& S, const int64_t* M, cudaStream_t st) {
+  MRSR_REQUIRE(S.d == 3 && S.n < (1ll << 31), MRSR_ERR_UNSUPPORTED, "sample order: 3D, < 2^31 samples");
+  const int64_t nt3 = cdiv(M[0], kTile3) * cdiv(M[1], kTile3) * cdiv(M[2], kTile3);
+  MRSR_REQUIRE(nt3 < (1ll << 31), MRSR_ERR_UNSUPPORTED, "sample order: too many tiles");
+  ntiles = (int)nt3;
+  MRSR_TRY(counts.alloc(sizeof(int) * ntiles));
+  MRSR_TRY(offset.alloc(sizeof(int) * ntiles));
+  MRSR_TRY(choff.alloc(sizeof(int) * ntiles));
+  MRSR_TRY(cursor.alloc(sizeof(int) * ntiles));
+  MRSR_TRY(tile_of.alloc(sizeof(int) * std::max<int64_t>(S.n, 1)));
+  MRSR_TRY(order.alloc(sizeof(int) * std::max<int64_t>(S.n, 1)));
+  MRSR_TRY(nitems.alloc(sizeof(int)));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int) * ntiles, st));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int) * ntiles, st));
+  const unsigned gb = (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(S.n, 256), 1), 152 * 16);
+  k_tile_home3<<<gb, 256, 0, st>>>(S, (int)M[0], (int)M[1], (int)M[2], tile_of.as<int>(), counts.as<int>());
+  MRSR_LAUNCH_CHECK();
+  k_tile_scan<<<1, 1024, 0, st>>>(counts.as<int>(), ntiles, offset.as<int>(), choff.as<int>(), nitems.as<int>());
+  MRSR_LAUNCH_CHECK();
+  k_tile_scatter<<<gb, 256, 0, st>>>(S.n, tile_of.as<int>(), offset.as<int>(), cursor.as<int>(), order.as<int>());
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
 }
@@ -594,31 +646,33 @@ static int spread_tiled(const SampleSet& S, const int64_t* M, int64_t cells, int
 
 int spread_lambda(const SpreadLambdaArgs& a, const TileSort* ts, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
-  if (ts) {
+  if (ts && a.S.d == 2) {
     const LamParts parts{a.U, a.u_complex, a.nq, a.p0, a.S.nt, a.S.ns_pf};
     return spread_tiled(a.S, a.M, a.cells, a.np * a.nq, a.q, a.fs, *ts, parts, st);
   }
   MRSR_REQUIRE(a.cells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "spreading grid of 2^32 cells or more");
+  const int* order = ts ? ts->order.as<int>() : nullptr;
   if (a.S.d == 2)
-    k_spread_lambda<2><<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+    k_spread_lambda<2><<<spread_blocks(a.S.n), 256, 0, st>>>(a, order);
   else
-    k_spread_lambda<16><<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+    k_spread_lambda<16><<<spread_blocks(a.S.n), 256, 0, st>>>(a, order);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
 }
 
 int spread_data(const SpreadDataArgs& a, const TileSort* ts, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
-  if (ts && a.U) {
+  if (ts && a.S.d == 2 && a.U) {
     const DataParts parts{a.data, a.U, a.u_complex, a.K, a.c0, a.dcf_kind, a.dcf,
                           a.S.nt, a.S.ns_pf, a.S.ns_pf * a.S.nt};
     return spread_tiled(a.S, a.M, a.cells, 2 * a.nc * a.K, a.q, a.fs, *ts, parts, st);
   }
   MRSR_REQUIRE(a.cells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "spreading grid of 2^32 cells or more");
+  const int* order = ts && a.S.d == 3 ? ts->order.as<int>() : nullptr;
   if (a.S.d == 2)
-    k_spread_data<2><<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+    k_spread_data<2><<<spread_blocks(a.S.n), 256, 0, st>>>(a, order);
   else
-    k_spread_data<16><<<spread_blocks(a.S.n), 256, 0, st>>>(a);
+    k_spread_data<16><<<spread_blocks(a.S.n), 256, 0, st>>>(a, order);
   MRSR_LAUNCH_CHECK();
   return MRSR_OK;
 }
@@ -854,7 +908,11 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
     MRSR_TRY(fixed_scale(f, n, 2, u_complex ? 2.0 : 1.0, (double)S.n * taps_per_cell(d, M), fsb.as<FixedScale>(), st));
   }
   TileSort ts;
-  if (d == 2) MRSR_TRY(ts.build(S, M[0], M[1], st));
+  if (d == 2)
+    MRSR_TRY(ts.build(S, M[0], M[1], st));
+  else if (S.n < (1ll << 31))
+    MRSR_TRY(ts.build3(S, M, st));
+  const TileSort* tsp = d == 2 || S.n < (1ll << 31) ? &ts : nullptr;
   MRSR_TRY(packed.alloc((u_complex ? 8 : 4) * (size_t)P * std::max<int64_t>(*nk_out, 1)));
   // channels in batches of pb: spread, inverse DFT on the upsampled grid, deconvolve and fold onto the 2x grid
   for (int p0 = 0; p0 < P; p0 += pb) {
@@ -862,7 +920,7 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
     MRSR_CHECK_CUDA(cudaMemsetAsync(qgrid.p, 0, sizeof(long long) * nq * mcells * np, st));
     SpreadLambdaArgs sa{S, {M[0], M[1], M[2]}, mcells, U, u_complex, K, P, p0, np, nq, qgrid.as<long long>(),
                         fsb.as<FixedScale>()};
-    MRSR_TRY(spread_lambda(sa, d == 2 ? &ts : nullptr, st));
+    MRSR_TRY(spread_lambda(sa, tsp, st));
     MRSR_TRY(fixed_to_grid(qgrid.as<long long>(), nq, mcells, np, fsb.as<FixedScale>(), grid.as<float2>(), st));
     MRSR_TRY(fM.run(grid.as<float2>(), np, +1, 1.0f, st));
     FoldArgs fa;
@@ -997,7 +1055,7 @@ __device__ __forceinline__ void es_axis(float k, int M, float* w, int* idx) {
   }
 }
 
-// One thread per kept sample: the w^d taps of the K gridded planes, summed in the thread
+// 2D: one thread per kept sample, the w^2 taps of the K gridded planes summed in the thread
 // (no cross-lane reduction); the 32 samples of a warp are consecutive along the trajectory,
 // so their taps share cache lines.
 __global__ void __launch_bounds__(256) k_interp(InterpArgs a) {
@@ -1056,6 +1114,52 @@ __global__ void __launch_bounds__(256) k_interp(InterpArgs a) {
       }
     }
     a.data[li + ns_tot * a.c] = y;
+  }
+}
+
+// 3D: one warp per sample, lanes over its 512 taps (16 each, lane_taps), one shuffle
+// reduction per plane; for 512 taps per sample this beats a thread per sample (which
+// serialises 512 x K gathers in one thread).
+__global__ void __launch_bounds__(256) k_interp3(InterpArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t ns_tot = a.S.ns_pf * a.S.nt;
+  for (int64_t n = warp; n < a.S.n; n += nwarps) {
+    const int64_t li = sample_lin(a.S, n);
+    const int64_t t = frame_of(li, a.S.ns_pf);
+    float w[16];
+    unsigned cell[16];
+    lane_taps<16>(a.S, a.M, li, lane, 1.f, w, cell);
+    float2 z[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) z[k] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (k < a.K) {
+          const float2 gv = __ldg(a.g + (int64_t)k * a.mcells + cell[j]);
+          z[k].x = fmaf(w[j], gv.x, z[k].x);
+          z[k].y = fmaf(w[j], gv.y, z[k].y);
+        }
+    }
+    float2 y = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k < a.K) {
+        float2 v = z[k];
+        for (int o = 16; o > 0; o >>= 1) {
+          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (a.u_complex)
+          y = cadd(y, cmul(reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k], v));
+        else
+          y = cadd(y, cscale(v, reinterpret_cast<const float*>(a.U)[t + a.S.nt * k]));
+      }
+    }
+    if (lane == 0) a.data[li + ns_tot * a.c] = y;
   }
 }
 
@@ -1166,6 +1270,8 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
   }
   TileSort ts;
   if (tiled) MRSR_TRY(ts.build(sl.set, M[0], M[1], st));
+  const bool ordered = ndims == 3 && sl.set.n < (1ll << 31);
+  if (ordered) MRSR_TRY(ts.build3(sl.set, M, st));
   const int64_t out_elems = nimg * K * (cmaps ? 1 : ncoils);
   if (cmaps) MRSR_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(float2) * out_elems, st));
   for (int c0 = 0; c0 < ncoils; c0 += cc) {
@@ -1173,7 +1279,7 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
     MRSR_CHECK_CUDA(cudaMemsetAsync(qgrid.p, 0, (size_t)per_coil * 2 * nc, st));
     SpreadDataArgs sa{sl.set, {M[0], M[1], M[2]}, mcells, reinterpret_cast<const float2*>(data), c0, nc, U,
                       u_is_complex, K, dcf_kind, dcf_array, qgrid.as<long long>(), fsb.as<FixedScale>()};
-    MRSR_TRY(spread_data(sa, tiled ? &ts : nullptr, st));
+    MRSR_TRY(spread_data(sa, tiled || ordered ? &ts : nullptr, st));
     MRSR_TRY(fixed_to_grid(qgrid.as<long long>(), 2, mcells, (int64_t)nc * K, fsb.as<FixedScale>(), grid.as<float2>(),
                            st));
     MRSR_TRY(fM.run(grid.as<float2>(), (int64_t)nc * K, +1, 1.0f, st));
@@ -1245,7 +1351,12 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
     MRSR_TRY(fM.run(grid.as<float2>(), K, -1, 1.0f, st));
     InterpArgs ia{sl.set, {M[0], M[1], M[2]}, mcells, K, c, u_is_complex, U, grid.as<float2>(),
                   reinterpret_cast<float2*>(data_out)};
-    k_interp<<<(unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(sl.set.n, 256), 1), 152 * 64), 256, 0, st>>>(ia);
+    if (ndims == 3) {
+      MRSR_REQUIRE(mcells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "forward model grid of 2^32 cells or more");
+      k_interp3<<<spread_blocks(sl.set.n), 256, 0, st>>>(ia);
+    } else {
+      k_interp<<<(unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(sl.set.n, 256), 1), 152 * 64), 256, 0, st>>>(ia);
+    }
     MRSR_LAUNCH_CHECK();
   }
   return MRSR_OK;  // asynchronous on `st`

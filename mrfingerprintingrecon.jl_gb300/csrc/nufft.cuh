@@ -78,9 +78,9 @@ int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, const float** out);
 // 40 - ceil(log2(max|term|))) from a device-side bound: no cell sum can leave 63 bits, no
 // term reaches 2^40 (a resolution of 2^-40 of the largest term, far below float32's).
 //
-// A term is never converted to int64 by the float-to-int64 instruction, which runs on this
-// GPU's narrow float64 pipe (~0.4 T/s, it bounded the spreading kernels).  With a = term *
-// 2^-21 (|a| < 2^19) it is split as round(a) * 2^21 + round((a - round(a)) * 2^21), both
+// A term is never converted with __float2ll_rn, whose rate on this GPU is that of its
+// narrow float64 pipe (~0.4 T/s measured; it bounded the spreading kernels).  With a = term
+// * 2^-21 (|a| < 2^19) it is split as round(a) * 2^21 + round((a - round(a)) * 2^21), both
 // parts rounded by adding 1.5 * 2^23 in float32 (the sum's low mantissa bits are then the
 // rounded integer), which takes two float adds, one fma and two integer subtractions.
 constexpr int kFxLoBits = 21;
@@ -133,14 +133,17 @@ struct SpreadLambdaArgs {
 // Samples of a 2D set counting-sorted by the 12 x 12 tile of the grid M0 x M1 that holds
 // their first tap, in chunks of at most 1024 samples (the work items of the tile-sorted
 // spreading kernels).  Built once per sample set and grid, shared by every spread of it.
+// build3: for a 3D set, only `order`, by 8 x 8 x 8 tiles (the global kernels then take
+// samples in that order, so the warps in flight touch neighbouring grid lines in L2).
 struct TileSort {
   DevBuf counts, offset, choff, cursor, tile_of, order, items, nitems, next;
   int ntx = 0, ntiles = 0, m0 = 0, m1 = 0;
   int build(const SampleSet& S, int64_t M0, int64_t M1, cudaStream_t st);
+  int build3(const SampleSet& S, const int64_t* M, cudaStream_t st);
 };
 
-// ts: tile sort of a.S on a.M (2D), or null for the global kernel (one warp per sample,
-// every term a global atomic; used for 3D).
+// ts: tile sort of a.S on a.M.  2D: the tile-sorted kernel; 3D (ts from build3, or null):
+// the global kernel (one warp per sample, every term a global atomic).
 int spread_lambda(const SpreadLambdaArgs& a, const TileSort* ts, cudaStream_t st);
 
 struct SpreadDataArgs {

@@ -23,8 +23,8 @@ The server
   throughput and latency percentiles.
 
 Each request's arithmetic depends only on its own inputs (its own operator,
-work vectors and CG state; fixed-order reductions), so its image is the same
-alone and in any mix, up to the float32 atomics of its backprojection.
+work vectors and CG state; fixed-order reductions; backprojection grids summed in
+64-bit fixed point), so its image is bit-identical alone and in any mix.
 
 The scheduling core (:class:`ReconServer`) is separate from the device work
 (:class:`GpuExecutor`) so that admission, batching and eviction can be tested
