@@ -696,6 +696,22 @@ def pipeline_arm(args, world, rank, local):
         res = mr.cg_refined(A16, A, b, inner_iters=20, max_outer=2, tol=0.0, log=True)
         st["refined_2x20_fp16"] = _events_ms(lambda: mr.cg_refined(A16, A, b, inner_iters=20, max_outer=2, tol=0.0),
                                              1, stream)
+        # cg-20 images of the fp16-storage operator and of the relaxed CG (float32 products
+        # while ||r|| > 0.05 ||b||), against the float32 cg-20 image
+        x32 = mr.cg(A, b, maxiter=20, reltol=0.0)
+        x16 = mr.cg(A16, b, maxiter=20, reltol=0.0)
+        rel = mr.cg_relaxed(A16, A, b, maxiter=20, reltol=0.0, switch=0.05, log=True)
+        st["relaxed_cg20_fp16"] = _events_ms(
+            lambda: mr.cg_relaxed(A16, A, b, maxiter=20, reltol=0.0, switch=0.05), 1, stream)
+
+        def _err(a_, r_):
+            return float(torch.linalg.vector_norm(a_ - r_) / torch.linalg.vector_norm(r_))
+
+        cg_errs = {"fp16_cg20": _err(x16, x32), "relaxed_cg20": _err(rel.x, x32),
+                   "relaxed_float32_products": rel.hi_iters,
+                   "fp64": "the float64 oracle's CG is out of reach at 128^3 on the host; tests/"
+                           "test_mixed_precision_gpu.py measures the relaxed CG against it on 32^3"}
+        del x16, rel
         value, unit = 1000.0 / ms32, "applies/s"
         # algorithmic bytes of one 3D apply: x in, y out, coil maps in both row passes, the two
         # half-pruned stacks (2N x N x N and 2N x 2N x N per coil and coefficient) written and
@@ -704,7 +720,8 @@ def pipeline_arm(args, world, rank, local):
         b3 = N ** 3 * K * 16 + 2 * Nc * N ** 3 * 8 + 4 * Nc * (m1 + m2) * 8 + A.nk * A.P * (
             8 if A.lambda_is_complex else 4)
         extra = {"fp16_applies_s": 1000.0 / ms16, "fp16_vs_fp32_apply_rel_l2": diff,
-                 "refined_relres_after_2x20": res.resnorm, "apply_roofline": _apply_roofline(b3, ms32)}
+                 "refined_relres_after_2x20": res.resnorm, "cg20_image_rel_l2_vs_fp32_cg20": cg_errs,
+                 "apply_roofline": _apply_roofline(b3, ms32)}
         cfg = {"workload": PIPE3D, "img": list(img), "Nr": Nr, "Ncyc": Ncyc, "Nt": Nt, "Nc": Nc, "K": K,
                "trajectory": "koosh-ball golden means", "samples": Nr * Ncyc * Nt}
     elif args.workload == PIPE2D:

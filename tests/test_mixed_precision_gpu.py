@@ -12,8 +12,10 @@ iterate by ~1e-2: CG amplifies product errors, most of all those taken while the
 residual is large.  ``cg_relaxed`` takes the products on the float32 operator until
 ||r|| <= 0.05 ||b|| and on the reduced-precision operator after that, on one recurrence;
 its image is within 1e-3 of the float64 CG image.  Checked here with the tensor-core
-operator (fp16-tc, 256^2) and the fp16-storage operator (the 64^2, 4-coil, K = 4
-configuration at its exact shape).
+operator (fp16-tc, 256^2), the fp16-storage operator at the 64^2, 4-coil, K = 4
+configuration's exact shape, and the fp16-storage operator on a 3D koosh-ball problem
+(32^3; the 128^3 configuration's operator is the same code on longer lines, and its
+float64 CG is out of reach of the CPU oracle in a test).
 """
 import numpy as np
 import pytest
@@ -31,7 +33,11 @@ TOL_MIXED = 1e-3    # reduced-precision reconstruction vs float64 (the mixed-pre
 
 
 def _problem(mr, img, Nr, Nt, K, Nc, lo_precision):
-    trj = otraj.traj_2d_radial_goldenratio(Nr, 1, Nt)
+    if len(img) == 2:
+        trj = otraj.traj_2d_radial_goldenratio(Nr, 1, Nt)
+    else:  # 16 spokes per frame: 2400 spokes for 32^3 (with 2 coils or 600 spokes even the
+        # float32 CG-20 is 3e-4 .. 6e-4 from the float64 one: too ill-conditioned to measure)
+        trj = otraj.traj_kooshball_goldenratio(Nr, 16, Nt).astype(np.float32)
     D = mr.synthetic.dictionary(Nt)
     U = mr.synthetic.basis(D, K)
     x = mr.synthetic.phantom(img, D, U)
@@ -60,6 +66,7 @@ def _oracle_cg(img, trj, U, cm, b, iters):
 @pytest.mark.parametrize("img,Nr,Nt,K,Nc,lo", [
     ((256, 256), 512, 200, 4, 4, "fp16-tc"),
     ((64, 64), 128, 200, 4, 4, "fp16"),
+    ((32, 32, 32), 64, 150, 3, 4, "fp16"),
 ])
 def test_relaxed_mixed_precision_cg_matches_float64(mr, cuda, img, Nr, Nt, K, Nc, lo):
     trj, U, cm, A32, Alo, b = _problem(mr, img, Nr, Nt, K, Nc, lo)
