@@ -26,10 +26,14 @@
 #include <cmath>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "fftnd.cuh"
 
 namespace mrsr {
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -83,8 +87,8 @@ __global__ void k_esp_fro2(const float2* B, int64_t total, double* out) {
 // |b_i^H b_j| > tol |b_i| |b_j| and |b_i^H b_j| > 1e-10 |B|_F^2, and counted: the second
 // bound stops pairs of weak columns (far below the eigThresh_1 cut) from chasing the
 // float32 rounding that rotations of strong columns leave in them.
-__global__ void __launch_bounds__(kJacThreads) k_esp_jacobi(float2* B, int64_t n, int m, int m2, int t,
-                                                           const double* fro2, float tol, int* nrot) {
+__device__ __forceinline__ void esp_jacobi_pair(float2* B, int64_t n, int m, int m2, int t, const double* fro2,
+                                                float tol, int* nrot) {
   const int k = blockIdx.x;
   int i, j;
   if (k == 0) {
@@ -138,6 +142,25 @@ __global__ void __launch_bounds__(kJacThreads) k_esp_jacobi(float2* B, int64_t n
     bj[e] = make_float2(sn * eu.x + c * v.x, sn * eu.y + c * v.y);
   }
   if (threadIdx.x == 0) atomicAdd(nrot, 1);
+}
+
+// one round per launch
+__global__ void __launch_bounds__(kJacThreads) k_esp_jacobi(float2* B, int64_t n, int m, int m2, int t,
+                                                           const double* fro2, float tol, int* nrot) {
+  esp_jacobi_pair(B, n, m, m2, t, fro2, tol, nrot);
+}
+
+// A whole sweep (the m2 - 1 rounds) in one cooperative launch: every CTA takes its pair of
+// the round, then the grid synchronises before the next round.  The launch is cooperative,
+// so all m2 / 2 CTAs are resident and the grid barrier always completes; 361 round launches
+// of ~14 us each (launch and latency bound) become one.
+__global__ void __launch_bounds__(kJacThreads) k_esp_jacobi_sweep(float2* B, int64_t n, int m, int m2,
+                                                                 const double* fro2, float tol, int* nrot) {
+  cg::grid_group grid = cg::this_grid();
+  for (int t = 0; t < m2 - 1; ++t) {
+    esp_jacobi_pair(B, n, m, m2, t, fro2, tol, nrot);
+    grid.sync();
+  }
 }
 
 // sig2[p] = |column p|^2 and the largest of them (float bits, non-negative: atomicMax)
@@ -412,14 +435,33 @@ extern "C" int mrsr_espirit(int ndims, const int64_t* img_shape, const int64_t* 
   MRSR_CHECK_CUDA(cudaMemsetAsync(fro.p, 0, sizeof(double), st));
   k_esp_fro2<<<blocks_for(g.n * g.npos, 256, 152 * 4), 256, 0, st>>>(B.as<float2>(), g.n * g.npos, fro.as<double>());
   MRSR_LAUNCH_CHECK();
-  // one-sided Jacobi sweeps until a sweep applies no rotation
+  // one-sided Jacobi sweeps until a sweep applies no rotation; a sweep is one cooperative
+  // launch when its m2 / 2 CTAs fit on the device at once, else one launch per round
+  int dev = 0, nsm = 0, per_sm = 0, coop = 0;
+  MRSR_CHECK_CUDA(cudaGetDevice(&dev));
+  MRSR_CHECK_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  MRSR_CHECK_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  MRSR_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_esp_jacobi_sweep, kJacThreads, 0));
+  const bool one_launch = coop && (int64_t)per_sm * nsm >= m2 / 2;
   int last = -1;
   for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
     MRSR_CHECK_CUDA(cudaMemsetAsync(nrot.p, 0, sizeof(int), st));
-    for (int t = 0; t < m2 - 1; ++t) {
-      k_esp_jacobi<<<m2 / 2, kJacThreads, 0, st>>>(B.as<float2>(), g.n, m, m2, t, fro.as<double>(), kJacTol,
-                                                   nrot.as<int>());
-      MRSR_LAUNCH_CHECK();
+    if (one_launch) {
+      float2* Bp = B.as<float2>();
+      int64_t nn = g.n;
+      int mm = m, mm2 = m2;
+      const double* fp = fro.as<double>();
+      float tol = kJacTol;
+      int* np_ = nrot.as<int>();
+      void* args[] = {&Bp, &nn, &mm, &mm2, &fp, &tol, &np_};
+      MRSR_CHECK_CUDA(cudaLaunchCooperativeKernel((const void*)k_esp_jacobi_sweep, dim3(m2 / 2), dim3(kJacThreads), args,
+                                                  0, st));
+    } else {
+      for (int t = 0; t < m2 - 1; ++t) {
+        k_esp_jacobi<<<m2 / 2, kJacThreads, 0, st>>>(B.as<float2>(), g.n, m, m2, t, fro.as<double>(), kJacTol,
+                                                     nrot.as<int>());
+        MRSR_LAUNCH_CHECK();
+      }
     }
     MRSR_CHECK_CUDA(cudaMemcpyAsync(&last, nrot.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     MRSR_CHECK_CUDA(cudaStreamSynchronize(st));

@@ -270,6 +270,27 @@ static double taps_per_cell(int d, const int64_t* M) {
 
 static unsigned spread_blocks(int64_t n) { return (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(n * 32, 256), 1), 152 * 64); }
 
+// The w tap weights and wrapped tap indices of one sample along one dimension, in the
+// arithmetic of es_lane_weight (every tap of one thread).
+__device__ __forceinline__ void es_axis(float k, int M, float* w, int* idx) {
+  const int hw = kEsWidth / 2;
+  const float m = (float)M;
+  const float uh = __fmul_rn(k, m);
+  const float ul = fmaf(k, m, -uh);
+  const float f = floorf(uh);
+  const float r = __fadd_rn(__fsub_rn(uh, f), ul);
+  const int c = r > 0.f ? 1 : 0;
+  int l = ((int)f - hw + c) % M;
+  if (l < 0) l += M;
+#pragma unroll
+  for (int t = 0; t < kEsWidth; ++t) {
+    const float z = ((float)(c - hw + t) - r) * (1.f / hw);
+    w[t] = (fabsf(z) < 1.f) ? expf(kEsBeta * (sqrtf(1.f - z * z) - 1.f)) : 0.f;
+    idx[t] = l;
+    l = l + 1 == M ? 0 : l + 1;
+  }
+}
+
 // ------------------------------------------------- tile-sorted (2D) ---
 //
 // 2D grids are spread tile by tile.  Samples are counting-sorted by the 12 x 12 tile that
@@ -369,6 +390,51 @@ __global__ void k_tile_items(const int* counts, const int* offset, const int* ch
   }
 }
 
+// Per-sample tap record of the tile-sorted kernels, in sorted order: the separable weights
+// (the density compensation folded into wy), the wrapped first tap, the linear sample index
+// and its frame.  Formed once per sample set, read by every part group (a broadcast load
+// per sample instead of the weights, shuffles and index arithmetic per group).
+struct __align__(16) TapRec {
+  float wx[kEsWidth], wy[kEsWidth];
+  int li, t, lx0, ly0;
+};
+
+__global__ void k_tile_prep(SampleSet S, int M0, int M1, const int* order, int dcf_kind, const float* dcf,
+                            TapRec* rec) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < S.n; s += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t n = order[s];
+    const int64_t li = sample_lin(S, n);
+    const float k0 = S.trj[2 * li], k1 = S.trj[2 * li + 1];
+    TapRec r;
+    int ix[kEsWidth], iy[kEsWidth];
+    es_axis(k0, M0, r.wx, ix);
+    es_axis(k1, M1, r.wy, iy);
+    float w = 1.f;
+    if (dcf_kind == MRSR_DCF_RADIAL_3D || dcf_kind == MRSR_DCF_RADIAL_2D) {
+      const float s2 = __fadd_rn(__fmul_rn(k0, k0), __fmul_rn(k1, k1));
+      w = dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
+    } else if (dcf_kind == MRSR_DCF_ARRAY) {
+      w = dcf[n];
+    }
+#pragma unroll
+    for (int j = 0; j < kEsWidth; ++j) r.wy[j] *= w;
+    r.li = (int)li;
+    r.t = (int)frame_of(li, S.ns_pf);
+    r.lx0 = ix[0];
+    r.ly0 = iy[0];
+    rec[s] = r;
+  }
+}
+
+int TileSort::prep(const SampleSet& S, int dcf_kind, const float* dcf, cudaStream_t st) {
+  MRSR_REQUIRE(S.ns_pf * S.nt < (1ll << 31), MRSR_ERR_UNSUPPORTED, "tile records: < 2^31 samples per set");
+  MRSR_TRY(rec.alloc(sizeof(TapRec) * std::max<int64_t>(S.n, 1)));
+  const unsigned gb = (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(S.n, 256), 1), 152 * 16);
+  k_tile_prep<<<gb, 256, 0, st>>>(S, m0, m1, order.as<int>(), dcf_kind, dcf, rec.as<TapRec>());
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
 int TileSort::build(const SampleSet& S, int64_t M0, int64_t M1, cudaStream_t st) {
   MRSR_REQUIRE(S.d == 2 && S.n < (1ll << 31) && M0 < (1ll << 24) && M1 < (1ll << 24), MRSR_ERR_UNSUPPORTED,
                "tile-sorted spreading: 2D, < 2^31 samples, grid < 2^24 per dimension");
@@ -459,7 +525,7 @@ struct TiledArgs {
   long long* q;            // [nparts][cells]
   const FixedScale* fs;
   int ntx;
-  const int* order;        // kept-sample indices sorted by home tile
+  const TapRec* rec;       // per-sample tap records in sorted order
   const int4* items;       // (tile, first sorted position, count, -)
   const int* nitems;
   int* next;               // work counter, zeroed before the launch
@@ -480,8 +546,7 @@ struct LamParts {
     while ((k2 + 1) * (k2 + 2) / 2 <= p) ++k2;
     return Lane{p - k2 * (k2 + 1) / 2, k2, q};
   }
-  __device__ float value(const Lane& L, int64_t, int64_t li, const float*) const {
-    const int64_t t = frame_of(li, ns_pf);
+  __device__ float value(const Lane& L, int64_t, int64_t t) const {
     if (u_complex) {
       const float2* u = reinterpret_cast<const float2*>(U);
       const float2 v = cmulc(u[t + nt * L.k2], u[t + nt * L.k1]);  // conj(U[t,k1]) * U[t,k2]
@@ -507,15 +572,7 @@ struct DataParts {
     const int ch = part >> 1, c = ch / K;
     return Lane{c, ch - c * K, part & 1};
   }
-  __device__ float value(const Lane& L, int64_t n, int64_t li, const float* kd) const {
-    const int64_t t = frame_of(li, ns_pf);
-    float w = 1.f;
-    if (dcf_kind == MRSR_DCF_RADIAL_3D || dcf_kind == MRSR_DCF_RADIAL_2D) {
-      const float s2 = __fadd_rn(__fmul_rn(kd[0], kd[0]), __fmul_rn(kd[1], kd[1]));
-      w = dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
-    } else if (dcf_kind == MRSR_DCF_ARRAY) {
-      w = dcf[n];
-    }
+  __device__ float value(const Lane& L, int64_t li, int64_t t) const {
     const float2 y = data[li + ns_tot * (c0 + L.c)];
     float2 v;
     if (u_complex) {
@@ -524,7 +581,7 @@ struct DataParts {
       const float uu = reinterpret_cast<const float*>(U)[t + nt * L.k];
       v = make_float2(y.x * uu, y.y * uu);
     }
-    return (L.q ? v.y : v.x) * w;
+    return L.q ? v.y : v.x;
   }
 };
 
@@ -554,7 +611,6 @@ __global__ void __launch_bounds__(kTiledThreads, 2) k_spread_tiled(TiledArgs a, 
   const int nitems = *a.nitems;
   const int ngroups = (a.nparts + P - 1) / P;
   const int total = nitems * ngroups;
-  const int64_t M[2] = {a.M0, a.M1};
   const float sc = a.fs->scale;
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(a.next, 1);
@@ -571,22 +627,19 @@ __global__ void __launch_bounds__(kTiledThreads, 2) k_spread_tiled(TiledArgs a, 
     for (int i = threadIdx.x; i < P * kWinCells / 2; i += blockDim.x) w4[i] = make_int4(0, 0, 0, 0);
     __syncthreads();
     for (int s0 = warp * SPW; s0 < item.z; s0 += nwarps * SPW) {
-      const bool live_s = s0 + slot < item.z;
-      const int64_t n = a.order[item.y + min(s0 + slot, item.z - 1)];
-      const int64_t li = sample_lin(a.S, n);
-      const float kd[3] = {a.S.trj[2 * li], a.S.trj[2 * li + 1], 0.f};
-      float wt;
-      int64_t l0[3] = {0, 0, 0};
-      es_lane_weight(kd, M, 2, lane & 15, &wt, l0);
+      if (s0 + slot >= item.z || !live_part) continue;
+      const float4* r4 = reinterpret_cast<const float4*>(a.rec + item.y + s0 + slot);
       float wx[kEsWidth], wy[kEsWidth];
-#pragma unroll
-      for (int j = 0; j < kEsWidth; ++j) {
-        wx[j] = __shfl_sync(0xffffffffu, wt, slot * P + j);
-        wy[j] = __shfl_sync(0xffffffffu, wt, slot * P + kEsWidth + j);
+      {
+        const float4 q0 = r4[0], q1 = r4[1], q2 = r4[2], q3 = r4[3];
+        wx[0] = q0.x; wx[1] = q0.y; wx[2] = q0.z; wx[3] = q0.w;
+        wx[4] = q1.x; wx[5] = q1.y; wx[6] = q1.z; wx[7] = q1.w;
+        wy[0] = q2.x; wy[1] = q2.y; wy[2] = q2.z; wy[3] = q2.w;
+        wy[4] = q3.x; wy[5] = q3.y; wy[6] = q3.z; wy[7] = q3.w;
       }
-      if (!(live_s && live_part)) continue;
-      const float v = parts.value(L, n, li, kd) * sc;
-      const int lx0 = wrap32((int)l0[0], a.M0), ly0 = wrap32((int)l0[1], a.M1);
+      const int4 ri = reinterpret_cast<const int4*>(r4)[4];  // li, t, lx0, ly0
+      const float v = parts.value(L, ri.x, ri.y) * sc;
+      const int lx0 = ri.z, ly0 = ri.w;
       const int lx = lx0 - ox, ly = ly0 - oy;
       if ((unsigned)lx < (unsigned)kTile && (unsigned)ly < (unsigned)kTile) {
         int* pl = wlo + part * kWinCells + ly * kWin + lx;
@@ -639,8 +692,9 @@ template <class Parts>
 static int spread_tiled(const SampleSet& S, const int64_t* M, int64_t cells, int nparts, long long* q,
                         const FixedScale* fs, const TileSort& ts, const Parts& parts, cudaStream_t st) {
   MRSR_REQUIRE(ts.m0 == (int)M[0] && ts.m1 == (int)M[1], MRSR_ERR_STATE, "tile sort built for another grid");
+  MRSR_REQUIRE(ts.rec.p != nullptr, MRSR_ERR_STATE, "tile sort without tap records");
   const TiledArgs a{S, ts.m0, ts.m1, cells, nparts, q, fs, ts.ntx,
-                    ts.order.as<int>(), ts.items.as<int4>(), ts.nitems.as<int>(), ts.next.as<int>()};
+                    ts.rec.as<TapRec>(), ts.items.as<int4>(), ts.nitems.as<int>(), ts.next.as<int>()};
   return nparts <= 16 ? launch_tiled<16>(a, parts, st) : launch_tiled<32>(a, parts, st);
 }
 
@@ -908,11 +962,15 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
     MRSR_TRY(fixed_scale(f, n, 2, u_complex ? 2.0 : 1.0, (double)S.n * taps_per_cell(d, M), fsb.as<FixedScale>(), st));
   }
   TileSort ts;
-  if (d == 2)
+  const bool tiled = d == 2 && S.ns_pf * S.nt < (1ll << 31);
+  const bool ordered = d == 3 && S.n < (1ll << 31);
+  if (tiled) {
     MRSR_TRY(ts.build(S, M[0], M[1], st));
-  else if (S.n < (1ll << 31))
+    MRSR_TRY(ts.prep(S, MRSR_DCF_NONE, nullptr, st));
+  } else if (ordered) {
     MRSR_TRY(ts.build3(S, M, st));
-  const TileSort* tsp = d == 2 || S.n < (1ll << 31) ? &ts : nullptr;
+  }
+  const TileSort* tsp = tiled || ordered ? &ts : nullptr;
   MRSR_TRY(packed.alloc((u_complex ? 8 : 4) * (size_t)P * std::max<int64_t>(*nk_out, 1)));
   // channels in batches of pb: spread, inverse DFT on the upsampled grid, deconvolve and fold onto the 2x grid
   for (int p0 = 0; p0 < P; p0 += pb) {
@@ -1033,27 +1091,6 @@ struct InterpArgs {
   const float2* g;       // [K][mcells] after the forward DFT
   float2* data;          // (ns_pf, nt, ncoils)
 };
-
-// The w tap weights and wrapped tap indices of one sample along one dimension, in the
-// arithmetic of es_lane_weight (every tap of one thread).
-__device__ __forceinline__ void es_axis(float k, int M, float* w, int* idx) {
-  const int hw = kEsWidth / 2;
-  const float m = (float)M;
-  const float uh = __fmul_rn(k, m);
-  const float ul = fmaf(k, m, -uh);
-  const float f = floorf(uh);
-  const float r = __fadd_rn(__fsub_rn(uh, f), ul);
-  const int c = r > 0.f ? 1 : 0;
-  int l = ((int)f - hw + c) % M;
-  if (l < 0) l += M;
-#pragma unroll
-  for (int t = 0; t < kEsWidth; ++t) {
-    const float z = ((float)(c - hw + t) - r) * (1.f / hw);
-    w[t] = (fabsf(z) < 1.f) ? expf(kEsBeta * (sqrtf(1.f - z * z) - 1.f)) : 0.f;
-    idx[t] = l;
-    l = l + 1 == M ? 0 : l + 1;
-  }
-}
 
 // 2D: one thread per kept sample, the w^2 taps of the K gridded planes summed in the thread
 // (no cross-lane reduction); the 32 samples of a warp are consecutive along the trajectory,
@@ -1247,7 +1284,8 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
   // fixed-point scale: |term component| <= max|data| max|U| (x2 for complex U) x dcf bound,
   // at most ceil(w / M) taps per sample, cell and dimension
   MRSR_TRY(fsb.alloc(sizeof(FixedScale)));
-  const bool tiled = ndims == 2 && U != nullptr;  // an identity basis gives every sample one channel
+  // an identity basis gives every sample one channel: the global kernel
+  const bool tiled = ndims == 2 && U != nullptr && ns_per_frame * nt < (1ll << 31);
   {
     const float* f[3];
     int64_t n[3];
@@ -1269,7 +1307,10 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
     MRSR_TRY(fixed_scale(f, n, nf, mult, (double)sl.set.n * taps_per_cell(ndims, M), fsb.as<FixedScale>(), st));
   }
   TileSort ts;
-  if (tiled) MRSR_TRY(ts.build(sl.set, M[0], M[1], st));
+  if (tiled) {
+    MRSR_TRY(ts.build(sl.set, M[0], M[1], st));
+    MRSR_TRY(ts.prep(sl.set, dcf_kind, dcf_array, st));
+  }
   const bool ordered = ndims == 3 && sl.set.n < (1ll << 31);
   if (ordered) MRSR_TRY(ts.build3(sl.set, M, st));
   const int64_t out_elems = nimg * K * (cmaps ? 1 : ncoils);
