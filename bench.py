@@ -49,9 +49,12 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS) + [SERVED, PIPE3D, PIPEGROG, PIPE2D])
-    p.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "fp16-tc", "refined", "refined-tc"],
+    p.add_argument("--precision", default="fp32",
+                   choices=["fp32", "fp16", "fp16-tc", "refined", "refined-tc", "relaxed-tc"],
                    help="operator storage: fp32, fp16 (per-tile scaled half stacks and kernel); "
-                        "refined (served workload only: fp16 inner CG + float32 residual steps)")
+                        "refined (served workload only: fp16 inner CG + float32 residual steps); "
+                        "relaxed-tc (served workload only: first 5 of 20 CG products float32, "
+                        "the rest tensor-core)")
     p.add_argument("--rate", type=float, default=40.0, help="served workload: Poisson arrival rate (requests/s)")
     p.add_argument("--requests", type=int, default=500, help="served workload: requests in the timed stream")
     return p.parse_args()
@@ -535,14 +538,15 @@ def served_stream(mr, sv, rank, local, world, n_requests, rate, precision, keep_
             "budget": budget}
 
 
-def served_fp64_check(mr, reqs, iters, n_check=2):
+def served_fp64_check(mr, reqs, iters, n_check=2, img=None):
     """Relative L2 error of served images against the float64 oracle's cg-`iters` on the same
     request's backprojection, for the `n_check` requests cheapest for the CPU oracle (smallest
-    matrix, then fewest coils)."""
+    matrix, then fewest coils; only matrix `img` when given)."""
     import torch
     from oracle import cg as ocg
     from oracle import normalop as onormal
-    cand = sorted(reqs, key=lambda r: (r.protocol.img[0], r.ncoils, r.protocol.K, r.rid))[:n_check]
+    pool = [r for r in reqs if img is None or tuple(r.protocol.img) == tuple(img)]
+    cand = sorted(pool, key=lambda r: (r.protocol.img[0], r.ncoils, r.protocol.K, r.rid))[:n_check]
     out = []
     for r in cand:
         p = r.protocol
@@ -581,12 +585,16 @@ def served_arm(args, world, rank, local):
     import __graft_entry__ as ge
     mr = ge.package()
     sv = importlib.import_module(mr.__name__ + ".serving")
-    run = served_stream(mr, sv, rank, local, world, args.requests, args.rate, args.precision)
+    run = served_stream(mr, sv, rank, local, world, args.requests, args.rate, args.precision, keep_results=True)
     st, reqs, warm, protos, clk, iters, budget = (run[k] for k in ("stats", "reqs", "warm", "protos", "clocks",
                                                                   "iters", "budget"))
     wall = max_over_ranks(st.wall_s, world)
     if rank != 0:
         return
+    # float64 check of served images: the reduced-precision forms exist for the 256^2 matrices
+    # (512-point lines), so those requests are the ones checked when one is used
+    reduced = args.precision != "fp32"
+    chk = served_fp64_check(mr, reqs, iters, n_check=1 if reduced else 2, img=(256, 256) if reduced else None)
     value = world * st.completed / wall
     h2d = int(sum(r.data.numel() * 8 for r in reqs) / len(reqs))
     line = {
@@ -595,7 +603,8 @@ def served_arm(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "c64" if args.precision == "fp32" else "c64/f16",
         "data": "synthetic (8 seeded protocols, one 32-coil scan each, forward model + 1% noise)",
         "config": {"workload": SERVED, "requests": st.completed, "rate_hz": args.rate, "precision": args.precision,
-                   "cg_iters": iters, "outer_steps": 2 if args.precision.startswith("refined") else None, "slots": 4,
+                   "cg_iters": iters, "outer_steps": 2 if args.precision.startswith("refined") else None,
+                   "float32_cg_products": 5 if args.precision == "relaxed-tc" else None, "slots": 4,
                    "max_batch": 4, "hbm_budget_gb": budget / 2 ** 30,
                    "protocols": [p.name for p in protos], "coils": [8, 32],
                    "parallelism": f"replicas x{world}", "l2": "inputs (per-request data 7-295 MB) stream through"},
@@ -604,6 +613,9 @@ def served_arm(args, world, rank, local):
                 "note": "request latency includes the host-to-device copy of its data"},
         "serving": st.as_dict(),
         "clocks": clk,
+        "fp64_check": {"max_image_rel_l2": max((c["image_rel_l2_vs_fp64"] for c in chk), default=None),
+                       "requests": chk,
+                       "what": "served cg-20 image vs the float64 oracle's cg-20 on the request's backprojection"},
     }
     print(json.dumps(line), flush=True)
 

@@ -334,6 +334,16 @@ typedef struct mrsr_cg_batch mrsr_cg_batch; /* opaque handle */
 int mrsr_cg_batch_create(mrsr_normalop* const* ops_lo, mrsr_normalop* const* ops_hi, const float* const* b,
                          float* const* x, int n, int inner_iters, int outer_steps, mrsr_stream_t stream,
                          mrsr_cg_batch** out);
+/* A batch of relaxed mixed-precision solves: the fixed-schedule form of
+ * mrsr_cg_relaxed for graph capture.  Entry i is cg(A, b; maxiter = iters,
+ * reltol = 0) from x0 = 0 on one recurrence (vectors in ops_hi[i]'s workspace)
+ * whose first hi_iters products use ops_hi[i] (float32) and the others
+ * ops_lo[i] (a reduced-precision share of the same kernel and maps).
+ * hi_iters = iters gives the float32 solve, 0 the reduced one.  Launch,
+ * result (iterations and final ||r||) and destroy as for the batches above. */
+int mrsr_cg_batch_create_relaxed(mrsr_normalop* const* ops_lo, mrsr_normalop* const* ops_hi, const float* const* b,
+                                 float* const* x, int n, int iters, int hi_iters, mrsr_stream_t stream,
+                                 mrsr_cg_batch** out);
 int mrsr_cg_batch_launch(mrsr_cg_batch* batch, mrsr_stream_t stream);
 int mrsr_cg_batch_result(mrsr_cg_batch* batch, int i, int* iters_out, double* resnorm_out);
 void mrsr_cg_batch_destroy(mrsr_cg_batch* batch);

@@ -49,6 +49,8 @@ SIGNATURES = {
     "mrsr_cg_stacked": [p, p, p, i32, f64, f64, C.POINTER(i32), C.POINTER(f64), p],
     "mrsr_normalop_share": [p, p, i32, i32, p, C.POINTER(p)],
     "mrsr_cg_batch_create": [C.POINTER(p), C.POINTER(p), C.POINTER(p), C.POINTER(p), i32, i32, i32, p, C.POINTER(p)],
+    "mrsr_cg_batch_create_relaxed": [C.POINTER(p), C.POINTER(p), C.POINTER(p), C.POINTER(p), i32, i32, i32, p,
+                                     C.POINTER(p)],
     "mrsr_cg_batch_launch": [p, p],
     "mrsr_cg_batch_result": [p, i32, C.POINTER(i32), C.POINTER(f64)],
     "mrsr_cg_batch_destroy": [p],

@@ -326,15 +326,16 @@ int cg_fixed_init_enqueue(mrsr_normalop* op, const float2* b, float2* x, int ite
   return MRSR_OK;
 }
 
-int cg_fixed_iter_enqueue(mrsr_normalop* op, float2* x, cudaStream_t st) {
+int cg_fixed_iter_enqueue(mrsr_normalop* op, float2* x, cudaStream_t st, mrsr_normalop* apply_op) {
   CgWork& w = op->cg;
+  if (!apply_op) apply_op = op;
   const int64_t n = op->geo.nimg() * op->geo.K;
   CgState* s = w.state.as<CgState>();
   double2* part = w.partial.as<double2>();
   const unsigned nb = vec_blocks(n);
   k_cg_dir<<<nb, kCgThreads, 0, st>>>(w.r.as<float2>(), w.u.as<float2>(), n, s);
   MRSR_LAUNCH_CHECK();
-  MRSR_TRY(normalop_apply_internal(op, w.u.as<float2>(), w.c.as<float2>(), make_float2(1.f, 0.f),
+  MRSR_TRY(normalop_apply_internal(apply_op, w.u.as<float2>(), w.c.as<float2>(), make_float2(1.f, 0.f),
                                    make_float2(0.f, 0.f), st));
   k_cg_alpha<<<nb, kCgThreads, 0, st>>>(w.u.as<float2>(), w.c.as<float2>(), n, s, part);
   MRSR_LAUNCH_CHECK();

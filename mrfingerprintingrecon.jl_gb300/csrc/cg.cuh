@@ -48,9 +48,11 @@ int cg_run(mrsr_normalop* op, CgWork& w, const float2* b, float2* x, int maxiter
 // residual norm after the stream has finished.
 int cg_fixed_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st);
 // the same in two parts: x = 0, r = b (with the iteration limit `iters`), and one iteration;
-// iterations after the limit or the tolerance return at once
+// iterations after the limit or the tolerance return at once.  apply_op (same size; null =
+// op) takes the iteration's product while the CG vectors stay in op's workspace: the relaxed
+// schedule's reduced-precision iterations.
 int cg_fixed_init_enqueue(mrsr_normalop* op, const float2* b, float2* x, int iters, cudaStream_t st);
-int cg_fixed_iter_enqueue(mrsr_normalop* op, float2* x, cudaStream_t st);
+int cg_fixed_iter_enqueue(mrsr_normalop* op, float2* x, cudaStream_t st, mrsr_normalop* apply_op = nullptr);
 int cg_fixed_result(mrsr_normalop* op, int* iters, double* res);
 
 }  // namespace mrsr

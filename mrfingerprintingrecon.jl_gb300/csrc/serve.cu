@@ -133,6 +133,7 @@ struct mrsr_cg_batch {
   cudaStream_t last = nullptr;
   cudaEvent_t done = nullptr;  // recorded after each launch
   int inner = 0, outer = 0;
+  int hi_iters = -1;  // >= 0: relaxed schedule (products on hi for the first hi_iters iterations)
   ~mrsr_cg_batch() {
     if (done) {
       cudaEventSynchronize(done);  // the graph and its vectors outlive its last launch
@@ -154,6 +155,12 @@ static int batch_branch(mrsr_cg_batch* bt, int i, cudaStream_t st) {
   const int64_t n = en.lo->geo.nimg() * en.lo->geo.K;
   const unsigned nb = vec_grid(n);
   if (!en.hi) return cg_fixed_enqueue(en.lo, en.b, en.x, bt->inner, st);
+  if (bt->hi_iters >= 0) {
+    // relaxed: one CG recurrence in hi's workspace, float32 products first
+    MRSR_TRY(cg_fixed_init_enqueue(en.hi, en.b, en.x, bt->inner, st));
+    for (int k = 0; k < bt->inner; ++k) MRSR_TRY(cg_fixed_iter_enqueue(en.hi, en.x, st, k < bt->hi_iters ? en.hi : en.lo));
+    return MRSR_OK;
+  }
   // refinement with a fixed schedule: x = 0, r = b; repeat: d = CG_lo(r), x += d, r = b - A_hi x
   double* nrm = bt->nrm.as<double>() + 2 * i;
   MRSR_TRY(sv_norm2(en.b, n, en.part.as<double>(), nrm, st));
@@ -241,18 +248,19 @@ static int batch_build(mrsr_cg_batch* bt, cudaStream_t st) {
 
 }  // namespace mrsr
 
-extern "C" int mrsr_cg_batch_create(mrsr_normalop* const* ops_lo, mrsr_normalop* const* ops_hi,
-                                    const float* const* b, float* const* x, int n, int inner_iters, int outer_steps,
-                                    mrsr_stream_t stream, mrsr_cg_batch** out) {
-  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
+namespace mrsr {
+
+static int batch_create(mrsr_normalop* const* ops_lo, mrsr_normalop* const* ops_hi, const float* const* b,
+                        float* const* x, int n, int inner_iters, int outer_steps, int hi_iters, cudaStream_t st,
+                        mrsr_cg_batch** out) {
   MRSR_REQUIRE(out, MRSR_ERR_ARG, "out is NULL");
   *out = nullptr;
   MRSR_REQUIRE(ops_lo && b && x && n >= 1, MRSR_ERR_ARG, "empty or NULL batch");
   MRSR_REQUIRE(inner_iters >= 1, MRSR_ERR_ARG, "inner_iters must be >= 1");
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   mrsr_cg_batch* bt = new mrsr_cg_batch();
   bt->inner = inner_iters;
   bt->outer = std::max(outer_steps, 1);
+  bt->hi_iters = hi_iters;
   bt->e.reset(new mrsr_cg_batch::Entry[n]);
   bt->ne = n;
   int s = MRSR_OK;
@@ -287,6 +295,15 @@ extern "C" int mrsr_cg_batch_create(mrsr_normalop* const* ops_lo, mrsr_normalop*
       }
     }
     if (s != MRSR_OK) break;
+    if (hi_iters >= 0) {
+      if (!en.hi) {
+        set_error("relaxed batch entry %d has no float32 operator", i);
+        s = MRSR_ERR_ARG;
+        break;
+      }
+      s = en.hi->cg.ensure(nv);  // the recurrence's vectors
+      continue;
+    }
     s = en.lo->cg.ensure(nv);
     if (s == MRSR_OK && en.hi) s = en.r.alloc(sizeof(float2) * nv);
     if (s == MRSR_OK && en.hi) s = en.d.alloc(sizeof(float2) * nv);
@@ -318,6 +335,25 @@ extern "C" int mrsr_cg_batch_create(mrsr_normalop* const* ops_lo, mrsr_normalop*
   return MRSR_OK;
 }
 
+}  // namespace mrsr
+
+extern "C" int mrsr_cg_batch_create(mrsr_normalop* const* ops_lo, mrsr_normalop* const* ops_hi,
+                                    const float* const* b, float* const* x, int n, int inner_iters, int outer_steps,
+                                    mrsr_stream_t stream, mrsr_cg_batch** out) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
+  return batch_create(ops_lo, ops_hi, b, x, n, inner_iters, outer_steps, -1, reinterpret_cast<cudaStream_t>(stream),
+                      out);
+}
+
+extern "C" int mrsr_cg_batch_create_relaxed(mrsr_normalop* const* ops_lo, mrsr_normalop* const* ops_hi,
+                                            const float* const* b, float* const* x, int n, int iters, int hi_iters,
+                                            mrsr_stream_t stream, mrsr_cg_batch** out) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
+  MRSR_REQUIRE(ops_hi, MRSR_ERR_ARG, "a relaxed batch needs the float32 operators");
+  MRSR_REQUIRE(hi_iters >= 0 && hi_iters <= iters, MRSR_ERR_ARG, "hi_iters must be in [0, iters]");
+  return batch_create(ops_lo, ops_hi, b, x, n, iters, 1, hi_iters, reinterpret_cast<cudaStream_t>(stream), out);
+}
+
 extern "C" int mrsr_cg_batch_launch(mrsr_cg_batch* bt, mrsr_stream_t stream) {
   MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(bt && bt->exec, MRSR_ERR_ARG, "batch is NULL");
@@ -341,6 +377,12 @@ extern "C" int mrsr_cg_batch_result(mrsr_cg_batch* bt, int i, int* iters_out, do
   const mrsr_cg_batch::Entry& en = bt->e[i];
   if (!en.hi) {
     return cg_fixed_result(en.lo, iters_out, resnorm_out);
+  }
+  if (bt->hi_iters >= 0) {
+    MRSR_TRY(cg_fixed_result(en.hi, iters_out, resnorm_out));
+    int lo_err = 0;
+    MRSR_CHECK_CUDA(cudaMemcpy(&lo_err, en.lo->errflag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    return device_error_status(en.lo, lo_err, call_stream());
   }
   double h[2];
   int dev_err[2] = {0, 0};

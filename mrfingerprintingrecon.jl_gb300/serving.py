@@ -131,7 +131,8 @@ def request_bytes(img, K, nc, precision="fp32", refine=False):
     ops = stacks + nimg * nc * 8
     if refine:
         ops *= 2
-    bp_grid = K * G * 8 * min(nc, max(1, (2 << 30) // (K * G * 8)))
+    # backprojection: float2 grid plus its 64-bit fixed-point accumulator (re, im) per coil batch
+    bp_grid = 3 * K * G * 8 * min(nc, max(1, (2 << 30) // (K * G * 8)))
     cgwork = 3 * vec + 32 * 1024
     return int(1.1 * (ops + bp_grid + cgwork + 2 * vec + (2 * vec if refine else 0))) + (1 << 20)
 
@@ -335,13 +336,16 @@ class GpuExecutor:
     ``precision``: "fp32" (cg on the float32 operator), "fp16" (cg on the
     fp16-storage operator), "refined" (fp16 inner CG with ``outer`` float32
     residual corrections, all inside one graph), "fp16-tc" / "refined-tc" (the
-    same with the tensor-core operator).  Matrix sizes without the reduced
-    form (fp16: a four-step 2x grid; fp16-tc: 512-point lines, i.e. 256
-    samples along dims 1 and last) run the float32 operator in every mode.
+    same with the tensor-core operator), "relaxed-tc" (one CG recurrence whose
+    first ``relaxed_hi`` products use the float32 operator and the rest the
+    tensor-core one: the fixed-schedule relaxed CG, within 1e-3 of float64).
+    Matrix sizes without the reduced form (fp16: a four-step 2x grid; fp16-tc:
+    512-point lines, i.e. 256 samples along dims 1 and last) run the float32
+    operator in every mode.
     """
-    PRECISIONS = ("fp32", "fp16", "refined", "fp16-tc", "refined-tc")
+    PRECISIONS = ("fp32", "fp16", "refined", "fp16-tc", "refined-tc", "relaxed-tc")
 
-    def __init__(self, mr, iters=20, precision="fp32", outer=2, keep_results=True):
+    def __init__(self, mr, iters=20, precision="fp32", outer=2, keep_results=True, relaxed_hi=5):
         import torch
         if precision not in self.PRECISIONS:
             raise ValueError("precision must be one of " + ", ".join(self.PRECISIONS))
@@ -350,6 +354,7 @@ class GpuExecutor:
         self.iters = iters
         self.precision = precision
         self.outer = outer
+        self.relaxed_hi = relaxed_hi
         self.keep_results = keep_results
         self.streams: Dict[int, Any] = {}
 
@@ -359,7 +364,7 @@ class GpuExecutor:
         return self.streams[si]
 
     def _tc(self):
-        return self.precision in ("fp16-tc", "refined-tc")
+        return self.precision in ("fp16-tc", "refined-tc", "relaxed-tc")
 
     def kernel_bytes(self, proto):
         return kernel_bytes(proto.img, proto.K, complex_kernel=self.torch.is_complex(proto.U),
@@ -368,7 +373,7 @@ class GpuExecutor:
     def request_bytes(self, r):
         return request_bytes(r.protocol.img, r.protocol.K, r.ncoils,
                              "fp16" if self.precision in ("fp16", "refined") else "fp32",
-                             refine=self.precision in ("refined", "refined-tc"))
+                             refine=self.precision in ("refined", "refined-tc", "relaxed-tc"))
 
     def build_kernel(self, proto, si):
         s = self._stream(si)
@@ -389,6 +394,7 @@ class GpuExecutor:
             mixed, lo_prec = self.precision != "fp32" and all(2 * n in FOUR_STEP_LENGTHS for n in img), "fp16"
         lo_prec = lo_prec if mixed else "fp32"
         refined = mixed and self.precision in ("refined", "refined-tc")
+        relaxed = mixed and self.precision == "relaxed-tc"
         with torch.cuda.stream(s):
             ops, ops_hi, bs, xs = [], [], [], []
             for r in batch:
@@ -398,11 +404,12 @@ class GpuExecutor:
                     d.copy_(r.data, non_blocking=True)
                     r.data = d
                 ops.append(kern.share(cmaps=r.cmaps, precision=lo_prec, stream=s))
-                if refined:
+                if refined or relaxed:
                     ops_hi.append(kern.share(cmaps=r.cmaps, precision="fp32", stream=s))
                 bs.append(mr.calculate_backprojection(r.data, p.trj, r.cmaps, U=p.U, stream=s))
                 xs.append(mr.jl_empty(bs[-1].shape, torch.complex64))
-            cgb = mr.CgBatch(ops, bs, xs, self.iters, ops_hi=ops_hi or None, outer=self.outer, stream=s)
+            cgb = mr.CgBatch(ops, bs, xs, self.iters, ops_hi=ops_hi or None, outer=self.outer, stream=s,
+                             hi_iters=min(self.relaxed_hi, self.iters) if relaxed else None)
             cgb.launch(stream=s)
             ev = torch.cuda.Event()
             ev.record(s)

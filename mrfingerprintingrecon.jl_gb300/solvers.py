@@ -116,12 +116,15 @@ class CgBatch:
     Entry i solves ``ops[i] x[i] = b[i]`` with ``cg(A, b; maxiter=iters,
     reltol=0)`` from x0 = 0, or, when ``ops_hi`` is given, by mixed-precision
     refinement with ``outer`` fixed steps (inner CG on ``ops[i]``, residual with
-    ``ops_hi[i]``).  Each entry is a branch of the graph, so the solves overlap
-    on the device; :meth:`launch` re-solves with the current contents of the
-    ``b`` tensors (their storage is baked into the graph).
+    ``ops_hi[i]``), or, when ``ops_hi`` and ``hi_iters`` are given, by the relaxed
+    schedule (one CG recurrence, the first ``hi_iters`` products on ``ops_hi[i]``,
+    the rest on ``ops[i]``; the fixed-schedule form of :func:`cg_relaxed`).  Each
+    entry is a branch of the graph, so the solves overlap on the device;
+    :meth:`launch` re-solves with the current contents of the ``b`` tensors
+    (their storage is baked into the graph).
     """
 
-    def __init__(self, ops, bs, xs, iters, ops_hi=None, outer=1, stream=None):
+    def __init__(self, ops, bs, xs, iters, ops_hi=None, outer=1, stream=None, hi_iters=None):
         lib = _lib.load()
         n = len(ops)
         if not (len(bs) == len(xs) == n) or n == 0:
@@ -138,8 +141,14 @@ class CgBatch:
         bp = P(*[t.data_ptr() for t in self._b])
         xp = P(*[t.data_ptr() for t in self._x])
         h = C.c_void_p()
-        _lib.check(lib.mrsr_cg_batch_create(lo, hi, bp, xp, n, int(iters), int(outer), stream_handle(stream),
-                                            C.byref(h)))
+        if hi_iters is not None:
+            if hi is None:
+                raise ValueError("the relaxed schedule needs ops_hi")
+            _lib.check(lib.mrsr_cg_batch_create_relaxed(lo, hi, bp, xp, n, int(iters), int(hi_iters),
+                                                        stream_handle(stream), C.byref(h)))
+        else:
+            _lib.check(lib.mrsr_cg_batch_create(lo, hi, bp, xp, n, int(iters), int(outer), stream_handle(stream),
+                                                C.byref(h)))
         self._h = h
         self.n = n
 

@@ -152,3 +152,84 @@ def test_server_tensor_core_precision(mr, cuda, sv):
         b = mr.calculate_backprojection(r.data, p.trj, r.cmaps, U=p.U)
         x = mr.to_host(mr.cg(A, b, maxiter=iters, reltol=0.0))
         np.testing.assert_array_equal(x, mr.to_host(r.x), err_msg=f"{r.rid} {prec}")
+
+
+def test_cg_batch_relaxed_schedule(mr, cuda):
+    """The relaxed batch (one recurrence, float32 products first) is the float32 CG when every
+    product is float32 and the reduced-precision CG when none is, bit for bit (its accuracy
+    against float64 is checked on a reconstruction below; on this random right-hand side the
+    mixed schedules only have to stay near both)."""
+    N, K, Nc, it = 256, 3, 2, 8
+    trj = otraj.traj_2d_radial_goldenratio(2 * N, 2, 24)
+    rng = np.random.default_rng(7)
+    U = np.linalg.svd(rand_c(rng, (24, K)), full_matrices=False)[0].real.astype(np.float32)
+    cml = [rand_c(rng, (N, N)) for _ in range(Nc)]
+    A32 = mr.NFFTNormalOp((N, N), trj, U, cmaps=cml)
+    Atc = A32.share(cmaps=cml, precision="fp16-tc")
+    b = mr.to_jl(rand_c(rng, (N, N, K)), torch.complex64)
+    x32 = mr.to_host(mr.cg(A32, b, maxiter=it, reltol=0.0))
+    xtc = mr.to_host(mr.cg(Atc, b, maxiter=it, reltol=0.0))
+    out = {}
+    for hi in (it, 0, 3):
+        lo_op = A32.share(cmaps=cml, precision="fp16-tc")
+        hi_op = A32.share(cmaps=cml)
+        x = mr.jl_empty(b.shape, torch.complex64)
+        bt = mr.CgBatch([lo_op], [b], [x], it, ops_hi=[hi_op], hi_iters=hi)
+        bt.launch()
+        n_it, rn = bt.result(0)
+        assert n_it == it and np.isfinite(rn)
+        out[hi] = mr.to_host(x)
+        bt.close()
+    np.testing.assert_array_equal(out[it], x32)
+    np.testing.assert_array_equal(out[0], xtc)
+    assert rel_l2(out[3], x32) < 1e-2 and rel_l2(out[3], xtc) < 1e-2
+    with pytest.raises(ValueError):
+        mr.CgBatch([Atc], [b], [mr.jl_empty(b.shape, torch.complex64)], it, hi_iters=2)
+
+
+def test_server_relaxed_precision_equal_alone_and_within_float64_bar(mr, cuda, sv):
+    """relaxed-tc serving: bit-identical alone and in a mix; the 256^2 protocol's image is
+    within 1e-3 of the float64 oracle's CG on the same backprojection."""
+    from oracle import cg as ocg
+    from oracle import normalop as onormal
+    protos = []
+    for i, (N, K, Nt) in enumerate(((256, 3, 200), (32, 3, 24))):
+        trj = mr.trajectories.traj_2d_radial_goldenratio(2 * N, 2, Nt, thetaRot=0.2 * i)
+        U = mr.synthetic.basis(mr.synthetic.dictionary(Nt, natoms=200, seed=i), K)
+        protos.append(sv.Protocol(name=f"p{i}", img=(N, N), trj=mr.to_jl(trj, torch.float32),
+                                  U=mr.to_jl(U, torch.float32), K=K))
+    scans = [sv.make_scans(mr, p, 4, seed=30 + i) for i, p in enumerate(protos)]
+    torch.cuda.synchronize()
+    iters = 20
+    reqs = sv.make_request_stream(protos, scans, 5, rate_hz=0.0, coil_range=(3, 4), seed=6)
+    srv = sv.ReconServer(sv.GpuExecutor(mr, iters=iters, precision="relaxed-tc"), 8 << 30, slots=2, max_batch=2)
+    srv.run(reqs)
+    srv.close()
+    checked = False
+    for r in reqs:
+        alone = sv.Request(rid=r.rid, protocol=r.protocol, data=r.data, cmaps=r.cmaps, arrival=0.0)
+        srv1 = sv.ReconServer(sv.GpuExecutor(mr, iters=iters, precision="relaxed-tc"), 8 << 30, slots=1,
+                              max_batch=1)
+        srv1.run([alone])
+        srv1.close()
+        np.testing.assert_array_equal(mr.to_host(alone.x), mr.to_host(r.x), err_msg=str(r.rid))
+        p = r.protocol
+        if p.img[0] != 256 or checked:
+            continue
+        checked = True
+        trj, U = mr.to_host(p.trj), mr.to_host(p.U)
+        cm = mr.to_host(r.cmaps)
+        cml = [cm[..., c] for c in range(cm.shape[-1])]
+        b = mr.to_host(mr.calculate_backprojection(r.data, p.trj, r.cmaps, U=p.U)).astype(np.complex128)
+        G = tuple(2 * n for n in p.img)
+        Lam, km = onormal.calculate_kernel_noncartesian(G, trj, U, fast=True)
+
+        def apply(v):
+            return onormal.nfft_normalop_apply(v.reshape(p.img + (p.K,), order="F"), Lam, km, p.img,
+                                               cmaps=cml).ravel(order="F")
+
+        x64, _, _ = ocg.cg(apply, b.ravel(order="F"), maxiter=iters, reltol=0.0)
+        err = rel_l2(mr.to_host(r.x), x64.reshape(p.img + (p.K,), order="F"))
+        print(f"served relaxed-tc 256^2 cg-20 vs float64: {err:.2e}")
+        assert err < 1e-3
+    assert checked
