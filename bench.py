@@ -753,6 +753,9 @@ def pipeline_arm(args, world, rank, local):
         st["backprojection"] = _events_ms(lambda: mr.calculate_backprojection(data, trj, cm, U=U), reps, stream)
         mr.cg(A, b, maxiter=20, reltol=0.0)
         st["cg20"] = _events_ms(lambda: mr.cg(A, b, maxiter=20, reltol=0.0), reps, stream)
+        # the configuration's reconstruction: Λ/kmask, backprojection and 50 CG iterations
+        st["cg50"] = _events_ms(lambda: mr.cg(A, b, maxiter=50, reltol=0.0), reps, stream)
+        st["recon_lambda_bp_cg50"] = st["lambda_kmask"] + st["backprojection"] + st["cg50"]
         value, unit = 1000.0 / st["backprojection"], "backprojections/s"
         ns = Nr * Ncyc * Nt
         P = K * (K + 1) // 2

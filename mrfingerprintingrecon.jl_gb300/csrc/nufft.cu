@@ -261,6 +261,99 @@ __global__ void __launch_bounds__(256, 2) k_spread_data(SpreadDataArgs a, const 
   }
 }
 
+// 3D data spreading with a basis into a [cell][part] accumulator (the NP <= 32 parts of a
+// coil batch consecutive: re and im of each coil and coefficient).  One warp per sample,
+// lanes over the parts: a lane forms its part's value once, then adds its 512 terms, and
+// the 32 atomics of one warp instruction land on one cell's consecutive parts (a few
+// 32-byte sectors instead of one sector per lane).  Samples in 8^3-tile order.
+__global__ void __launch_bounds__(256, 2) k_spread_data_cp(SpreadDataArgs a, const int* order, int NP) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const float sc = a.fs->scale;
+  const int64_t ns_tot = a.S.ns_pf * a.S.nt;
+  const bool live = lane < NP;
+  const int ch = live ? lane >> 1 : 0, qpart = lane & 1;
+  const int c = ch / a.K, k = ch - c * a.K;
+  const int M0 = (int)a.M[0], M1 = (int)a.M[1], M2 = (int)a.M[2];
+  for (int64_t i = warp; i < a.S.n; i += nwarps) {
+    const int64_t n = order ? (int64_t)order[i] : i;
+    const int64_t li = sample_lin(a.S, n);
+    const int64_t t = frame_of(li, a.S.ns_pf);
+    const float kd[3] = {a.S.trj[3 * li], a.S.trj[1 + 3 * li], a.S.trj[2 + 3 * li]};
+    float dcf = 1.f;
+    if (a.dcf_kind == MRSR_DCF_RADIAL_3D || a.dcf_kind == MRSR_DCF_RADIAL_2D) {
+      float s2 = 0.f;
+      for (int dd = 0; dd < 3; ++dd) s2 = __fadd_rn(s2, __fmul_rn(kd[dd], kd[dd]));
+      dcf = a.dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
+    } else if (a.dcf_kind == MRSR_DCF_ARRAY) {
+      dcf = a.dcf[n];
+    }
+    float wt;
+    int64_t l0[3] = {0, 0, 0};
+    es_lane_weight(kd, a.M, 3, lane, &wt, l0);
+    float wx[kEsWidth], wy[kEsWidth], wz[kEsWidth];
+#pragma unroll
+    for (int j = 0; j < kEsWidth; ++j) {
+      wx[j] = __shfl_sync(0xffffffffu, wt, j);
+      wy[j] = __shfl_sync(0xffffffffu, wt, kEsWidth + j);
+      wz[j] = __shfl_sync(0xffffffffu, wt, 2 * kEsWidth + j);
+    }
+    if (!live) continue;
+    const float2 y = a.data[li + ns_tot * (a.c0 + c)];
+    float2 vv;
+    if (a.u_complex) {
+      vv = cmulc(y, reinterpret_cast<const float2*>(a.U)[t + a.S.nt * k]);  // y * conj(U)
+    } else {
+      const float uu = reinterpret_cast<const float*>(a.U)[t + a.S.nt * k];
+      vv = make_float2(y.x * uu, y.y * uu);
+    }
+    const float v = (qpart ? vv.y : vv.x) * sc * dcf;
+    unsigned ix[kEsWidth];
+    const int x0 = wrap32((int)l0[0], M0), y0 = wrap32((int)l0[1], M1), z0 = wrap32((int)l0[2], M2);
+#pragma unroll
+    for (int j = 0; j < kEsWidth; ++j) ix[j] = (unsigned)((x0 + j) % M0);
+#pragma unroll 1
+    for (int t3 = 0; t3 < kEsWidth; ++t3) {
+      const unsigned zoff = (unsigned)((z0 + t3) % M2) * (unsigned)M1;
+      const float v3 = v * wz[t3];
+#pragma unroll
+      for (int t2 = 0; t2 < kEsWidth; ++t2) {
+        const unsigned rowc = (zoff + (unsigned)((y0 + t2) % M1)) * (unsigned)M0;
+        const float w23 = v3 * wy[t2];
+#pragma unroll
+        for (int t1 = 0; t1 < kEsWidth; ++t1) {
+          const unsigned cell = rowc + ix[t1];
+          atomicAdd(reinterpret_cast<unsigned long long*>(a.q + (int64_t)cell * NP + lane),
+                    (unsigned long long)fx_term(w23 * wx[t1]));
+        }
+      }
+    }
+  }
+}
+
+// [cell][NP] fixed-point accumulator -> [NP / 2][cell] float2 planes: 32 cells per block
+// through a shared tile (coalesced on both sides)
+__global__ void k_fixed_to_grid_cp(const long long* q, int NP, int64_t cells, const FixedScale* fs, float2* out) {
+  __shared__ float tile[32][33];
+  const float inv = fs->inv;
+  const int64_t cell0 = (int64_t)blockIdx.x * 32;
+  const int nc = cells - cell0 < 32 ? (int)(cells - cell0) : 32;
+  for (int e = threadIdx.x; e < nc * NP; e += blockDim.x) {
+    const int c = e / NP, p = e - c * NP;
+    const long long v = q[(cell0 + c) * NP + p];
+    const long long hi = (v + (1ll << 31)) >> 32;
+    const int lo = (int)(v - hi * 4294967296ll);
+    tile[c][p] = __fmaf_rn((float)(int)hi, 4294967296.f, (float)lo) * inv;
+  }
+  __syncthreads();
+  const int nch = NP / 2;
+  for (int e = threadIdx.x; e < nch * 32; e += blockDim.x) {
+    const int chn = e >> 5, c = e & 31;
+    if (c < nc) out[(int64_t)chn * cells + cell0 + c] = make_float2(tile[c][2 * chn], tile[c][2 * chn + 1]);
+  }
+}
+
 // taps of one sample that can land on the same cell (the w taps wrap around a grid shorter than w)
 static double taps_per_cell(int d, const int64_t* M) {
   double t = 1.0;
@@ -723,6 +816,11 @@ int spread_data(const SpreadDataArgs& a, const TileSort* ts, cudaStream_t st) {
   }
   MRSR_REQUIRE(a.cells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "spreading grid of 2^32 cells or more");
   const int* order = ts && a.S.d == 3 ? ts->order.as<int>() : nullptr;
+  if (a.S.d == 3 && a.U && 2 * a.nc * a.K <= 32) {  // [cell][part] accumulator (the 3D backprojection)
+    k_spread_data_cp<<<spread_blocks(a.S.n), 256, 0, st>>>(a, order, 2 * a.nc * a.K);
+    MRSR_LAUNCH_CHECK();
+    return MRSR_OK;
+  }
   if (a.S.d == 2)
     k_spread_data<2><<<spread_blocks(a.S.n), 256, 0, st>>>(a, order);
   else
@@ -1277,7 +1375,11 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
   // coil batches of ~2 GB of float2 grid
   const int64_t max_bytes = 2ll << 30;
   const int64_t per_coil = (int64_t)K * mcells * (int64_t)sizeof(float2);
-  const int cc = (int)std::max<int64_t>(1, std::min<int64_t>(ncoils, max_bytes / std::max<int64_t>(per_coil, 1)));
+  int cc = (int)std::max<int64_t>(1, std::min<int64_t>(ncoils, max_bytes / std::max<int64_t>(per_coil, 1)));
+  // 3D with a basis: the batch's parts (2 per coil and coefficient) interleaved per cell, at
+  // most 32 (one per lane of k_spread_data_cp)
+  const bool parts_layout = ndims == 3 && U != nullptr && 2 * K <= 32;
+  if (parts_layout) cc = std::min(cc, 16 / K);
   DevBuf grid, qgrid, fsb;
   MRSR_TRY(grid.alloc((size_t)per_coil * cc));
   MRSR_TRY(qgrid.alloc((size_t)per_coil * 2 * cc));  // fixed-point re and im, 8 bytes each
@@ -1321,8 +1423,14 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
     SpreadDataArgs sa{sl.set, {M[0], M[1], M[2]}, mcells, reinterpret_cast<const float2*>(data), c0, nc, U,
                       u_is_complex, K, dcf_kind, dcf_array, qgrid.as<long long>(), fsb.as<FixedScale>()};
     MRSR_TRY(spread_data(sa, tiled || ordered ? &ts : nullptr, st));
-    MRSR_TRY(fixed_to_grid(qgrid.as<long long>(), 2, mcells, (int64_t)nc * K, fsb.as<FixedScale>(), grid.as<float2>(),
-                           st));
+    if (parts_layout) {
+      k_fixed_to_grid_cp<<<(unsigned)cdiv(mcells, 32), 256, 0, st>>>(qgrid.as<long long>(), 2 * nc * K, mcells,
+                                                                    fsb.as<FixedScale>(), grid.as<float2>());
+      MRSR_LAUNCH_CHECK();
+    } else {
+      MRSR_TRY(fixed_to_grid(qgrid.as<long long>(), 2, mcells, (int64_t)nc * K, fsb.as<FixedScale>(),
+                             grid.as<float2>(), st));
+    }
     MRSR_TRY(fM.run(grid.as<float2>(), (int64_t)nc * K, +1, 1.0f, st));
     BpFoldArgs fa;
     fa.d = ndims;
