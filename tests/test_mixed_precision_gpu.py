@@ -63,17 +63,20 @@ def _oracle_cg(img, trj, U, cm, b, iters):
     return x.reshape(img + (K,), order="F")
 
 
-@pytest.mark.parametrize("img,Nr,Nt,K,Nc,lo", [
-    ((256, 256), 512, 200, 4, 4, "fp16-tc"),
-    ((64, 64), 128, 200, 4, 4, "fp16"),
-    ((32, 32, 32), 64, 150, 3, 4, "fp16"),
+# switch: the relative residual below which products go to the reduced operator.  The 3D
+# koosh ball is worse conditioned (CG-20 amplifies an apply error more), so its products
+# stay float32 a little longer (0.05: 7e-4 .. 8e-4 from float64; 0.02: ~1e-4).
+@pytest.mark.parametrize("img,Nr,Nt,K,Nc,lo,switch", [
+    ((256, 256), 512, 200, 4, 4, "fp16-tc", 0.05),
+    ((64, 64), 128, 200, 4, 4, "fp16", 0.05),
+    ((32, 32, 32), 64, 150, 3, 4, "fp16", 0.02),
 ])
-def test_relaxed_mixed_precision_cg_matches_float64(mr, cuda, img, Nr, Nt, K, Nc, lo):
+def test_relaxed_mixed_precision_cg_matches_float64(mr, cuda, img, Nr, Nt, K, Nc, lo, switch):
     trj, U, cm, A32, Alo, b = _problem(mr, img, Nr, Nt, K, Nc, lo)
     x64 = _oracle_cg(img, trj, U, cm, mr.to_host(b).astype(np.complex128), 20)
     x32 = mr.to_host(mr.cg(A32, b, maxiter=20, reltol=0.0))
     xlo = mr.to_host(mr.cg(Alo, b, maxiter=20, reltol=0.0))
-    rel = mr.cg_relaxed(Alo, A32, b, maxiter=20, reltol=0.0, switch=0.05, log=True)
+    rel = mr.cg_relaxed(Alo, A32, b, maxiter=20, reltol=0.0, switch=switch, log=True)
     e32, elo, erel = rel_l2(x32, x64), rel_l2(xlo, x64), rel_l2(mr.to_host(rel.x), x64)
     print(f"{img} {lo}: cg-20 vs float64: float32 {e32:.2e}, {lo} {elo:.2e}, relaxed {erel:.2e} "
           f"({rel.hi_iters} of {rel.iters} products float32)")
