@@ -607,6 +607,66 @@ int TileSort::build3(const SampleSet& S, const int64_t* M, cudaStream_t st) {
   MRSR_LAUNCH_CHECK();
   k_tile_scatter<<<gb, 256, 0, st>>>(S.n, tile_of.as<int>(), offset.as<int>(), cursor.as<int>(), order.as<int>());
   MRSR_LAUNCH_CHECK();
+  // work items of the 3D tile-sorted kernel: chunks of at most kChunk samples of one tile
+  m0 = (int)M[0];
+  m1 = (int)M[1];
+  m2 = (int)M[2];
+  ntx = (int)cdiv(M[0], kTile3);
+  nty = (int)cdiv(M[1], kTile3);
+  const int64_t maxitems = ntiles + cdiv(S.n, kChunk);
+  MRSR_TRY(items.alloc(sizeof(int4) * maxitems));
+  MRSR_TRY(next.alloc(sizeof(int)));
+  const unsigned gt = (unsigned)std::max<int64_t>(cdiv(ntiles, 256), 1);
+  k_tile_items<<<gt, 256, 0, st>>>(counts.as<int>(), offset.as<int>(), choff.as<int>(), ntiles, items.as<int4>());
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
+// 3D tap record: weights along x, y, z (the density compensation folded into wz), the
+// wrapped first tap, the linear sample index and its frame, in sorted order.
+struct __align__(16) TapRec3 {
+  float wx[kEsWidth], wy[kEsWidth], wz[kEsWidth];
+  int li, t, lx0, ly0, lz0, pad0, pad1, pad2;
+};
+static_assert(sizeof(TapRec3) == 128, "TapRec3 is eight 16-byte loads");
+
+__global__ void k_tile_prep3(SampleSet S, int M0, int M1, int M2, const int* order, int dcf_kind, const float* dcf,
+                             TapRec3* rec) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < S.n; s += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t n = order[s];
+    const int64_t li = sample_lin(S, n);
+    const float k0 = S.trj[3 * li], k1 = S.trj[3 * li + 1], k2 = S.trj[3 * li + 2];
+    TapRec3 r;
+    int ix[kEsWidth], iy[kEsWidth], iz[kEsWidth];
+    es_axis(k0, M0, r.wx, ix);
+    es_axis(k1, M1, r.wy, iy);
+    es_axis(k2, M2, r.wz, iz);
+    float w = 1.f;
+    if (dcf_kind == MRSR_DCF_RADIAL_3D || dcf_kind == MRSR_DCF_RADIAL_2D) {
+      const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(k0, k0), __fmul_rn(k1, k1)), __fmul_rn(k2, k2));
+      w = dcf_kind == MRSR_DCF_RADIAL_3D ? s2 : sqrtf(s2);
+    } else if (dcf_kind == MRSR_DCF_ARRAY) {
+      w = dcf[n];
+    }
+#pragma unroll
+    for (int j = 0; j < kEsWidth; ++j) r.wz[j] *= w;
+    r.li = (int)li;
+    r.t = (int)frame_of(li, S.ns_pf);
+    r.lx0 = ix[0];
+    r.ly0 = iy[0];
+    r.lz0 = iz[0];
+    r.pad0 = r.pad1 = r.pad2 = 0;
+    rec[s] = r;
+  }
+}
+
+int TileSort::prep3(const SampleSet& S, int dcf_kind, const float* dcf, cudaStream_t st) {
+  MRSR_REQUIRE(S.ns_pf * S.nt < (1ll << 31), MRSR_ERR_UNSUPPORTED, "tile records: < 2^31 samples per set");
+  MRSR_TRY(rec.alloc(sizeof(TapRec3) * std::max<int64_t>(S.n, 1)));
+  const unsigned gb = (unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(S.n, 256), 1), 152 * 16);
+  k_tile_prep3<<<gb, 256, 0, st>>>(S, m0, m1, m2, order.as<int>(), dcf_kind, dcf, rec.as<TapRec3>());
+  MRSR_LAUNCH_CHECK();
+  rec3 = true;
   return MRSR_OK;
 }
 
@@ -791,11 +851,153 @@ static int spread_tiled(const SampleSet& S, const int64_t* M, int64_t cells, int
   return nparts <= 16 ? launch_tiled<16>(a, parts, st) : launch_tiled<32>(a, parts, st);
 }
 
+// ------------------------------------------------- tile-sorted (3D) ---
+//
+// The 2D scheme in three dimensions: samples in 8^3 tiles (home tile of the first tap), work
+// items of at most kChunk samples of one tile x a group of kP3 = 4 parts, a window of
+// (8 + w - 1)^3 = 15^3 cells x 4 parts of 32-bit limbs in shared memory (106 KB: two CTAs
+// per SM), and one global 64-bit atomic per nonzero window cell at the flush, a warp on
+// consecutive cells.  A warp takes one sample at a time: lane = 8 part + t1 (part < 4, x tap
+// t1 < 8), so a warp instruction adds 8 consecutive cells of 4 parts, and the part stride
+// (3384 = 24 mod 32 words) puts the four 8-cell runs in disjoint bank ranges: no bank
+// conflicts.  With 64-bit global atomics capped near 0.73 T/s on this GPU, every term as a
+// global atomic (the one-warp-per-sample kernels) spends ~0.55 s on the 401 G terms of a
+// 128^3, 4.9 M-sample, 16-coil backprojection.
+constexpr int kWin3 = kTile3 + kEsWidth - 1;           // 15
+constexpr int kWin3Cells = kWin3 * kWin3 * kWin3;      // 3375
+constexpr int kWin3Stride = 3384;                      // part stride, = 24 (mod 32)
+constexpr int kP3 = 4;
+constexpr int kTiled3Smem = 2 * kP3 * kWin3Stride * (int)sizeof(int);
+static_assert(kWin3Stride >= kWin3Cells && kWin3Stride % 32 == 24 && kWin3Stride % 4 == 0, "3D window stride");
+
+struct TiledArgs3 {
+  SampleSet S;
+  int M0, M1, M2;
+  int64_t cells;
+  int nparts;
+  long long* q;            // [nparts][cells]
+  const FixedScale* fs;
+  int ntx, nty;
+  const TapRec3* rec;
+  const int4* items;
+  const int* nitems;
+  int* next;
+};
+
+template <class Parts>
+__global__ void __launch_bounds__(kTiledThreads, 2) k_spread_tiled3(TiledArgs3 a, Parts parts) {
+  extern __shared__ __align__(16) int win3[];  // [2][kP3][kWin3Stride]
+  int* wlo = win3;
+  int* whi = win3 + kP3 * kWin3Stride;
+  __shared__ int s_item;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int part = lane >> 3, t1 = lane & 7;
+  const int nitems = *a.nitems;
+  const int ngroups = (a.nparts + kP3 - 1) / kP3;
+  const int total = nitems * ngroups;
+  const float sc = a.fs->scale;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.next, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= total) break;
+    const int grp = it / nitems;
+    const int4 item = a.items[it - grp * nitems];
+    const int gpart = grp * kP3 + part;
+    const bool live_part = gpart < a.nparts;
+    const typename Parts::Lane L = parts.bind(live_part ? gpart : 0);
+    const int tx = item.x % a.ntx, tyz = item.x / a.ntx;
+    const int ox = tx * kTile3, oy = (tyz % a.nty) * kTile3, oz = (tyz / a.nty) * kTile3;
+    int4* w4 = reinterpret_cast<int4*>(win3);
+    for (int i = threadIdx.x; i < 2 * kP3 * kWin3Stride / 4; i += blockDim.x) w4[i] = make_int4(0, 0, 0, 0);
+    __syncthreads();
+    if (live_part) {
+      for (int smp = warp; smp < item.z; smp += nwarps) {
+        const float4* r4 = reinterpret_cast<const float4*>(a.rec + item.y + smp);
+        float wy[kEsWidth], wz[kEsWidth];
+        {
+          const float4 q2 = r4[2], q3 = r4[3], q4 = r4[4], q5 = r4[5];
+          wy[0] = q2.x; wy[1] = q2.y; wy[2] = q2.z; wy[3] = q2.w;
+          wy[4] = q3.x; wy[5] = q3.y; wy[6] = q3.z; wy[7] = q3.w;
+          wz[0] = q4.x; wz[1] = q4.y; wz[2] = q4.z; wz[3] = q4.w;
+          wz[4] = q5.x; wz[5] = q5.y; wz[6] = q5.z; wz[7] = q5.w;
+        }
+        const float wx1 = reinterpret_cast<const float*>(r4)[t1];
+        const int4 ri = reinterpret_cast<const int4*>(r4)[6];  // li, t, lx0, ly0
+        const int lz0 = reinterpret_cast<const int*>(r4)[28];
+        const float v = parts.value(L, ri.x, ri.y) * sc * wx1;
+        const int lx = ri.z - ox, ly = ri.w - oy, lz = lz0 - oz;
+        if ((unsigned)lx < (unsigned)kTile3 && (unsigned)ly < (unsigned)kTile3 && (unsigned)lz < (unsigned)kTile3) {
+          const int base = part * kWin3Stride + (lz * kWin3 + ly) * kWin3 + lx + t1;
+          int* pl = wlo + base;
+          int* ph = whi + base;
+#pragma unroll
+          for (int t3 = 0; t3 < kEsWidth; ++t3) {
+            const float v3 = v * wz[t3];
+#pragma unroll
+            for (int t2 = 0; t2 < kEsWidth; ++t2) {
+              int hi, lo;
+              fx_split_prod(v3, wy[t2], hi, lo);
+              atomicAdd(pl + (t3 * kWin3 + t2) * kWin3, lo);
+              atomicAdd(ph + (t3 * kWin3 + t2) * kWin3, hi);
+            }
+          }
+        } else {
+          // the sort put the first tap in this tile (the same float arithmetic); a sample
+          // outside it goes straight to the grid rather than out of the window
+          long long* g = a.q + (int64_t)gpart * a.cells;
+          const int64_t x = wrap32(ri.z + t1, a.M0);
+          for (int t3 = 0; t3 < kEsWidth; ++t3)
+            for (int t2 = 0; t2 < kEsWidth; ++t2) {
+              const int64_t row = (int64_t)a.M0 * (wrap32(ri.w + t2, a.M1) + (int64_t)a.M1 * wrap32(lz0 + t3, a.M2));
+              atomicAdd(reinterpret_cast<unsigned long long*>(g + row + x),
+                        (unsigned long long)fx_term(v * wz[t3] * wy[t2]));
+            }
+        }
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kP3 * kWin3Cells; e += blockDim.x) {
+      const int p = e / kWin3Cells, c = e - p * kWin3Cells;
+      const int gp = grp * kP3 + p;
+      if (gp >= a.nparts) continue;
+      const int w = p * kWin3Stride + c;
+      const long long v = (long long)whi[w] * (1ll << kFxLoBits) + (long long)wlo[w];
+      if (v == 0) continue;
+      const int cx = c % kWin3, cyz = c / kWin3;
+      const int cy = cyz % kWin3, cz = cyz / kWin3;
+      const int64_t cell = wrap32(ox + cx, a.M0) +
+                           (int64_t)a.M0 * (wrap32(oy + cy, a.M1) + (int64_t)a.M1 * wrap32(oz + cz, a.M2));
+      atomicAdd(reinterpret_cast<unsigned long long*>(a.q + (int64_t)gp * a.cells + cell), (unsigned long long)v);
+    }
+    __syncthreads();
+  }
+}
+
+template <class Parts>
+static int spread_tiled3(const SampleSet& S, const int64_t* M, int64_t cells, int nparts, long long* q,
+                         const FixedScale* fs, const TileSort& ts, const Parts& parts, cudaStream_t st) {
+  MRSR_REQUIRE(ts.rec3 && ts.m0 == (int)M[0] && ts.m1 == (int)M[1] && ts.m2 == (int)M[2], MRSR_ERR_STATE,
+               "3D tile sort built for another grid or without tap records");
+  const TiledArgs3 a{S, ts.m0, ts.m1, ts.m2, cells, nparts, q, fs, ts.ntx, ts.nty,
+                     ts.rec.as<TapRec3>(), ts.items.as<int4>(), ts.nitems.as<int>(), ts.next.as<int>()};
+  MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_spread_tiled3<Parts>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kTiled3Smem));
+  MRSR_CHECK_CUDA(cudaMemsetAsync(a.next, 0, sizeof(int), st));
+  k_spread_tiled3<Parts><<<152 * 2, kTiledThreads, kTiled3Smem, st>>>(a, parts);
+  MRSR_LAUNCH_CHECK();
+  return MRSR_OK;
+}
+
 int spread_lambda(const SpreadLambdaArgs& a, const TileSort* ts, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
   if (ts && a.S.d == 2) {
     const LamParts parts{a.U, a.u_complex, a.nq, a.p0, a.S.nt, a.S.ns_pf};
     return spread_tiled(a.S, a.M, a.cells, a.np * a.nq, a.q, a.fs, *ts, parts, st);
+  }
+  if (ts && a.S.d == 3 && ts->rec3) {
+    const LamParts parts{a.U, a.u_complex, a.nq, a.p0, a.S.nt, a.S.ns_pf};
+    return spread_tiled3(a.S, a.M, a.cells, a.np * a.nq, a.q, a.fs, *ts, parts, st);
   }
   MRSR_REQUIRE(a.cells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "spreading grid of 2^32 cells or more");
   const int* order = ts ? ts->order.as<int>() : nullptr;
@@ -809,10 +1011,11 @@ int spread_lambda(const SpreadLambdaArgs& a, const TileSort* ts, cudaStream_t st
 
 int spread_data(const SpreadDataArgs& a, const TileSort* ts, cudaStream_t st) {
   if (a.S.n == 0) return MRSR_OK;
-  if (ts && a.S.d == 2 && a.U) {
+  if (ts && a.U && (a.S.d == 2 || ts->rec3)) {
     const DataParts parts{a.data, a.U, a.u_complex, a.K, a.c0, a.dcf_kind, a.dcf,
                           a.S.nt, a.S.ns_pf, a.S.ns_pf * a.S.nt};
-    return spread_tiled(a.S, a.M, a.cells, 2 * a.nc * a.K, a.q, a.fs, *ts, parts, st);
+    if (a.S.d == 2) return spread_tiled(a.S, a.M, a.cells, 2 * a.nc * a.K, a.q, a.fs, *ts, parts, st);
+    return spread_tiled3(a.S, a.M, a.cells, 2 * a.nc * a.K, a.q, a.fs, *ts, parts, st);
   }
   MRSR_REQUIRE(a.cells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "spreading grid of 2^32 cells or more");
   const int* order = ts && a.S.d == 3 ? ts->order.as<int>() : nullptr;
@@ -1041,10 +1244,12 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
   MRSR_TRY(fG.init(d, G));
   const float* ipsi[3] = {nullptr, nullptr, nullptr};
   for (int i = 0; i < d; ++i) MRSR_TRY(es_inv_psi_table(M[i], -G[i] / 2, G[i] + 1, &ipsi[i]));
-  // channel batches of ~2 GB of upsampled float2 grid
+  // channel batches of ~2 GB of upsampled float2 grid; the 3D tile-sorted kernel takes four
+  // parts per pass, so a 3D batch holds at least four channels' parts (8-12 GB on 512^3)
   const int nq = u_complex ? 2 : 1;  // a real basis spreads real values
   const int64_t max_bytes = 2ll << 30;
-  const int pb = (int)std::max<int64_t>(1, std::min<int64_t>(P, max_bytes / (mcells * (int64_t)sizeof(float2))));
+  int pb = (int)std::max<int64_t>(1, std::min<int64_t>(P, max_bytes / (mcells * (int64_t)sizeof(float2))));
+  if (d == 3) pb = std::max(pb, std::min(P, kP3 / nq));
   DevBuf grid, qgrid, cgrid, fsb;
   MRSR_TRY(grid.alloc(sizeof(float2) * mcells * pb));
   MRSR_TRY(qgrid.alloc(sizeof(long long) * nq * mcells * pb));
@@ -1067,6 +1272,7 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
     MRSR_TRY(ts.prep(S, MRSR_DCF_NONE, nullptr, st));
   } else if (ordered) {
     MRSR_TRY(ts.build3(S, M, st));
+    if (S.ns_pf * S.nt < (1ll << 31)) MRSR_TRY(ts.prep3(S, MRSR_DCF_NONE, nullptr, st));
   }
   const TileSort* tsp = tiled || ordered ? &ts : nullptr;
   MRSR_TRY(packed.alloc((u_complex ? 8 : 4) * (size_t)P * std::max<int64_t>(*nk_out, 1)));
@@ -1378,7 +1584,8 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
   int cc = (int)std::max<int64_t>(1, std::min<int64_t>(ncoils, max_bytes / std::max<int64_t>(per_coil, 1)));
   // 3D with a basis: the batch's parts (2 per coil and coefficient) interleaved per cell, at
   // most 32 (one per lane of k_spread_data_cp)
-  const bool parts_layout = ndims == 3 && U != nullptr && 2 * K <= 32;
+  const bool tiled3 = ndims == 3 && U != nullptr && sl.set.n < (1ll << 31) && ns_per_frame * nt < (1ll << 31);
+  const bool parts_layout = ndims == 3 && U != nullptr && !tiled3 && 2 * K <= 32;
   if (parts_layout) cc = std::min(cc, 16 / K);
   DevBuf grid, qgrid, fsb;
   MRSR_TRY(grid.alloc((size_t)per_coil * cc));
@@ -1415,6 +1622,7 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
   }
   const bool ordered = ndims == 3 && sl.set.n < (1ll << 31);
   if (ordered) MRSR_TRY(ts.build3(sl.set, M, st));
+  if (tiled3) MRSR_TRY(ts.prep3(sl.set, dcf_kind, dcf_array, st));
   const int64_t out_elems = nimg * K * (cmaps ? 1 : ncoils);
   if (cmaps) MRSR_CHECK_CUDA(cudaMemsetAsync(out, 0, sizeof(float2) * out_elems, st));
   for (int c0 = 0; c0 < ncoils; c0 += cc) {

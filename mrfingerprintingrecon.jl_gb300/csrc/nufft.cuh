@@ -133,16 +133,20 @@ struct SpreadLambdaArgs {
 // Samples of a 2D set counting-sorted by the 12 x 12 tile of the grid M0 x M1 that holds
 // their first tap, in chunks of at most 1024 samples (the work items of the tile-sorted
 // spreading kernels).  Built once per sample set and grid, shared by every spread of it.
-// build3: for a 3D set, only `order`, by 8 x 8 x 8 tiles (the global kernels then take
-// samples in that order, so the warps in flight touch neighbouring grid lines in L2).
+// build3: for a 3D set, `order` and work items by 8 x 8 x 8 tiles (the global kernels take
+// samples in that order, so the warps in flight touch neighbouring grid lines in L2; the
+// 3D tile-sorted kernel takes the items).
 // prep: the per-sample tap records the 2D tile-sorted kernels read (weights with the
 // density compensation folded in, first tap, sample index and frame), after build.
+// prep3: the same records for the 3D tile-sorted kernels, after build3.
 struct TileSort {
   DevBuf counts, offset, choff, cursor, tile_of, order, items, nitems, next, rec;
-  int ntx = 0, ntiles = 0, m0 = 0, m1 = 0;
+  int ntx = 0, nty = 0, ntiles = 0, m0 = 0, m1 = 0, m2 = 0;
+  bool rec3 = false;
   int build(const SampleSet& S, int64_t M0, int64_t M1, cudaStream_t st);
   int build3(const SampleSet& S, const int64_t* M, cudaStream_t st);
   int prep(const SampleSet& S, int dcf_kind, const float* dcf, cudaStream_t st);
+  int prep3(const SampleSet& S, int dcf_kind, const float* dcf, cudaStream_t st);
 };
 
 // ts: tile sort of a.S on a.M.  2D: the tile-sorted kernel; 3D (ts from build3, or null):
