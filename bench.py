@@ -373,7 +373,7 @@ def gb300_arm(args, world, rank, local):
     lam_bytes = 2.0 * cg * K * N2 * G1 * esz + nk * P * lsz      # stack in + out, Λ once
     achieved = lam_bytes / (lam_avg * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    lam_kernel = {"fp32": "k4_lambda", "fp16": "kh_lambda", "fp16-tc": "kt_lambda"}[prec]
+    lam_kernel = {"fp32": "k8_lambda", "fp16": "kh_lambda", "fp16-tc": "kt_lambda"}[prec]
     traffic = profile_traffic(lam_kernel)
     apply_bytes = N1 * N2 * K * 16 + 2 * Nc * N1 * N2 * 8 + 4 * Nc * (G1 * N2 * K) * esz + nk * P * lsz
     # the mixed-precision tensor-core operator on the same kernel and inputs, same protocol

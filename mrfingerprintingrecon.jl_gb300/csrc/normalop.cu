@@ -555,6 +555,8 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       if (op->precision == MRSR_PREC_FP16_TC) {
         a.lam = op->lam_tc.p;
         MRSR_TRY(tc_lambda(a, ncg, op->lam_max.as<float>(), op->tc_consts.p, op->errflag.as<int>(), st));
+      } else if (lambda8_supported(a)) {
+        MRSR_TRY(fast_lambda8(a, ncl, st));
       } else if (fast_length(Ll))
         MRSR_TRY(fast_lambda(a, ncl, op->Cg * K, op->errflag.as<int>(), st));
       else
