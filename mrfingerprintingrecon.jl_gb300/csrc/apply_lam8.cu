@@ -1,21 +1,22 @@
-// Λ pass of the float32 operator for 512-point lines (the 256^2 NFFT operator's columns) as
-// three radix-8 steps each way: 512 = 8 x 8 x 8,
-//   n = 64 n1 + 8 n2 + n3,  f = f1 + 8 f2 + 64 f3,
-//   X[f] = sum_n3 w8^(n3 f3) w64^(n3 f2) sum_n2 w8^(n2 f2) [w512^((8 n2 + n3) f1) sum_n1 w8^(n1 f1) x[n]]
-// with the input pruned to n1 < 4 (the zero-padded half) and the inverse's output to n1 < 4
-// (the kept half).  Every task holds eight values (one DFT-8), so the kernel fits in 64
-// registers and runs 512-thread CTAs two per SM: 32 warps per SM against 16 for the
-// two-step radix-16 x 32 kernel (apply_lam.cu), which is bound by latency, not by its
-// arithmetic.  The price is one more shared-memory exchange each way.
+// Λ pass of the float32 operator as three DFT steps each way for the two line lengths the
+// operators mostly use, L = R1 x 8 x 8: R1 = 8 (512-point lines, the 256^2 images' columns)
+// and R1 = 4 (256-point lines, the 128^3 volumes'):
+//   n = 64 n1 + 8 n2 + n3,  f = f1 + R1 f2 + 8 R1 f3,
+//   X[f] = sum_n3 w8^(n3 f3) w64^(n3 f2) sum_n2 w8^(n2 f2) [wL^((8 n2 + n3) f1) sum_n1 wR1^(n1 f1) x[n]]
+// with the input pruned to n1 < R1 / 2 (the zero-padded half) and the inverse's output to
+// n1 < R1 / 2 (the kept half).  Every task holds at most eight values (one DFT-8), so the
+// kernel fits in 64 registers and runs 512-thread CTAs two per SM: 32 warps per SM against 16
+// for the two-step kernels (apply_lam.cu), which are bound by latency, not by arithmetic.
+// The price is one more shared-memory exchange each way.
 // src/NFFTNormalOp.jl:227-267 / ext/MRISubspaceReconCUDAExt/NFFTNormalOp.jl:193-218.
 //
-// Shared layout of plane k, column li (TC = 4 columns per tile): position (a, b, c) of three
-// octal digits at k * 2336 + a * 292 + b * 36 + c * 4 + li (float2 units).  Every step's warp
-// varies li and one of a, b, c (the rest fixed); the strides are 4 (mod 16), so the 16 lanes
-// of a half-warp touch 16 distinct 8-byte bank pairs for any of the three, and a task's
-// running digit is a compile-time loop index, so its eight addresses are one register plus
-// immediate offsets.  A task reads and writes the same eight positions (one digit running),
-// so every step works in place.
+// Shared layout of plane k, column li (TC = 4 or 8 columns per tile): position (a, b, c) of
+// the three digits at k * SP + a * SA + b * SB + c * TC + li (float2 units).  Every step's warp
+// varies li and one of a, b, c (the rest fixed); SA and SB are TC (mod 16), so the 16 lanes of
+// a half-warp (16 / TC values of the running digit) touch 16 distinct 8-byte bank pairs for
+// any of the three, and a task's running digit is a compile-time loop index, so its addresses
+// are one register plus immediate offsets.  A task reads and writes the same positions (one
+// digit running), so every step works in place.
 #include "fft4.cuh"
 #include "passes.cuh"
 
@@ -23,52 +24,77 @@ namespace mrsr {
 
 namespace {
 
-constexpr int kL8 = 512, kTC8 = 4, kL8Threads = 512;
+constexpr int kL8Threads = 512;
+constexpr int kL8MaxK = 6;
+constexpr size_t kL8MaxSmem = 227 * 1024;
 
-constexpr int kSB8 = 36, kSA8 = 292, kSP8 = 2336;  // digit b, digit a and plane strides
-static_assert(kSB8 >= 8 * 4 && kSA8 >= 8 * kSB8 && kSP8 >= 8 * kSA8, "8 x 8 x 8 positions x 4 columns");
-static_assert(kSB8 % 16 == 4 && kSA8 % 16 == 4, "a half-warp on 16 distinct bank pairs");
-
-__device__ __forceinline__ int p8(int k, int a, int b, int c, int li) { return k * kSP8 + a * kSA8 + b * kSB8 + c * 4 + li; }
+template <int R1_, int TC_>
+struct L8 {
+  static constexpr int R1 = R1_, TC = TC_, L = 64 * R1;
+  static constexpr int LT = TC == 4 ? 2 : 3;  // log2 TC
+  static constexpr int LR = R1 == 4 ? 2 : 3;  // log2 R1
+  static constexpr int SB = 8 * TC + TC, SA = 8 * SB + TC, SP = R1 * SA;  // digit b, digit a, plane
+  static constexpr int T1 = R1 * 64, T2 = 64, T3 = 64, TW = T1 + T2 + T3;  // twiddle tables
+  static constexpr int NT1 = TC * 64;      // tasks per plane of the steps running n1 / f1
+  static constexpr int NT2 = TC * 8 * R1;  // tasks per plane of the other steps
+  static_assert((TC == 4 || TC == 8) && (R1 == 4 || R1 == 8), "tile of 4 or 8 columns, L = 256 or 512");
+  static_assert(SB % 16 == TC && SA % 16 == TC, "a half-warp on 16 distinct bank pairs");
+  static constexpr size_t smem(int K) { return sizeof(float2) * ((size_t)TW + (size_t)K * SP); }
+  static __device__ __forceinline__ int at(int k, int a, int b, int c, int li) { return k * SP + a * SA + b * SB + c * TC + li; }
+};
 
 __device__ __forceinline__ float2 cj(float2 w) { return make_float2(w.x, -w.y); }
 
-// Twiddle tables in the order the steps' lanes read them (a warp's lanes vary n3 or f2 with
-// the loop digit fixed, so each table read is 8 consecutive entries, bank-conflict free; a
-// table indexed (m * f) & 511 would put the lanes of an even f on the same banks):
-//   t1[f1 * 64 + m] = w512^(m f1), m = 8 n2 + n3     (F1, I2 conjugated)
-//   t2[f2 * 8 + n3] = w64^(n3 f2)                    (F2)
-//   t3[n3 * 8 + f2] = w64^(-n3 f2)                   (I1)
-constexpr int kT1 = 512, kT2 = 64, kT3 = 64, kTwTables = kT1 + kT2 + kT3;
+// 16-byte global -> shared copy that bypasses L1 (cp.async.cg); both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async16(float2* dst, const float2* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+// Closes the thread's copies into one group / waits for it (the caller's barrier then makes
+// every thread's copies visible to the CTA).
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// Twiddle tables in the order the steps' lanes read them (a warp's lanes vary n3 or f2 with
+// the loop digit fixed, so each table read is consecutive entries, bank-conflict free; a
+// table indexed (m * f) mod L would put the lanes of an even f on the same banks):
+//   t1[f1 * 64 + m] = wL^(m f1), m = 8 n2 + n3     (F1, I2 conjugated)
+//   t2[f2 * 8 + n3] = w64^(n3 f2)                  (F2)
+//   t3[n3 * 8 + f2] = w64^(-n3 f2)                 (I1)
+template <class C>
 __device__ __forceinline__ void build_tables(float2* t, const FftPlan& pl) {
-  const float2* w = pl.tw;  // w512^p
-  for (int i = threadIdx.x; i < kTwTables; i += blockDim.x) {
+  const float2* w = pl.tw;  // wL^p
+  for (int i = threadIdx.x; i < C::TW; i += blockDim.x) {
     int p;
     bool conj = false;
-    if (i < kT1) {
+    if (i < C::T1) {
       p = (i & 63) * (i >> 6);
-    } else if (i < kT1 + kT2) {
-      const int j = i - kT1;
-      p = 8 * (j & 7) * (j >> 3);
+    } else if (i < C::T1 + C::T2) {
+      const int j = i - C::T1;
+      p = C::R1 * (j & 7) * (j >> 3);
     } else {
-      const int j = i - kT1 - kT2;
-      p = 8 * (j >> 3) * (j & 7);
+      const int j = i - C::T1 - C::T2;
+      p = C::R1 * (j >> 3) * (j & 7);
       conj = true;
     }
-    const float2 v = w[p & (kL8 - 1)];
+    const float2 v = w[p & (C::L - 1)];
     t[i] = conj ? cj(v) : v;
   }
 }
 
-template <int KK>
+template <class C, int KK>
 __device__ __forceinline__ void lam8_voxels(const LamPassArgs& a, float2* sm, int64_t tile) {
-  const int64_t pstride = (int64_t)a.FC * kTC8;
-  constexpr int T = kL8 * kTC8;
+  const int64_t pstride = (int64_t)a.FC * C::TC;
+  constexpr int T = C::L * C::TC;
   auto lbase_of = [&](int t) -> int64_t {
-    const int f = t >> 2;
+    const int f = t >> C::LT;
     const int ch = (int)a.fcd.div((uint32_t)f), fc = f - ch * a.FC;
-    return (((tile * a.NCH + ch) * a.P) * (int64_t)a.FC + fc) * kTC8 + (t & 3);
+    return (((tile * a.NCH + ch) * a.P) * (int64_t)a.FC + fc) * C::TC + (t & (C::TC - 1));
+  };
+  // X[f] of column li sits at (f1, f2, f3) = (f mod R1, (f / R1) mod 8, f / (8 R1))
+  auto pos0 = [](int t) {
+    const int li = t & (C::TC - 1), f = t >> C::LT;
+    return C::at(0, f & (C::R1 - 1), (f >> C::LR) & 7, f >> (C::LR + 3), li);
   };
   if (a.lam_mode == LAM_PACKED_REAL) {
     constexpr int P = KK * (KK + 1) / 2;
@@ -78,149 +104,176 @@ __device__ __forceinline__ void lam8_voxels(const LamPassArgs& a, float2* sm, in
       float lc[P];
 #pragma unroll
       for (int p = 0; p < P; ++p) lc[p] = lam[lb + p * pstride];
-      const int li = t & 3, f = t >> 2;
-      const int f1 = f & 7, f2 = (f >> 3) & 7, f3 = f >> 6;
+      const int p0 = pos0(t);
       float2 X[KK], Y[KK];
 #pragma unroll
-      for (int k = 0; k < KK; ++k) X[k] = sm[p8(k, f1, f2, f3, li)];
+      for (int k = 0; k < KK; ++k) X[k] = sm[p0 + k * C::SP];
       lam_real_regs<KK>(lc, X, Y);
 #pragma unroll
-      for (int k = 0; k < KK; ++k) sm[p8(k, f1, f2, f3, li)] = Y[k];
+      for (int k = 0; k < KK; ++k) sm[p0 + k * C::SP] = Y[k];
     }
     return;
   }
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
-    const int li = t & 3, f = t >> 2;
-    const int f1 = f & 7, f2 = (f >> 3) & 7, f3 = f >> 6;
+    const int p0 = pos0(t);
     float2 X[KK], Y[KK];
 #pragma unroll
-    for (int k = 0; k < KK; ++k) X[k] = sm[p8(k, f1, f2, f3, li)];
+    for (int k = 0; k < KK; ++k) X[k] = sm[p0 + k * C::SP];
     lam_apply_ptr<KK>(a.lam_mode, KK, a.lam, lbase_of(t), pstride, X, Y);
 #pragma unroll
-    for (int k = 0; k < KK; ++k) sm[p8(k, f1, f2, f3, li)] = Y[k];
+    for (int k = 0; k < KK; ++k) sm[p0 + k * C::SP] = Y[k];
   }
 }
 
-template <int KK>
+template <class C, int KK>
 __global__ void __launch_bounds__(kL8Threads, 2) k8_lambda(LamPassArgs a) {
+  constexpr int R1 = C::R1, TC = C::TC, LT = C::LT, LR = C::LR, H = R1 / 2;
   extern __shared__ float2 smem[];
   float2* t1 = smem;                 // twiddle tables
-  const float2* t2 = smem + kT1;
-  const float2* t3 = smem + kT1 + kT2;
-  float2* sm = smem + kTwTables;     // positions p8(k, a, b, c, li)
-  build_tables(t1, a.pl);
+  const float2* t2 = smem + C::T1;
+  const float2* t3 = smem + C::T1 + C::T2;
+  float2* sm = smem + C::TW;         // positions C::at(k, a, b, c, li)
   const int cl = (int)(blockIdx.x % (unsigned)a.ncg);
   const int64_t tile = blockIdx.x / (unsigned)a.ncg;
   const int64_t plane = (int64_t)a.nrow * a.inner;
-  float2* base = a.stack + (int64_t)cl * KK * plane + tile * kTC8;
-  constexpr int NT = KK * 256;  // tasks per step: k, two octal digits, li
+  float2* base = a.stack + (int64_t)cl * KK * plane + tile * TC;
+  constexpr int N1 = KK * C::NT1, N2 = KK * C::NT2;
+  // Stage the tile's input (rows n1 < R1/2) into the upper digit slots a = R1/2 + n1 with
+  // 16-byte asynchronous copies, all issued before anything waits on them, so the loads of
+  // a CTA are in flight together; F1 reads them back and, in place, overwrites them.
+  {
+    constexpr int NC = KK * H * 64 * (TC / 2);  // 16-byte chunks: two columns each
+    for (int c = threadIdx.x; c < NC; c += blockDim.x) {
+      const int j = c & (TC / 2 - 1), r = c >> (LT - 1);
+      const int n3 = r & 7, n2 = (r >> 3) & 7, n1 = (r >> 6) % H, k = (r >> 6) / H;
+      cp_async16(sm + C::at(k, H + n1, n2, n3, 2 * j), base + k * plane + (int64_t)(64 * n1 + 8 * n2 + n3) * a.inner + 2 * j);
+    }
+    cp_async_commit();
+  }
+  build_tables<C>(t1, a.pl);
+  cp_async_wait_all();
   __syncthreads();
-  // F1: DFT-8 over n1 (n1 < 4 nonzero) -> f1, twiddle w512^((8 n2 + n3) f1); position (f1, n2, n3)
-  for (int t = threadIdx.x; t < NT; t += blockDim.x) {
-    const int li = t & 3, n3 = (t >> 2) & 7, n2 = (t >> 5) & 7, k = t >> 8;
-    float2 v[8];
+  // F1: DFT-R1 over n1 (n1 < R1/2 nonzero) -> f1, twiddle wL^((8 n2 + n3) f1); position (f1, n2, n3)
+  for (int t = threadIdx.x; t < N1; t += blockDim.x) {
+    const int li = t & (TC - 1), n3 = (t >> LT) & 7, n2 = (t >> (LT + 3)) & 7, k = t >> (LT + 6);
+    float2 v[R1];
 #pragma unroll
-    for (int n1 = 0; n1 < 4; ++n1) v[n1] = base[k * plane + (int64_t)(64 * n1 + 8 * n2 + n3) * a.inner + li];
+    for (int n1 = 0; n1 < H; ++n1) v[n1] = sm[C::at(k, H + n1, n2, n3, li)];
 #pragma unroll
-    for (int n1 = 4; n1 < 8; ++n1) v[n1] = make_float2(0.f, 0.f);
-    RDft<8, -1>::run(v);
+    for (int n1 = H; n1 < R1; ++n1) v[n1] = make_float2(0.f, 0.f);
+    RDft<R1, -1>::run(v);
     const int m = 8 * n2 + n3;
 #pragma unroll
-    for (int f1 = 0; f1 < 8; ++f1) sm[p8(k, f1, n2, n3, li)] = f1 == 0 ? v[0] : cmul(v[f1], t1[f1 * 64 + m]);
+    for (int f1 = 0; f1 < R1; ++f1) sm[C::at(k, f1, n2, n3, li)] = f1 == 0 ? v[0] : cmul(v[f1], t1[f1 * 64 + m]);
   }
   __syncthreads();
-  // F2: DFT-8 over n2 -> f2, twiddle w64^(n3 f2) = w512^(8 n3 f2); position (f1, f2, n3)
-  for (int t = threadIdx.x; t < NT; t += blockDim.x) {
-    const int li = t & 3, n3 = (t >> 2) & 7, f1 = (t >> 5) & 7, k = t >> 8;
+  // F2: DFT-8 over n2 -> f2, twiddle w64^(n3 f2); position (f1, f2, n3)
+  for (int t = threadIdx.x; t < N2; t += blockDim.x) {
+    const int li = t & (TC - 1), n3 = (t >> LT) & 7, f1 = (t >> (LT + 3)) & (R1 - 1), k = t >> (LT + 3 + LR);
     float2 v[8];
 #pragma unroll
-    for (int n2 = 0; n2 < 8; ++n2) v[n2] = sm[p8(k, f1, n2, n3, li)];
+    for (int n2 = 0; n2 < 8; ++n2) v[n2] = sm[C::at(k, f1, n2, n3, li)];
     RDft<8, -1>::run(v);
 #pragma unroll
-    for (int f2 = 0; f2 < 8; ++f2) sm[p8(k, f1, f2, n3, li)] = f2 == 0 ? v[0] : cmul(v[f2], t2[f2 * 8 + n3]);
+    for (int f2 = 0; f2 < 8; ++f2) sm[C::at(k, f1, f2, n3, li)] = f2 == 0 ? v[0] : cmul(v[f2], t2[f2 * 8 + n3]);
   }
   __syncthreads();
-  // F3: DFT-8 over n3 -> f3; X[f1 + 8 f2 + 64 f3] at position (f1, f2, f3)
-  for (int t = threadIdx.x; t < NT; t += blockDim.x) {
-    const int li = t & 3, f2 = (t >> 2) & 7, f1 = (t >> 5) & 7, k = t >> 8;
+  // F3: DFT-8 over n3 -> f3; X[f1 + R1 f2 + 8 R1 f3] at position (f1, f2, f3)
+  for (int t = threadIdx.x; t < N2; t += blockDim.x) {
+    const int li = t & (TC - 1), f2 = (t >> LT) & 7, f1 = (t >> (LT + 3)) & (R1 - 1), k = t >> (LT + 3 + LR);
     float2 v[8];
 #pragma unroll
-    for (int n3 = 0; n3 < 8; ++n3) v[n3] = sm[p8(k, f1, f2, n3, li)];
+    for (int n3 = 0; n3 < 8; ++n3) v[n3] = sm[C::at(k, f1, f2, n3, li)];
     RDft<8, -1>::run(v);
 #pragma unroll
-    for (int f3 = 0; f3 < 8; ++f3) sm[p8(k, f1, f2, f3, li)] = v[f3];
+    for (int f3 = 0; f3 < 8; ++f3) sm[C::at(k, f1, f2, f3, li)] = v[f3];
   }
   __syncthreads();
-  lam8_voxels<KK>(a, sm, tile);
+  lam8_voxels<C, KK>(a, sm, tile);
   __syncthreads();
   // I1: inverse DFT-8 over f3 -> n3, twiddle w64^(-n3 f2); position (f1, f2, n3)
-  for (int t = threadIdx.x; t < NT; t += blockDim.x) {
-    const int li = t & 3, f2 = (t >> 2) & 7, f1 = (t >> 5) & 7, k = t >> 8;
+  for (int t = threadIdx.x; t < N2; t += blockDim.x) {
+    const int li = t & (TC - 1), f2 = (t >> LT) & 7, f1 = (t >> (LT + 3)) & (R1 - 1), k = t >> (LT + 3 + LR);
     float2 v[8];
 #pragma unroll
-    for (int f3 = 0; f3 < 8; ++f3) v[f3] = sm[p8(k, f1, f2, f3, li)];
+    for (int f3 = 0; f3 < 8; ++f3) v[f3] = sm[C::at(k, f1, f2, f3, li)];
     RDft<8, +1>::run(v);
 #pragma unroll
-    for (int n3 = 0; n3 < 8; ++n3) sm[p8(k, f1, f2, n3, li)] = n3 == 0 ? v[0] : cmul(v[n3], t3[n3 * 8 + f2]);
+    for (int n3 = 0; n3 < 8; ++n3) sm[C::at(k, f1, f2, n3, li)] = n3 == 0 ? v[0] : cmul(v[n3], t3[n3 * 8 + f2]);
   }
   __syncthreads();
-  // I2: inverse DFT-8 over f2 -> n2, twiddle w512^(-(8 n2 + n3) f1); position (f1, n2, n3)
-  for (int t = threadIdx.x; t < NT; t += blockDim.x) {
-    const int li = t & 3, n3 = (t >> 2) & 7, f1 = (t >> 5) & 7, k = t >> 8;
+  // I2: inverse DFT-8 over f2 -> n2, twiddle wL^(-(8 n2 + n3) f1); position (f1, n2, n3)
+  for (int t = threadIdx.x; t < N2; t += blockDim.x) {
+    const int li = t & (TC - 1), n3 = (t >> LT) & 7, f1 = (t >> (LT + 3)) & (R1 - 1), k = t >> (LT + 3 + LR);
     float2 v[8];
 #pragma unroll
-    for (int f2 = 0; f2 < 8; ++f2) v[f2] = sm[p8(k, f1, f2, n3, li)];
+    for (int f2 = 0; f2 < 8; ++f2) v[f2] = sm[C::at(k, f1, f2, n3, li)];
     RDft<8, +1>::run(v);
 #pragma unroll
     for (int n2 = 0; n2 < 8; ++n2)
-      sm[p8(k, f1, n2, n3, li)] = f1 == 0 ? v[n2] : cmul(v[n2], cj(t1[f1 * 64 + 8 * n2 + n3]));
+      sm[C::at(k, f1, n2, n3, li)] = f1 == 0 ? v[n2] : cmul(v[n2], cj(t1[f1 * 64 + 8 * n2 + n3]));
   }
   __syncthreads();
-  // I3: inverse DFT-8 over f1 -> n1, the kept half n1 < 4 written back
-  for (int t = threadIdx.x; t < NT; t += blockDim.x) {
-    const int li = t & 3, n3 = (t >> 2) & 7, n2 = (t >> 5) & 7, k = t >> 8;
-    float2 v[8];
+  // I3: inverse DFT-R1 over f1 -> n1, the kept half n1 < R1/2 written back
+  for (int t = threadIdx.x; t < N1; t += blockDim.x) {
+    const int li = t & (TC - 1), n3 = (t >> LT) & 7, n2 = (t >> (LT + 3)) & 7, k = t >> (LT + 6);
+    float2 v[R1];
 #pragma unroll
-    for (int f1 = 0; f1 < 8; ++f1) v[f1] = sm[p8(k, f1, n2, n3, li)];
-    RDft<8, +1>::run(v);
+    for (int f1 = 0; f1 < R1; ++f1) v[f1] = sm[C::at(k, f1, n2, n3, li)];
+    RDft<R1, +1>::run(v);
 #pragma unroll
-    for (int n1 = 0; n1 < 4; ++n1) base[k * plane + (int64_t)(64 * n1 + 8 * n2 + n3) * a.inner + li] = v[n1];
+    for (int n1 = 0; n1 < H; ++n1) base[k * plane + (int64_t)(64 * n1 + 8 * n2 + n3) * a.inner + li] = v[n1];
   }
 }
 
-template <int KK>
+template <class C, int KK>
 int launch8(const LamPassArgs& a, dim3 grid, cudaStream_t st) {
-  const size_t smem = sizeof(float2) * ((size_t)kTwTables + (size_t)KK * kSP8);
-  MRSR_REQUIRE(smem <= 227 * 1024, MRSR_ERR_UNSUPPORTED, "shared memory request %zu too large", smem);
-  MRSR_CHECK_CUDA(cudaFuncSetAttribute(k8_lambda<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k8_lambda<KK><<<grid, kL8Threads, smem, st>>>(a);
-  MRSR_LAUNCH_CHECK();
-  return MRSR_OK;
+  if constexpr (C::smem(KK) > kL8MaxSmem) {
+    return MRSR_ERR_UNSUPPORTED;
+  } else {
+    constexpr size_t smem = C::smem(KK);
+    MRSR_CHECK_CUDA(cudaFuncSetAttribute(k8_lambda<C, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k8_lambda<C, KK><<<grid, kL8Threads, smem, st>>>(a);
+    MRSR_LAUNCH_CHECK();
+    return MRSR_OK;
+  }
+}
+
+template <class C>
+int dispatch8(const LamPassArgs& a, dim3 grid, cudaStream_t st) {
+  static_assert(kL8MaxK == 6, "one case per K");
+  switch (a.K) {
+    case 1: return launch8<C, 1>(a, grid, st);
+    case 2: return launch8<C, 2>(a, grid, st);
+    case 3: return launch8<C, 3>(a, grid, st);
+    case 4: return launch8<C, 4>(a, grid, st);
+    case 5: return launch8<C, 5>(a, grid, st);
+    default: return launch8<C, 6>(a, grid, st);
+  }
+}
+
+size_t smem8(int L, int TC, int K) {
+  if (L == 512) return TC == 4 ? L8<8, 4>::smem(K) : L8<8, 8>::smem(K);
+  return TC == 4 ? L8<4, 4>::smem(K) : L8<4, 8>::smem(K);
 }
 
 }  // namespace
 
 bool lambda8_supported(const LamPassArgs& a) {
-  return a.pl.L == kL8 && a.TC == kTC8 && a.nin == kL8 / 2 && a.nout == kL8 / 2 && !lam_is_diag(a.lam_mode) &&
-         a.K >= 1 && a.K <= 8 && a.inner % kTC8 == 0;
+  const bool shape = (a.pl.L == 512 || a.pl.L == 256) && (a.TC == 4 || a.TC == 8);
+  return shape && a.nin == a.pl.L / 2 && a.nout == a.pl.L / 2 && !lam_is_diag(a.lam_mode) && a.K >= 1 &&
+         a.K <= kL8MaxK && smem8(a.pl.L, a.TC, a.K) <= kL8MaxSmem && a.inner % a.TC == 0 &&
+         (reinterpret_cast<uintptr_t>(a.stack) & 15) == 0;  // 16-byte staging copies
 }
 
 int fast_lambda8(const LamPassArgs& a, int ncg, cudaStream_t st) {
-  MRSR_REQUIRE(lambda8_supported(a), MRSR_ERR_UNSUPPORTED, "radix-8 Λ pass: 512-point pruned lines only");
+  MRSR_REQUIRE(lambda8_supported(a), MRSR_ERR_UNSUPPORTED, "three-step Λ pass: 256- or 512-point pruned lines only");
   LamPassArgs b = a;
   b.ncg = ncg;
   b.fcd = FastDiv((uint32_t)a.FC);
-  const dim3 grid((unsigned)((a.inner / kTC8) * ncg));
-  switch (a.K) {
-    case 1: return launch8<1>(b, grid, st);
-    case 2: return launch8<2>(b, grid, st);
-    case 3: return launch8<3>(b, grid, st);
-    case 4: return launch8<4>(b, grid, st);
-    case 5: return launch8<5>(b, grid, st);
-    case 6: return launch8<6>(b, grid, st);
-    case 7: return launch8<7>(b, grid, st);
-    default: return launch8<8>(b, grid, st);
-  }
+  const dim3 grid((unsigned)((a.inner / a.TC) * ncg));
+  if (a.pl.L == 512) return a.TC == 4 ? dispatch8<L8<8, 4>>(b, grid, st) : dispatch8<L8<8, 8>>(b, grid, st);
+  return a.TC == 4 ? dispatch8<L8<4, 4>>(b, grid, st) : dispatch8<L8<4, 8>>(b, grid, st);
 }
 
 }  // namespace mrsr

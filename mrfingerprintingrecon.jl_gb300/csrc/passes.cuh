@@ -163,7 +163,7 @@ __device__ __forceinline__ void lam_apply(const LamPassArgs& a, int64_t lbase, i
 bool fast_length(int L);
 int fast_rows_fwd(const RowsFwdArgs& a, int64_t nrows, int ncg, cudaStream_t st);
 int fast_lambda(const LamPassArgs& a, int ncg, int planes_total, int* errword, cudaStream_t st);
-// radix-8 three-step Λ pass (apply_lam8.cu): 512-point lines pruned to half, 4-column tiles
+// three-step Λ pass (apply_lam8.cu): 256- or 512-point lines pruned to half, 4- or 8-column tiles, K <= 6
 bool lambda8_supported(const LamPassArgs& a);
 int fast_lambda8(const LamPassArgs& a, int ncg, cudaStream_t st);
 int fast_mid(const MidArgs& a, int nplanes, cudaStream_t st);

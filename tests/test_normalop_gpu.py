@@ -50,6 +50,11 @@ def _problem(seed, img, K, Nc, density=0.8, complex_lam=True):
     ((32, 64, 32), 3, 2, True),  # 3D mixed: 64 / 128
     ((256, 256), 5, 3, False),   # K = 5 on 512-point columns (the benchmark's Λ pass)
     ((128, 256), 5, 2, True),    # the same with a complex kernel
+    ((64, 128), 3, 2, True),     # three-step Λ pass at 256 points (4 x 8 x 8), 8-column tiles
+    ((10, 128), 4, 2, True),     # the same with 4-column tiles (plane width 20)
+    ((64, 256), 2, 2, False),    # 512 points with 8-column tiles (K = 2)
+    ((96, 128), 6, 2, False),    # K = 6, the largest the three-step kernel takes
+    ((16, 16, 128), 3, 2, True), # 3D with a 256-point last axis
 ])
 def test_nfft_apply_matches_oracle(mr, cuda, img, K, Nc, cplx):
     lam, cells, cm, x = _problem(1, img, K, Nc, complex_lam=cplx)
