@@ -82,68 +82,84 @@ __device__ __forceinline__ void build_tables(float2* t, const FftPlan& pl) {
   }
 }
 
+// Every step runs a fixed set of tasks per thread: task t = tid + 512 i, and since the tasks
+// of one plane (or, for the voxel step, the frequencies of two Λ chunks) number a divisor of
+// 512, the digits a thread owns are the same in every round i and only the plane (or f3)
+// moves, by a compile-time step.  So each thread forms its addresses and loads its twiddles
+// once per step, and the rounds are unrolled with immediate offsets.
+template <int N, class F>
+__device__ __forceinline__ void rounds(F&& body) {
+  constexpr int IT = (N + kL8Threads - 1) / kL8Threads;
+#pragma unroll
+  for (int i = 0; i < IT; ++i) {
+    if (N % kL8Threads != 0 && (int)threadIdx.x + i * kL8Threads >= N) break;
+    body(i);
+  }
+}
+
 template <class C, int KK>
 __device__ __forceinline__ void lam8_voxels(const LamPassArgs& a, float2* sm, int64_t tile) {
-  const int64_t pstride = (int64_t)a.FC * C::TC;
   constexpr int T = C::L * C::TC;
-  auto lbase_of = [&](int t) -> int64_t {
-    const int f = t >> C::LT;
-    const int ch = (int)a.fcd.div((uint32_t)f), fc = f - ch * a.FC;
-    return (((tile * a.NCH + ch) * a.P) * (int64_t)a.FC + fc) * C::TC + (t & (C::TC - 1));
-  };
+  // two Λ chunks (FC * TC = 256 entries each) per round: entry p of the chunk is 256 apart
+  constexpr int PS = 256, DF = kL8Threads / C::TC;  // frequencies per round
+  constexpr int DPOS = DF / (8 * C::R1) * C::TC;      // f3 += DF / (8 R1)
+  const int tid = threadIdx.x, li = tid & (C::TC - 1), f = tid >> C::LT;
+  const int ch = (int)a.fcd.div((uint32_t)f), fc = f - ch * a.FC;
+  const float* lam0 = nullptr;
+  const int64_t lb0 = (((tile * a.NCH + ch) * a.P) * (int64_t)a.FC + fc) * C::TC + li;
   // X[f] of column li sits at (f1, f2, f3) = (f mod R1, (f / R1) mod 8, f / (8 R1))
-  auto pos0 = [](int t) {
-    const int li = t & (C::TC - 1), f = t >> C::LT;
-    return C::at(0, f & (C::R1 - 1), (f >> C::LR) & 7, f >> (C::LR + 3), li);
-  };
+  const int p0 = C::at(0, f & (C::R1 - 1), (f >> C::LR) & 7, f >> (C::LR + 3), li);
   if (a.lam_mode == LAM_PACKED_REAL) {
     constexpr int P = KK * (KK + 1) / 2;
-    const float* lam = reinterpret_cast<const float*>(a.lam);
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
-      const int64_t lb = lbase_of(t);
+    lam0 = reinterpret_cast<const float*>(a.lam) + lb0;
+    rounds<T>([&](int i) {
+      const float* lam = lam0 + (int64_t)i * (2 * PS * P);
       float lc[P];
 #pragma unroll
-      for (int p = 0; p < P; ++p) lc[p] = lam[lb + p * pstride];
-      const int p0 = pos0(t);
+      for (int p = 0; p < P; ++p) lc[p] = lam[p * PS];
+      const int q = p0 + i * DPOS;
       float2 X[KK], Y[KK];
 #pragma unroll
-      for (int k = 0; k < KK; ++k) X[k] = sm[p0 + k * C::SP];
+      for (int k = 0; k < KK; ++k) X[k] = sm[q + k * C::SP];
       lam_real_regs<KK>(lc, X, Y);
 #pragma unroll
-      for (int k = 0; k < KK; ++k) sm[p0 + k * C::SP] = Y[k];
-    }
+      for (int k = 0; k < KK; ++k) sm[q + k * C::SP] = Y[k];
+    });
     return;
   }
-  for (int t = threadIdx.x; t < T; t += blockDim.x) {
-    const int p0 = pos0(t);
+  rounds<T>([&](int i) {
+    const int q = p0 + i * DPOS;
     float2 X[KK], Y[KK];
 #pragma unroll
-    for (int k = 0; k < KK; ++k) X[k] = sm[p0 + k * C::SP];
-    lam_apply_ptr<KK>(a.lam_mode, KK, a.lam, lbase_of(t), pstride, X, Y);
+    for (int k = 0; k < KK; ++k) X[k] = sm[q + k * C::SP];
+    lam_apply_ptr<KK>(a.lam_mode, KK, a.lam, lb0 + (int64_t)i * (2 * PS * a.P), PS, X, Y);
 #pragma unroll
-    for (int k = 0; k < KK; ++k) sm[p0 + k * C::SP] = Y[k];
-  }
+    for (int k = 0; k < KK; ++k) sm[q + k * C::SP] = Y[k];
+  });
 }
 
 template <class C, int KK>
 __global__ void __launch_bounds__(kL8Threads, 2) k8_lambda(LamPassArgs a) {
   constexpr int R1 = C::R1, TC = C::TC, LT = C::LT, LR = C::LR, H = R1 / 2;
+  constexpr int N1 = KK * C::NT1, N2 = KK * C::NT2;
+  constexpr int DK1 = kL8Threads / C::NT1 * C::SP, DK2 = kL8Threads / C::NT2 * C::SP;  // plane step per round
+  constexpr int SA = C::SA, SB = C::SB;
   extern __shared__ float2 smem[];
   float2* t1 = smem;                 // twiddle tables
   const float2* t2 = smem + C::T1;
   const float2* t3 = smem + C::T1 + C::T2;
   float2* sm = smem + C::TW;         // positions C::at(k, a, b, c, li)
+  const int tid = threadIdx.x;
   const int cl = (int)(blockIdx.x % (unsigned)a.ncg);
   const int64_t tile = blockIdx.x / (unsigned)a.ncg;
   const int64_t plane = (int64_t)a.nrow * a.inner;
   float2* base = a.stack + (int64_t)cl * KK * plane + tile * TC;
-  constexpr int N1 = KK * C::NT1, N2 = KK * C::NT2;
   // Stage the tile's input (rows n1 < R1/2) into the upper digit slots a = R1/2 + n1 with
   // 16-byte asynchronous copies, all issued before anything waits on them, so the loads of
   // a CTA are in flight together; F1 reads them back and, in place, overwrites them.
   {
     constexpr int NC = KK * H * 64 * (TC / 2);  // 16-byte chunks: two columns each
-    for (int c = threadIdx.x; c < NC; c += blockDim.x) {
+    for (int c = tid; c < NC; c += kL8Threads) {
       const int j = c & (TC / 2 - 1), r = c >> (LT - 1);
       const int n3 = r & 7, n2 = (r >> 3) & 7, n1 = (r >> 6) % H, k = (r >> 6) / H;
       cp_async16(sm + C::at(k, H + n1, n2, n3, 2 * j), base + k * plane + (int64_t)(64 * n1 + 8 * n2 + n3) * a.inner + 2 * j);
@@ -153,76 +169,122 @@ __global__ void __launch_bounds__(kL8Threads, 2) k8_lambda(LamPassArgs a) {
   build_tables<C>(t1, a.pl);
   cp_async_wait_all();
   __syncthreads();
+  // rounds of the steps running n1 / f1: the thread owns (li, n3, n2)
+  const int li = tid & (TC - 1), d1 = (tid >> LT) & 7;
+  const int e2 = (tid >> (LT + 3)) & 7, k1 = tid >> (LT + 6);
+  // rounds of the other steps: the thread owns (li, d1, f1) with d1 = n3 or f2
+  const int f1o = (tid >> (LT + 3)) & (R1 - 1), k2 = tid >> (LT + 3 + LR);
   // F1: DFT-R1 over n1 (n1 < R1/2 nonzero) -> f1, twiddle wL^((8 n2 + n3) f1); position (f1, n2, n3)
-  for (int t = threadIdx.x; t < N1; t += blockDim.x) {
-    const int li = t & (TC - 1), n3 = (t >> LT) & 7, n2 = (t >> (LT + 3)) & 7, k = t >> (LT + 6);
-    float2 v[R1];
+  {
+    const int n3 = d1, n2 = e2, m = 8 * n2 + n3;
+    float2 w[R1];
 #pragma unroll
-    for (int n1 = 0; n1 < H; ++n1) v[n1] = sm[C::at(k, H + n1, n2, n3, li)];
+    for (int f1 = 1; f1 < R1; ++f1) w[f1] = t1[f1 * 64 + m];
+    const int p0 = C::at(k1, 0, n2, n3, li);
+    rounds<N1>([&](int i) {
+      const int p = p0 + i * DK1;
+      float2 v[R1];
 #pragma unroll
-    for (int n1 = H; n1 < R1; ++n1) v[n1] = make_float2(0.f, 0.f);
-    RDft<R1, -1>::run(v);
-    const int m = 8 * n2 + n3;
+      for (int n1 = 0; n1 < H; ++n1) v[n1] = sm[p + (H + n1) * SA];
 #pragma unroll
-    for (int f1 = 0; f1 < R1; ++f1) sm[C::at(k, f1, n2, n3, li)] = f1 == 0 ? v[0] : cmul(v[f1], t1[f1 * 64 + m]);
+      for (int n1 = H; n1 < R1; ++n1) v[n1] = make_float2(0.f, 0.f);
+      RDft<R1, -1>::run(v);
+      sm[p] = v[0];
+#pragma unroll
+      for (int f1 = 1; f1 < R1; ++f1) sm[p + f1 * SA] = cmul(v[f1], w[f1]);
+    });
   }
   __syncthreads();
   // F2: DFT-8 over n2 -> f2, twiddle w64^(n3 f2); position (f1, f2, n3)
-  for (int t = threadIdx.x; t < N2; t += blockDim.x) {
-    const int li = t & (TC - 1), n3 = (t >> LT) & 7, f1 = (t >> (LT + 3)) & (R1 - 1), k = t >> (LT + 3 + LR);
-    float2 v[8];
+  {
+    const int n3 = d1;
+    float2 w[8];
 #pragma unroll
-    for (int n2 = 0; n2 < 8; ++n2) v[n2] = sm[C::at(k, f1, n2, n3, li)];
-    RDft<8, -1>::run(v);
+    for (int f2 = 1; f2 < 8; ++f2) w[f2] = t2[f2 * 8 + n3];
+    const int p0 = C::at(k2, f1o, 0, n3, li);
+    rounds<N2>([&](int i) {
+      const int p = p0 + i * DK2;
+      float2 v[8];
 #pragma unroll
-    for (int f2 = 0; f2 < 8; ++f2) sm[C::at(k, f1, f2, n3, li)] = f2 == 0 ? v[0] : cmul(v[f2], t2[f2 * 8 + n3]);
+      for (int n2 = 0; n2 < 8; ++n2) v[n2] = sm[p + n2 * SB];
+      RDft<8, -1>::run(v);
+      sm[p] = v[0];
+#pragma unroll
+      for (int f2 = 1; f2 < 8; ++f2) sm[p + f2 * SB] = cmul(v[f2], w[f2]);
+    });
   }
   __syncthreads();
   // F3: DFT-8 over n3 -> f3; X[f1 + R1 f2 + 8 R1 f3] at position (f1, f2, f3)
-  for (int t = threadIdx.x; t < N2; t += blockDim.x) {
-    const int li = t & (TC - 1), f2 = (t >> LT) & 7, f1 = (t >> (LT + 3)) & (R1 - 1), k = t >> (LT + 3 + LR);
-    float2 v[8];
+  {
+    const int f2 = d1;
+    const int p0 = C::at(k2, f1o, f2, 0, li);
+    rounds<N2>([&](int i) {
+      const int p = p0 + i * DK2;
+      float2 v[8];
 #pragma unroll
-    for (int n3 = 0; n3 < 8; ++n3) v[n3] = sm[C::at(k, f1, f2, n3, li)];
-    RDft<8, -1>::run(v);
+      for (int n3 = 0; n3 < 8; ++n3) v[n3] = sm[p + n3 * TC];
+      RDft<8, -1>::run(v);
 #pragma unroll
-    for (int f3 = 0; f3 < 8; ++f3) sm[C::at(k, f1, f2, f3, li)] = v[f3];
+      for (int f3 = 0; f3 < 8; ++f3) sm[p + f3 * TC] = v[f3];
+    });
   }
   __syncthreads();
   lam8_voxels<C, KK>(a, sm, tile);
   __syncthreads();
   // I1: inverse DFT-8 over f3 -> n3, twiddle w64^(-n3 f2); position (f1, f2, n3)
-  for (int t = threadIdx.x; t < N2; t += blockDim.x) {
-    const int li = t & (TC - 1), f2 = (t >> LT) & 7, f1 = (t >> (LT + 3)) & (R1 - 1), k = t >> (LT + 3 + LR);
-    float2 v[8];
+  {
+    const int f2 = d1;
+    float2 w[8];
 #pragma unroll
-    for (int f3 = 0; f3 < 8; ++f3) v[f3] = sm[C::at(k, f1, f2, f3, li)];
-    RDft<8, +1>::run(v);
+    for (int n3 = 1; n3 < 8; ++n3) w[n3] = t3[n3 * 8 + f2];
+    const int p0 = C::at(k2, f1o, f2, 0, li);
+    rounds<N2>([&](int i) {
+      const int p = p0 + i * DK2;
+      float2 v[8];
 #pragma unroll
-    for (int n3 = 0; n3 < 8; ++n3) sm[C::at(k, f1, f2, n3, li)] = n3 == 0 ? v[0] : cmul(v[n3], t3[n3 * 8 + f2]);
+      for (int f3 = 0; f3 < 8; ++f3) v[f3] = sm[p + f3 * TC];
+      RDft<8, +1>::run(v);
+      sm[p] = v[0];
+#pragma unroll
+      for (int n3 = 1; n3 < 8; ++n3) sm[p + n3 * TC] = cmul(v[n3], w[n3]);
+    });
   }
   __syncthreads();
   // I2: inverse DFT-8 over f2 -> n2, twiddle wL^(-(8 n2 + n3) f1); position (f1, n2, n3)
-  for (int t = threadIdx.x; t < N2; t += blockDim.x) {
-    const int li = t & (TC - 1), n3 = (t >> LT) & 7, f1 = (t >> (LT + 3)) & (R1 - 1), k = t >> (LT + 3 + LR);
-    float2 v[8];
+  // (row f1 = 0 of the table is exactly 1, so that row's products are exact)
+  {
+    const int n3 = d1;
+    float2 w[8];
 #pragma unroll
-    for (int f2 = 0; f2 < 8; ++f2) v[f2] = sm[C::at(k, f1, f2, n3, li)];
-    RDft<8, +1>::run(v);
+    for (int n2 = 0; n2 < 8; ++n2) w[n2] = cj(t1[f1o * 64 + 8 * n2 + n3]);
+    const int p0 = C::at(k2, f1o, 0, n3, li);
+    rounds<N2>([&](int i) {
+      const int p = p0 + i * DK2;
+      float2 v[8];
 #pragma unroll
-    for (int n2 = 0; n2 < 8; ++n2)
-      sm[C::at(k, f1, n2, n3, li)] = f1 == 0 ? v[n2] : cmul(v[n2], cj(t1[f1 * 64 + 8 * n2 + n3]));
+      for (int f2 = 0; f2 < 8; ++f2) v[f2] = sm[p + f2 * SB];
+      RDft<8, +1>::run(v);
+#pragma unroll
+      for (int n2 = 0; n2 < 8; ++n2) sm[p + n2 * SB] = cmul(v[n2], w[n2]);
+    });
   }
   __syncthreads();
   // I3: inverse DFT-R1 over f1 -> n1, the kept half n1 < R1/2 written back
-  for (int t = threadIdx.x; t < N1; t += blockDim.x) {
-    const int li = t & (TC - 1), n3 = (t >> LT) & 7, n2 = (t >> (LT + 3)) & 7, k = t >> (LT + 6);
-    float2 v[R1];
+  {
+    const int n3 = d1, n2 = e2;
+    const int p0 = C::at(k1, 0, n2, n3, li);
+    const int64_t g64 = 64 * a.inner;
+    float2* g0 = base + k1 * plane + (int64_t)(8 * n2 + n3) * a.inner + li;
+    rounds<N1>([&](int i) {
+      const int p = p0 + i * DK1;
+      float2 v[R1];
 #pragma unroll
-    for (int f1 = 0; f1 < R1; ++f1) v[f1] = sm[C::at(k, f1, n2, n3, li)];
-    RDft<R1, +1>::run(v);
+      for (int f1 = 0; f1 < R1; ++f1) v[f1] = sm[p + f1 * SA];
+      RDft<R1, +1>::run(v);
+      float2* g = g0 + (int64_t)i * (kL8Threads / C::NT1) * plane;
 #pragma unroll
-    for (int n1 = 0; n1 < H; ++n1) base[k * plane + (int64_t)(64 * n1 + 8 * n2 + n3) * a.inner + li] = v[n1];
+      for (int n1 = 0; n1 < H; ++n1) g[n1 * g64] = v[n1];
+    });
   }
 }
 
@@ -261,7 +323,9 @@ size_t smem8(int L, int TC, int K) {
 
 bool lambda8_supported(const LamPassArgs& a) {
   const bool shape = (a.pl.L == 512 || a.pl.L == 256) && (a.TC == 4 || a.TC == 8);
+  // the voxel step's rounds take two Λ chunks of 256 entries (FC * TC = 256) each
   return shape && a.nin == a.pl.L / 2 && a.nout == a.pl.L / 2 && !lam_is_diag(a.lam_mode) && a.K >= 1 &&
+         a.FC * a.TC == 256 && a.NCH * a.FC == a.pl.L &&
          a.K <= kL8MaxK && smem8(a.pl.L, a.TC, a.K) <= kL8MaxSmem && a.inner % a.TC == 0 &&
          (reinterpret_cast<uintptr_t>(a.stack) & 15) == 0;  // 16-byte staging copies
 }
