@@ -55,6 +55,39 @@ __device__ __forceinline__ void cp_async16(float2* dst, const float2* src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// DFT-R (R = 4 or 8, sign S) of v[0..R/2-1] followed by R/2 zeros, without the additions of
+// the zeros (x + 0 is not folded away by the compiler, as -0 + 0 = +0):
+//   R = 4: X[q] = v0 + (S i)^q v1;  R = 8: the even / odd halves of Dft<8> from two such DFT-4s.
+template <int R, int S>
+__device__ __forceinline__ void dft_half_in(float2* v) {
+  const float sg = (float)S;
+  if constexpr (R == 4) {
+    const float2 a = v[0], b = v[1], ib = cmul_i(b, sg);
+    v[0] = cadd(a, b);
+    v[1] = cadd(a, ib);
+    v[2] = csub(a, b);
+    v[3] = csub(a, ib);
+  } else {
+    static_assert(R == 8, "R = 4 or 8");
+    const float h = 0.70710678118654752440f;
+    float2 e[4] = {v[0], v[2]}, o[4] = {v[1], v[3]};
+    dft_half_in<4, S>(e);
+    dft_half_in<4, S>(o);
+    // w8^1 = h(1 + S i), w8^2 = S i, w8^3 = h(-1 + S i)
+    const float2 o1 = make_float2(h * (o[1].x - sg * o[1].y), h * (o[1].y + sg * o[1].x));
+    const float2 o2 = cmul_i(o[2], sg);
+    const float2 o3 = make_float2(h * (-o[3].x - sg * o[3].y), h * (-o[3].y + sg * o[3].x));
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], o1);
+    v[5] = csub(e[1], o1);
+    v[2] = cadd(e[2], o2);
+    v[6] = csub(e[2], o2);
+    v[3] = cadd(e[3], o3);
+    v[7] = csub(e[3], o3);
+  }
+}
+
 // Twiddle tables in the order the steps' lanes read them (a warp's lanes vary n3 or f2 with
 // the loop digit fixed, so each table read is consecutive entries, bank-conflict free; a
 // table indexed (m * f) mod L would put the lanes of an even f on the same banks):
@@ -186,9 +219,7 @@ __global__ void __launch_bounds__(kL8Threads, 2) k8_lambda(LamPassArgs a) {
       float2 v[R1];
 #pragma unroll
       for (int n1 = 0; n1 < H; ++n1) v[n1] = sm[p + (H + n1) * SA];
-#pragma unroll
-      for (int n1 = H; n1 < R1; ++n1) v[n1] = make_float2(0.f, 0.f);
-      RDft<R1, -1>::run(v);
+      dft_half_in<R1, -1>(v);
       sm[p] = v[0];
 #pragma unroll
       for (int f1 = 1; f1 < R1; ++f1) sm[p + f1 * SA] = cmul(v[f1], w[f1]);
