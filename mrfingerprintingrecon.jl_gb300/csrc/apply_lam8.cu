@@ -1,134 +1,20 @@
-// Λ pass of the float32 operator as three DFT steps each way for the two line lengths the
-// operators mostly use, L = R1 x 8 x 8: R1 = 8 (512-point lines, the 256^2 images' columns)
-// and R1 = 4 (256-point lines, the 128^3 volumes'):
-//   n = 64 n1 + 8 n2 + n3,  f = f1 + R1 f2 + 8 R1 f3,
-//   X[f] = sum_n3 w8^(n3 f3) w64^(n3 f2) sum_n2 w8^(n2 f2) [wL^((8 n2 + n3) f1) sum_n1 wR1^(n1 f1) x[n]]
-// with the input pruned to n1 < R1 / 2 (the zero-padded half) and the inverse's output to
-// n1 < R1 / 2 (the kept half).  Every task holds at most eight values (one DFT-8), so the
-// kernel fits in 64 registers and runs 512-thread CTAs two per SM: 32 warps per SM against 16
-// for the two-step kernels (apply_lam.cu), which are bound by latency, not by arithmetic.
-// The price is one more shared-memory exchange each way.
+// Λ pass of the float32 operator for 256- and 512-point lines (the 128^3 volumes' and the
+// 256^2 images' last axes) as the three-step transforms of three_step.cuh: stage the tile's
+// zero-padded columns, three forward steps, the K x K kernel at every cell of the line, three
+// inverse steps with the kept half written back.  Every task holds at most eight values, so
+// the kernel runs 512-thread CTAs two per SM: 32 warps per SM against 16 for the two-step
+// kernels (apply_lam.cu), which are bound by latency, not by arithmetic; the price is one
+// more shared-memory exchange each way.
 // src/NFFTNormalOp.jl:227-267 / ext/MRISubspaceReconCUDAExt/NFFTNormalOp.jl:193-218.
-//
-// Shared layout of plane k, column li (TC = 4 or 8 columns per tile): position (a, b, c) of
-// the three digits at k * SP + a * SA + b * SB + c * TC + li (float2 units).  Every step's warp
-// varies li and one of a, b, c (the rest fixed); SA and SB are TC (mod 16), so the 16 lanes of
-// a half-warp (16 / TC values of the running digit) touch 16 distinct 8-byte bank pairs for
-// any of the three, and a task's running digit is a compile-time loop index, so its addresses
-// are one register plus immediate offsets.  A task reads and writes the same positions (one
-// digit running), so every step works in place.
-#include "fft4.cuh"
-#include "passes.cuh"
+#include "three_step.cuh"
 
 namespace mrsr {
 
 namespace {
 
-constexpr int kL8Threads = 512;
+using namespace l8;
+
 constexpr int kL8MaxK = 6;
-constexpr size_t kL8MaxSmem = 227 * 1024;
-
-template <int R1_, int TC_>
-struct L8 {
-  static constexpr int R1 = R1_, TC = TC_, L = 64 * R1;
-  static constexpr int LT = TC == 4 ? 2 : 3;  // log2 TC
-  static constexpr int LR = R1 == 4 ? 2 : 3;  // log2 R1
-  static constexpr int SB = 8 * TC + TC, SA = 8 * SB + TC, SP = R1 * SA;  // digit b, digit a, plane
-  static constexpr int T1 = R1 * 64, T2 = 64, T3 = 64, TW = T1 + T2 + T3;  // twiddle tables
-  static constexpr int NT1 = TC * 64;      // tasks per plane of the steps running n1 / f1
-  static constexpr int NT2 = TC * 8 * R1;  // tasks per plane of the other steps
-  static_assert((TC == 4 || TC == 8) && (R1 == 4 || R1 == 8), "tile of 4 or 8 columns, L = 256 or 512");
-  static_assert(SB % 16 == TC && SA % 16 == TC, "a half-warp on 16 distinct bank pairs");
-  static constexpr size_t smem(int K) { return sizeof(float2) * ((size_t)TW + (size_t)K * SP); }
-  static __device__ __forceinline__ int at(int k, int a, int b, int c, int li) { return k * SP + a * SA + b * SB + c * TC + li; }
-};
-
-__device__ __forceinline__ float2 cj(float2 w) { return make_float2(w.x, -w.y); }
-
-// 16-byte global -> shared copy that bypasses L1 (cp.async.cg); both addresses 16-byte aligned.
-__device__ __forceinline__ void cp_async16(float2* dst, const float2* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
-}
-// Closes the thread's copies into one group / waits for it (the caller's barrier then makes
-// every thread's copies visible to the CTA).
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-// DFT-R (R = 4 or 8, sign S) of v[0..R/2-1] followed by R/2 zeros, without the additions of
-// the zeros (x + 0 is not folded away by the compiler, as -0 + 0 = +0):
-//   R = 4: X[q] = v0 + (S i)^q v1;  R = 8: the even / odd halves of Dft<8> from two such DFT-4s.
-template <int R, int S>
-__device__ __forceinline__ void dft_half_in(float2* v) {
-  const float sg = (float)S;
-  if constexpr (R == 4) {
-    const float2 a = v[0], b = v[1], ib = cmul_i(b, sg);
-    v[0] = cadd(a, b);
-    v[1] = cadd(a, ib);
-    v[2] = csub(a, b);
-    v[3] = csub(a, ib);
-  } else {
-    static_assert(R == 8, "R = 4 or 8");
-    const float h = 0.70710678118654752440f;
-    float2 e[4] = {v[0], v[2]}, o[4] = {v[1], v[3]};
-    dft_half_in<4, S>(e);
-    dft_half_in<4, S>(o);
-    // w8^1 = h(1 + S i), w8^2 = S i, w8^3 = h(-1 + S i)
-    const float2 o1 = make_float2(h * (o[1].x - sg * o[1].y), h * (o[1].y + sg * o[1].x));
-    const float2 o2 = cmul_i(o[2], sg);
-    const float2 o3 = make_float2(h * (-o[3].x - sg * o[3].y), h * (-o[3].y + sg * o[3].x));
-    v[0] = cadd(e[0], o[0]);
-    v[4] = csub(e[0], o[0]);
-    v[1] = cadd(e[1], o1);
-    v[5] = csub(e[1], o1);
-    v[2] = cadd(e[2], o2);
-    v[6] = csub(e[2], o2);
-    v[3] = cadd(e[3], o3);
-    v[7] = csub(e[3], o3);
-  }
-}
-
-// Twiddle tables in the order the steps' lanes read them (a warp's lanes vary n3 or f2 with
-// the loop digit fixed, so each table read is consecutive entries, bank-conflict free; a
-// table indexed (m * f) mod L would put the lanes of an even f on the same banks):
-//   t1[f1 * 64 + m] = wL^(m f1), m = 8 n2 + n3     (F1, I2 conjugated)
-//   t2[f2 * 8 + n3] = w64^(n3 f2)                  (F2)
-//   t3[n3 * 8 + f2] = w64^(-n3 f2)                 (I1)
-template <class C>
-__device__ __forceinline__ void build_tables(float2* t, const FftPlan& pl) {
-  const float2* w = pl.tw;  // wL^p
-  for (int i = threadIdx.x; i < C::TW; i += blockDim.x) {
-    int p;
-    bool conj = false;
-    if (i < C::T1) {
-      p = (i & 63) * (i >> 6);
-    } else if (i < C::T1 + C::T2) {
-      const int j = i - C::T1;
-      p = C::R1 * (j & 7) * (j >> 3);
-    } else {
-      const int j = i - C::T1 - C::T2;
-      p = C::R1 * (j >> 3) * (j & 7);
-      conj = true;
-    }
-    const float2 v = w[p & (C::L - 1)];
-    t[i] = conj ? cj(v) : v;
-  }
-}
-
-// Every step runs a fixed set of tasks per thread: task t = tid + 512 i, and since the tasks
-// of one plane (or, for the voxel step, the frequencies of two Λ chunks) number a divisor of
-// 512, the digits a thread owns are the same in every round i and only the plane (or f3)
-// moves, by a compile-time step.  So each thread forms its addresses and loads its twiddles
-// once per step, and the rounds are unrolled with immediate offsets.
-template <int N, class F>
-__device__ __forceinline__ void rounds(F&& body) {
-  constexpr int IT = (N + kL8Threads - 1) / kL8Threads;
-#pragma unroll
-  for (int i = 0; i < IT; ++i) {
-    if (N % kL8Threads != 0 && (int)threadIdx.x + i * kL8Threads >= N) break;
-    body(i);
-  }
-}
 
 template <class C, int KK>
 __device__ __forceinline__ void lam8_voxels(const LamPassArgs& a, float2* sm, int64_t tile) {
@@ -173,10 +59,7 @@ __device__ __forceinline__ void lam8_voxels(const LamPassArgs& a, float2* sm, in
 
 template <class C, int KK>
 __global__ void __launch_bounds__(kL8Threads, 2) k8_lambda(LamPassArgs a) {
-  constexpr int R1 = C::R1, TC = C::TC, LT = C::LT, LR = C::LR, H = R1 / 2;
-  constexpr int N1 = KK * C::NT1, N2 = KK * C::NT2;
-  constexpr int DK1 = kL8Threads / C::NT1 * C::SP, DK2 = kL8Threads / C::NT2 * C::SP;  // plane step per round
-  constexpr int SA = C::SA, SB = C::SB;
+  constexpr int TC = C::TC, LT = C::LT, H = C::R1 / 2;
   extern __shared__ float2 smem[];
   float2* t1 = smem;                 // twiddle tables
   const float2* t2 = smem + C::T1;
@@ -202,121 +85,27 @@ __global__ void __launch_bounds__(kL8Threads, 2) k8_lambda(LamPassArgs a) {
   build_tables<C>(t1, a.pl);
   cp_async_wait_all();
   __syncthreads();
-  // rounds of the steps running n1 / f1: the thread owns (li, n3, n2)
-  const int li = tid & (TC - 1), d1 = (tid >> LT) & 7;
-  const int e2 = (tid >> (LT + 3)) & 7, k1 = tid >> (LT + 6);
-  // rounds of the other steps: the thread owns (li, d1, f1) with d1 = n3 or f2
-  const int f1o = (tid >> (LT + 3)) & (R1 - 1), k2 = tid >> (LT + 3 + LR);
-  // F1: DFT-R1 over n1 (n1 < R1/2 nonzero) -> f1, twiddle wL^((8 n2 + n3) f1); position (f1, n2, n3)
-  {
-    const int n3 = d1, n2 = e2, m = 8 * n2 + n3;
-    float2 w[R1];
-#pragma unroll
-    for (int f1 = 1; f1 < R1; ++f1) w[f1] = t1[f1 * 64 + m];
-    const int p0 = C::at(k1, 0, n2, n3, li);
-    rounds<N1>([&](int i) {
-      const int p = p0 + i * DK1;
-      float2 v[R1];
-#pragma unroll
-      for (int n1 = 0; n1 < H; ++n1) v[n1] = sm[p + (H + n1) * SA];
-      dft_half_in<R1, -1>(v);
-      sm[p] = v[0];
-#pragma unroll
-      for (int f1 = 1; f1 < R1; ++f1) sm[p + f1 * SA] = cmul(v[f1], w[f1]);
-    });
-  }
+  const Own<C> o;
+  step_f1<C, KK>(sm, t1, o);
   __syncthreads();
-  // F2: DFT-8 over n2 -> f2, twiddle w64^(n3 f2); position (f1, f2, n3)
-  {
-    const int n3 = d1;
-    float2 w[8];
-#pragma unroll
-    for (int f2 = 1; f2 < 8; ++f2) w[f2] = t2[f2 * 8 + n3];
-    const int p0 = C::at(k2, f1o, 0, n3, li);
-    rounds<N2>([&](int i) {
-      const int p = p0 + i * DK2;
-      float2 v[8];
-#pragma unroll
-      for (int n2 = 0; n2 < 8; ++n2) v[n2] = sm[p + n2 * SB];
-      RDft<8, -1>::run(v);
-      sm[p] = v[0];
-#pragma unroll
-      for (int f2 = 1; f2 < 8; ++f2) sm[p + f2 * SB] = cmul(v[f2], w[f2]);
-    });
-  }
+  step_f2<C, KK>(sm, t2, o);
   __syncthreads();
-  // F3: DFT-8 over n3 -> f3; X[f1 + R1 f2 + 8 R1 f3] at position (f1, f2, f3)
-  {
-    const int f2 = d1;
-    const int p0 = C::at(k2, f1o, f2, 0, li);
-    rounds<N2>([&](int i) {
-      const int p = p0 + i * DK2;
-      float2 v[8];
-#pragma unroll
-      for (int n3 = 0; n3 < 8; ++n3) v[n3] = sm[p + n3 * TC];
-      RDft<8, -1>::run(v);
-#pragma unroll
-      for (int f3 = 0; f3 < 8; ++f3) sm[p + f3 * TC] = v[f3];
-    });
-  }
+  step_f3<C, KK>(sm, o);
   __syncthreads();
   lam8_voxels<C, KK>(a, sm, tile);
   __syncthreads();
-  // I1: inverse DFT-8 over f3 -> n3, twiddle w64^(-n3 f2); position (f1, f2, n3)
-  {
-    const int f2 = d1;
-    float2 w[8];
-#pragma unroll
-    for (int n3 = 1; n3 < 8; ++n3) w[n3] = t3[n3 * 8 + f2];
-    const int p0 = C::at(k2, f1o, f2, 0, li);
-    rounds<N2>([&](int i) {
-      const int p = p0 + i * DK2;
-      float2 v[8];
-#pragma unroll
-      for (int f3 = 0; f3 < 8; ++f3) v[f3] = sm[p + f3 * TC];
-      RDft<8, +1>::run(v);
-      sm[p] = v[0];
-#pragma unroll
-      for (int n3 = 1; n3 < 8; ++n3) sm[p + n3 * TC] = cmul(v[n3], w[n3]);
-    });
-  }
+  step_i1<C, KK>(sm, t3, o);
   __syncthreads();
-  // I2: inverse DFT-8 over f2 -> n2, twiddle wL^(-(8 n2 + n3) f1); position (f1, n2, n3)
-  // (row f1 = 0 of the table is exactly 1, so that row's products are exact)
-  {
-    const int n3 = d1;
-    float2 w[8];
-#pragma unroll
-    for (int n2 = 0; n2 < 8; ++n2) w[n2] = cj(t1[f1o * 64 + 8 * n2 + n3]);
-    const int p0 = C::at(k2, f1o, 0, n3, li);
-    rounds<N2>([&](int i) {
-      const int p = p0 + i * DK2;
-      float2 v[8];
-#pragma unroll
-      for (int f2 = 0; f2 < 8; ++f2) v[f2] = sm[p + f2 * SB];
-      RDft<8, +1>::run(v);
-#pragma unroll
-      for (int n2 = 0; n2 < 8; ++n2) sm[p + n2 * SB] = cmul(v[n2], w[n2]);
-    });
-  }
+  step_i2<C, KK>(sm, t1, o);
   __syncthreads();
-  // I3: inverse DFT-R1 over f1 -> n1, the kept half n1 < R1/2 written back
-  {
-    const int n3 = d1, n2 = e2;
-    const int p0 = C::at(k1, 0, n2, n3, li);
-    const int64_t g64 = 64 * a.inner;
-    float2* g0 = base + k1 * plane + (int64_t)(8 * n2 + n3) * a.inner + li;
-    rounds<N1>([&](int i) {
-      const int p = p0 + i * DK1;
-      float2 v[R1];
+  // I3: the kept half n1 < R1/2 written back to the columns
+  const int64_t g64 = 64 * a.inner;
+  float2* g0 = base + o.k1 * plane + (int64_t)(8 * o.e2 + o.d1) * a.inner + o.li;
+  step_i3<C, KK>(sm, o, [&](int i, const float2* v) {
+    float2* g = g0 + (int64_t)i * (kL8Threads / C::NT1) * plane;
 #pragma unroll
-      for (int f1 = 0; f1 < R1; ++f1) v[f1] = sm[p + f1 * SA];
-      RDft<R1, +1>::run(v);
-      float2* g = g0 + (int64_t)i * (kL8Threads / C::NT1) * plane;
-#pragma unroll
-      for (int n1 = 0; n1 < H; ++n1) g[n1 * g64] = v[n1];
-    });
-  }
+    for (int n1 = 0; n1 < H; ++n1) g[n1 * g64] = v[n1];
+  });
 }
 
 template <class C, int KK>

@@ -585,6 +585,8 @@ static int apply_impl(mrsr_normalop* op, const float2* x, float2* y, float2 alph
       dim3 grid((unsigned)cdiv(nrows, t.rpc), K);
       if (tc_rows)
         MRSR_TRY(tc_rows_inv(a, op->tc_consts.p, op->errflag.as<int>(), st));
+      else if (rows8_inv_supported(a))
+        MRSR_TRY(fast_rows8_inv(a, st));
       else if (fast_length(L1))
         MRSR_TRY(fast_rows_inv(a, nrows, st));
       else

@@ -166,6 +166,10 @@ int fast_lambda(const LamPassArgs& a, int ncg, int planes_total, int* errword, c
 // three-step Λ pass (apply_lam8.cu): 256- or 512-point lines pruned to half, 4- or 8-column tiles, K <= 6
 bool lambda8_supported(const LamPassArgs& a);
 int fast_lambda8(const LamPassArgs& a, int ncg, cudaStream_t st);
+// three-step inverse row pass (apply_rows8.cu): 256- or 512-point rows of the zero-padded
+// half, <= 20 coils per group
+bool rows8_inv_supported(const RowsInvArgs& a);
+int fast_rows8_inv(const RowsInvArgs& a, cudaStream_t st);
 int fast_mid(const MidArgs& a, int nplanes, cudaStream_t st);
 int fast_rows_inv(const RowsInvArgs& a, int64_t nrows, cudaStream_t st);
 

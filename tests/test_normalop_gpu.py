@@ -55,6 +55,10 @@ def _problem(seed, img, K, Nc, density=0.8, complex_lam=True):
     ((64, 256), 2, 2, False),    # 512 points with 8-column tiles (K = 2)
     ((96, 128), 6, 2, False),    # K = 6, the largest the three-step kernel takes
     ((16, 16, 128), 3, 2, True), # 3D with a 256-point last axis
+    ((256, 24), 3, 20, True),    # three-step row passes at 512 points, 20 coils (five groups of 4)
+    ((128, 10), 4, 13, False),   # 256-point rows, 13 coils (a partial group), 10 rows (a partial row block)
+    ((128, 64), 2, 0, True),     # 256-point rows without coil maps
+    ((128, 12, 8), 2, 3, True),  # 3D with 256-point rows
 ])
 def test_nfft_apply_matches_oracle(mr, cuda, img, K, Nc, cplx):
     lam, cells, cm, x = _problem(1, img, K, Nc, complex_lam=cplx)
