@@ -34,6 +34,24 @@ __global__ void __launch_bounds__(kL8Threads, 2) k8_rows_inv(RowsInvArgs a) {
   const int64_t r = blockIdx.x;
   const int k = blockIdx.y;
   const int n1len = L / 2;
+  // ask L2 for the CTA's lines and coil map rows first (128-byte lines), so that the loads of
+  // the first and the last step find them there
+  {
+    constexpr int LPL = L * 8 / 128;        // 128-byte lines per stack line
+    constexpr int LPC = (L / 2) * 8 / 128;  // per coil map row
+    const int nst = a.ncg * LPL, ncm = a.cmaps ? a.ncg * LPC : 0;
+    for (int j = tid; j < nst + ncm; j += kL8Threads) {
+      const float2* q;
+      if (j < nst) {
+        const int cl = j / LPL;
+        q = a.stack + (((int64_t)cl * a.K + k) * a.nrows + r) * L + (j - cl * LPL) * 16;
+      } else {
+        const int jc = j - nst, cl = jc / LPC;
+        q = a.cmaps + (int64_t)n1len * (r + a.nrows * (a.c0 + cl)) + (jc - cl * LPC) * 16;
+      }
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
+    }
+  }
   build_tables<C>(t1, a.pl);
   __syncthreads();
   const Own<C> o;
