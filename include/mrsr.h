@@ -140,6 +140,16 @@ int mrsr_fft_normalop_from_lambda(int ndims, const int64_t* img_shape, int K, co
 int mrsr_normalop_apply(mrsr_normalop* op, const float* x, float* y, float alpha_re, float alpha_im,
                         float beta_re, float beta_im, mrsr_stream_t stream);
 
+/* mul!(y, A, x, α, β) on host arrays: the reference's CPU method (src/NFFTNormalOp.jl:227-267,
+ * src/FFTNormalOp.jl:111-149) for callers whose x and y live in host memory.  Replaces
+ * copyto!(x_d, x); mul!(y_d, A, x_d, α, β); copyto!(y, y_d): x is copied into the operator's
+ * own device buffer (made on first use); with one coil group, and y page-locked (addressable
+ * by the device), the inverse row pass stores y straight into the host array over the
+ * CPU-GPU link, so no copy back follows the apply; otherwise y returns by a copy.  Enqueued on
+ * `stream`; y is final when `stream` has synchronised.  x and y must not alias. */
+int mrsr_normalop_apply_host(mrsr_normalop* op, const float* x, float* y, float alpha_re, float alpha_im,
+                             float beta_re, float beta_im, mrsr_stream_t stream);
+
 /* Sizes of an operator (host array of 12 int64):
  * [kind, ndims, n1, n2, n3, K, ncoils, nk, lambda_is_complex, precision, P, launches_per_apply] */
 int mrsr_normalop_info(const mrsr_normalop* op, int64_t* info);

@@ -29,6 +29,7 @@ SIGNATURES = {
     "mrsr_fft_normalop_create_from_mask": [i32, i64p, i64, p, p, i32, i32, p, i32, i32, p, C.POINTER(p)],
     "mrsr_fft_normalop_from_lambda": [i32, i64p, i32, p, p, i32, i32, p, C.POINTER(p)],
     "mrsr_normalop_apply": [p, p, p, f32, f32, f32, f32, p],
+    "mrsr_normalop_apply_host": [p, p, p, f32, f32, f32, f32, p],
     "mrsr_normalop_info": [p, i64p],
     "mrsr_normalop_get_kmask": [p, p, p],
     "mrsr_normalop_get_lambda": [p, p, p],

@@ -866,6 +866,43 @@ extern "C" int mrsr_normalop_apply(mrsr_normalop* op, const float* x, float* y, 
                     make_float2(alpha_re, alpha_im), make_float2(beta_re, beta_im), as_stream(stream), Recorder{});
 }
 
+// A host pointer the device can address directly (page-locked or mapped memory, or any host
+// memory on a system with address translation from the GPU), else null.
+static void* device_view(void* host) {
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, host, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return d;
+}
+
+extern "C" int mrsr_normalop_apply_host(mrsr_normalop* op, const float* x, float* y, float alpha_re, float alpha_im,
+                                        float beta_re, float beta_im, mrsr_stream_t stream) {
+  MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
+  MRSR_REQUIRE(op && x && y, MRSR_ERR_ARG, "NULL argument to mrsr_normalop_apply_host");
+  MRSR_REQUIRE((const void*)x != (const void*)y, MRSR_ERR_ARG, "x and y must not alias");
+  const cudaStream_t st = as_stream(stream);
+  OpUse use{op, st};
+  const OpGeom& g = op->geo;
+  const size_t bytes = sizeof(float2) * (size_t)(g.n[0] * g.n[1] * g.n[2] * g.K);
+  HostIo& h = op->hio;
+  if (h.x.bytes < bytes) MRSR_TRY(h.x.alloc(bytes));
+  float2* xd = h.x.as<float2>();
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(xd, x, bytes, cudaMemcpyHostToDevice, st));
+  const float2 alpha = make_float2(alpha_re, alpha_im), beta = make_float2(beta_re, beta_im);
+  // With one coil group the inverse row pass writes every element of y once: it stores
+  // straight into the host array over the CPU-GPU link, so no copy back follows the apply.
+  float2* yv = cdiv(g.ncoils, op->Cg) == 1 ? static_cast<float2*>(device_view(y)) : nullptr;
+  if (yv) return apply_impl(op, xd, yv, alpha, beta, st, Recorder{});
+  if (h.y.bytes < bytes) MRSR_TRY(h.y.alloc(bytes));
+  float2* yd = h.y.as<float2>();
+  if (beta_re != 0.f || beta_im != 0.f) MRSR_CHECK_CUDA(cudaMemcpyAsync(yd, y, bytes, cudaMemcpyHostToDevice, st));
+  MRSR_TRY(apply_impl(op, xd, yd, alpha, beta, st, Recorder{}));
+  MRSR_CHECK_CUDA(cudaMemcpyAsync(y, yd, bytes, cudaMemcpyDeviceToHost, st));
+  return MRSR_OK;
+}
+
 extern "C" int mrsr_normalop_info(const mrsr_normalop* op, int64_t* info) {
   MRSR_REQUIRE(op && info, MRSR_ERR_ARG, "NULL argument");
   const OpGeom& g = op->geo;

@@ -49,6 +49,13 @@ struct LamStore {
 
 }  // namespace mrsr
 
+namespace mrsr {
+// Device copies of x and y for host-buffer applies (mrsr_normalop_apply_host), made on first use.
+struct HostIo {
+  DevBuf x, y;
+};
+}  // namespace mrsr
+
 struct mrsr_normalop {
   mrsr_normalop() : mrsr_normalop(std::make_shared<mrsr::LamStore>()) {}
   explicit mrsr_normalop(std::shared_ptr<mrsr::LamStore> s)
@@ -88,6 +95,7 @@ struct mrsr_normalop {
   mrsr::DevBuf errflag;         // device int
   mrsr::FftPlanHost plan[3];
   mrsr::CgWork cg;              // CG vectors, allocated on first solve
+  mrsr::HostIo hio;             // host-buffer applies
   // recorded after every call that enqueues work on the operator; the
   // destructor frees the buffers only after it (stream-ordered, no device sync)
   cudaEvent_t last_use = nullptr;

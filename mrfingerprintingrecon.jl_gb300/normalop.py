@@ -97,6 +97,26 @@ class NormalOperator:
                                                   stream_handle(stream)))
         return res
 
+    def mul_host(self, res, x, alpha=1.0, beta=0.0, stream=None):
+        """``mul!(res, A, x, alpha, beta)`` on host arrays: res and x are complex64 CPU tensors
+        holding the column-major (img..., K) data (a flat vector, or a column-major view).  x is
+        copied to the device; with one coil group and res page-locked, the inverse row pass
+        stores res straight into host memory (``mrsr_normalop_apply_host``), else res returns by
+        a copy.  Enqueued on ``stream``; res is final once the stream has synchronised."""
+        n = self.shape[0]
+        for name, t in (("x", x), ("res", res)):
+            if not isinstance(t, torch.Tensor) or t.is_cuda or t.dtype != torch.complex64 or t.numel() != n:
+                raise ValueError(f"{name} must be a complex64 CPU tensor of {n} elements")
+            if not t.permute(*reversed(range(t.dim()))).is_contiguous():
+                raise ValueError(f"{name} must be dense (column-major (img..., K) data)")
+        if x.data_ptr() == res.data_ptr():
+            raise ValueError("x and res must not alias")
+        a = complex(alpha)
+        b = complex(beta)
+        _lib.check(_lib.load().mrsr_normalop_apply_host(self._h, ptr(x), ptr(res), a.real, a.imag, b.real, b.imag,
+                                                       stream_handle(stream)))
+        return res
+
     def __matmul__(self, x):
         xi = self._as_image(x)
         out = jl_empty(xi.shape, torch.complex64)
