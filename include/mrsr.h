@@ -143,7 +143,8 @@ int mrsr_normalop_apply(mrsr_normalop* op, const float* x, float* y, float alpha
 /* mul!(y, A, x, α, β) on host arrays: the reference's CPU method (src/NFFTNormalOp.jl:227-267,
  * src/FFTNormalOp.jl:111-149) for callers whose x and y live in host memory.  Replaces
  * copyto!(x_d, x); mul!(y_d, A, x_d, α, β); copyto!(y, y_d): x is copied into the operator's
- * own device buffer (made on first use); with one coil group, and y page-locked (addressable
+ * own device buffer (made on first use; by the SMs over the CPU-GPU link when x is page-locked,
+ * else by cudaMemcpyAsync); with one coil group, and y page-locked (addressable
  * by the device), the inverse row pass stores y straight into the host array over the
  * CPU-GPU link, so no copy back follows the apply; otherwise y returns by a copy.  Enqueued on
  * `stream`; y is final when `stream` has synchronised.  x and y must not alias. */

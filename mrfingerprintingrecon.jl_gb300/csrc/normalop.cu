@@ -866,6 +866,22 @@ extern "C" int mrsr_normalop_apply(mrsr_normalop* op, const float* x, float* y, 
                     make_float2(alpha_re, alpha_im), make_float2(beta_re, beta_im), as_stream(stream), Recorder{});
 }
 
+// Host -> device copy by the SMs: 16-byte loads over the CPU-GPU link from device-addressable
+// host memory, many in flight (n16 16-byte units; both addresses 16-byte aligned).
+__global__ void __launch_bounds__(256) k_copy_in(const float4* __restrict__ src, float4* __restrict__ dst, int64_t n16) {
+  constexpr int U = 4;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += U * step) {
+    float4 v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (i + u * step < n16) v[u] = src[i + u * step];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      if (i + u * step < n16) dst[i + u * step] = v[u];
+  }
+}
+
 // A host pointer the device can address directly (page-locked or mapped memory, or any host
 // memory on a system with address translation from the GPU), else null.
 static void* device_view(void* host) {
@@ -889,7 +905,18 @@ extern "C" int mrsr_normalop_apply_host(mrsr_normalop* op, const float* x, float
   HostIo& h = op->hio;
   if (h.x.bytes < bytes) MRSR_TRY(h.x.alloc(bytes));
   float2* xd = h.x.as<float2>();
-  MRSR_CHECK_CUDA(cudaMemcpyAsync(xd, x, bytes, cudaMemcpyHostToDevice, st));
+  const void* xv = device_view(const_cast<float*>(x));
+  if (xv && bytes % 16 == 0 && ((uintptr_t)xv & 15) == 0) {
+    const int64_t n16 = (int64_t)(bytes / 16);
+    int dev = 0, nsm = 0;
+    MRSR_CHECK_CUDA(cudaGetDevice(&dev));
+    MRSR_CHECK_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t blocks = std::min<int64_t>(cdiv(n16, 256), (int64_t)nsm * 8);
+    k_copy_in<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const float4*>(xv), reinterpret_cast<float4*>(xd), n16);
+    MRSR_LAUNCH_CHECK();
+  } else {
+    MRSR_CHECK_CUDA(cudaMemcpyAsync(xd, x, bytes, cudaMemcpyHostToDevice, st));
+  }
   const float2 alpha = make_float2(alpha_re, alpha_im), beta = make_float2(beta_re, beta_im);
   // With one coil group the inverse row pass writes every element of y once: it stores
   // straight into the host array over the CPU-GPU link, so no copy back follows the apply.
