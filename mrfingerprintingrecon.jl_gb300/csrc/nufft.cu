@@ -1392,9 +1392,20 @@ struct InterpArgs {
   int64_t M[3], mcells;
   int K, c, u_complex;
   const void* U;
-  const float2* g;       // [K][mcells] after the forward DFT
+  const float2* g;       // [mcells][K] after the forward DFT: a cell's K planes side by side
   float2* data;          // (ns_pf, nt, ncoils)
 };
+
+// [K][mcells] -> [mcells][K]: after the forward DFT the interpolation reads all K planes at
+// each tap, so the K values of a cell are put next to each other (one or two 32-byte sectors
+// per tap instead of K).
+__global__ void k_interleave(const float2* __restrict__ g, float2* __restrict__ gi, int K, int64_t mcells) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < mcells; l += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (k < K) gi[l * K + k] = g[(int64_t)k * mcells + l];
+  }
+}
 
 // 2D: one thread per kept sample, the w^2 taps of the K gridded planes summed in the thread
 // (no cross-lane reduction); the 32 samples of a warp are consecutive along the trajectory,
@@ -1429,15 +1440,15 @@ __global__ void __launch_bounds__(256) k_interp(InterpArgs a) {
 #pragma unroll
       for (int t2 = 0; t2 < kEsWidth; ++t2) {
         const float w23 = wy[t2] * w3;
-        const float2* row = a.g + base3 + (int64_t)iy[t2] * a.M[0];
+        const int64_t row = base3 + (int64_t)iy[t2] * a.M[0];
 #pragma unroll
         for (int t1 = 0; t1 < kEsWidth; ++t1) {
           const float w = w23 * wx[t1];
-          const float2* cell = row + ix[t1];
+          const float2* cell = a.g + (row + ix[t1]) * a.K;
 #pragma unroll
           for (int k = 0; k < 8; ++k)
             if (k < a.K) {
-              const float2 gv = __ldg(cell + (int64_t)k * a.mcells);
+              const float2 gv = __ldg(cell + k);
               z[k].x = fmaf(w, gv.x, z[k].x);
               z[k].y = fmaf(w, gv.y, z[k].y);
             }
@@ -1480,7 +1491,7 @@ __global__ void __launch_bounds__(256) k_interp3(InterpArgs a) {
 #pragma unroll
       for (int k = 0; k < 8; ++k)
         if (k < a.K) {
-          const float2 gv = __ldg(a.g + (int64_t)k * a.mcells + cell[j]);
+          const float2 gv = __ldg(a.g + (int64_t)cell[j] * a.K + k);
           z[k].x = fmaf(w[j], gv.x, z[k].x);
           z[k].y = fmaf(w[j], gv.y, z[k].y);
         }
@@ -1685,8 +1696,9 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
   MRSR_TRY(fM.init(ndims, M));
   const float* ipsi[3] = {nullptr, nullptr, nullptr};
   for (int i = 0; i < ndims; ++i) MRSR_TRY(es_inv_psi_table(M[i], -(N[i] / 2), N[i], &ipsi[i]));
-  DevBuf grid;
+  DevBuf grid, gridi;
   MRSR_TRY(grid.alloc(sizeof(float2) * K * mcells));
+  MRSR_TRY(gridi.alloc(sizeof(float2) * K * mcells));
   for (int c = 0; c < ncoils; ++c) {
     MRSR_CHECK_CUDA(cudaMemsetAsync(grid.p, 0, sizeof(float2) * K * mcells, st));
     FwdPlaceArgs pa;
@@ -1706,7 +1718,9 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
     k_fwd_place<<<grid1d(nimg * K), 256, 0, st>>>(pa);
     MRSR_LAUNCH_CHECK();
     MRSR_TRY(fM.run(grid.as<float2>(), K, -1, 1.0f, st));
-    InterpArgs ia{sl.set, {M[0], M[1], M[2]}, mcells, K, c, u_is_complex, U, grid.as<float2>(),
+    k_interleave<<<grid1d(mcells), 256, 0, st>>>(grid.as<float2>(), gridi.as<float2>(), K, mcells);
+    MRSR_LAUNCH_CHECK();
+    InterpArgs ia{sl.set, {M[0], M[1], M[2]}, mcells, K, c, u_is_complex, U, gridi.as<float2>(),
                   reinterpret_cast<float2*>(data_out)};
     if (ndims == 3) {
       MRSR_REQUIRE(mcells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "forward model grid of 2^32 cells or more");
