@@ -39,6 +39,7 @@ def _host(a):
     ((64, 256), 4, 4, "fp16-tc", True),    # tensor-core inverse row pass
     ((64, 64), 3, 2, "fp16", True),        # fp16-storage operator
     ((128, 64), 2, 3, "fp32", False),      # pageable y: copied back after the apply
+    ((256, 256), 3, 40, "fp32", True),     # two coil groups: y accumulated on the device, copied back
 ])
 def test_host_apply_equals_device_apply(mr, cuda, img, K, Nc, precision, pinned):
     A, rng = _op(mr, 11, img, K, Nc, precision)

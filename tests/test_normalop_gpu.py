@@ -61,6 +61,7 @@ def _problem(seed, img, K, Nc, density=0.8, complex_lam=True):
     ((128, 12, 8), 2, 3, True),  # 3D with 256-point rows
     ((32, 256), 6, 2, False),    # K = 6 on 512-point columns (4-column tiles, one CTA per SM)
     ((16, 256), 1, 3, True),     # K = 1 on 512-point columns (8-column tiles)
+    ((256, 256), 3, 40, False),  # two coil groups of 20 (the stack of one group kept L2-sized)
 ])
 def test_nfft_apply_matches_oracle(mr, cuda, img, K, Nc, cplx):
     lam, cells, cm, x = _problem(1, img, K, Nc, complex_lam=cplx)
