@@ -1469,6 +1469,94 @@ __global__ void __launch_bounds__(256) k_interp(InterpArgs a) {
   }
 }
 
+// 2D on the tile sort (the backprojection's 12 x 12 tiles and tap records): a work item,
+// up to 1024 samples whose first tap lies in one tile, loads the tile's 19 x 19-cell window of
+// the K interleaved planes into shared memory once, and each thread sums one sample's 64 taps
+// x K from the window.  Same weights and summation order as k_interp (w = (wy * 1) * wx,
+// taps y-major), so the data are bit-identical to it.
+struct InterpTiledArgs {
+  int M0, M1, K, c, u_complex, ntx;
+  int64_t nt, ns_tot;
+  const void* U;
+  const float2* g;         // [mcells][K]
+  float2* data;            // (ns_pf, nt, ncoils)
+  const TapRec* rec;       // tap records in sorted order
+  const int4* items;       // (tile, first sorted position, count, -)
+  const int* nitems;
+  int* next;               // work counter, zeroed before the launch
+};
+
+__global__ void __launch_bounds__(kTiledThreads, 2) k_interp_tiled(InterpTiledArgs a) {
+  extern __shared__ float2 wk[];  // [kWinCells][K]
+  __shared__ int s_item;
+  const int K = a.K;
+  const int nitems = *a.nitems;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.next, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= nitems) break;
+    const int4 item = a.items[it];
+    const int ox = (item.x % a.ntx) * kTile, oy = (item.x / a.ntx) * kTile;
+    for (int e = threadIdx.x; e < kWinCells * K; e += blockDim.x) {
+      const int cw = e / K, k = e - cw * K;
+      const int row = cw / kWin, col = cw - row * kWin;
+      const int64_t gc = wrap32(ox + col, a.M0) + (int64_t)a.M0 * wrap32(oy + row, a.M1);
+      wk[e] = a.g[gc * K + k];
+    }
+    __syncthreads();
+    for (int sidx = threadIdx.x; sidx < item.z; sidx += blockDim.x) {
+      const float4* r4 = reinterpret_cast<const float4*>(a.rec + item.y + sidx);
+      float wx[kEsWidth], wy[kEsWidth];
+      {
+        const float4 q0 = r4[0], q1 = r4[1], q2 = r4[2], q3 = r4[3];
+        wx[0] = q0.x; wx[1] = q0.y; wx[2] = q0.z; wx[3] = q0.w;
+        wx[4] = q1.x; wx[5] = q1.y; wx[6] = q1.z; wx[7] = q1.w;
+        wy[0] = q2.x; wy[1] = q2.y; wy[2] = q2.z; wy[3] = q2.w;
+        wy[4] = q3.x; wy[5] = q3.y; wy[6] = q3.z; wy[7] = q3.w;
+      }
+      const int4 ri = reinterpret_cast<const int4*>(r4)[4];  // li, t, lx0, ly0
+      const int lx = ri.z - ox, ly = ri.w - oy;
+      float2 z[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) z[k] = make_float2(0.f, 0.f);
+      const bool in_win = (unsigned)lx < (unsigned)kTile && (unsigned)ly < (unsigned)kTile;
+#pragma unroll
+      for (int t2 = 0; t2 < kEsWidth; ++t2) {
+        const float w23 = wy[t2] * 1.f;
+#pragma unroll
+        for (int t1 = 0; t1 < kEsWidth; ++t1) {
+          const float w = w23 * wx[t1];
+          // the sort put the first tap in this tile (the same float arithmetic); a sample
+          // outside it would read the grid itself
+          const float2* cell = in_win ? wk + ((ly + t2) * kWin + lx + t1) * K
+                                      : a.g + (wrap32(ri.z + t1, a.M0) + (int64_t)a.M0 * wrap32(ri.w + t2, a.M1)) * K;
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            if (k < K) {
+              const float2 gv = cell[k];
+              z[k].x = fmaf(w, gv.x, z[k].x);
+              z[k].y = fmaf(w, gv.y, z[k].y);
+            }
+        }
+      }
+      const int64_t t = ri.y;
+      float2 y = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (k < K) {
+          if (a.u_complex)
+            y = cadd(y, cmul(reinterpret_cast<const float2*>(a.U)[t + a.nt * k], z[k]));
+          else
+            y = cadd(y, cscale(z[k], reinterpret_cast<const float*>(a.U)[t + a.nt * k]));
+        }
+      }
+      a.data[ri.x + a.ns_tot * a.c] = y;
+    }
+    __syncthreads();
+  }
+}
+
 // 3D: one warp per sample, lanes over its 512 taps (16 each, lane_taps), one shuffle
 // reduction per plane; for 512 taps per sample this beats a thread per sample (which
 // serialises 512 x K gathers in one thread).
@@ -1699,6 +1787,16 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
   DevBuf grid, gridi;
   MRSR_TRY(grid.alloc(sizeof(float2) * K * mcells));
   MRSR_TRY(gridi.alloc(sizeof(float2) * K * mcells));
+  // 2D: the interpolation runs on the tile sort of the samples (built once for all coils)
+  TileSort ts;
+  const bool tiled = ndims == 2 && sl.set.n < (1ll << 31) && M[0] < (1ll << 24) && M[1] < (1ll << 24) &&
+                     ns_per_frame * nt < (1ll << 31);
+  if (tiled) {
+    MRSR_TRY(ts.build(sl.set, M[0], M[1], st));
+    MRSR_TRY(ts.prep(sl.set, MRSR_DCF_NONE, nullptr, st));
+  }
+  const size_t win_bytes = sizeof(float2) * kWinCells * (size_t)K;
+  if (tiled) MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_interp_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)win_bytes));
   for (int c = 0; c < ncoils; ++c) {
     MRSR_CHECK_CUDA(cudaMemsetAsync(grid.p, 0, sizeof(float2) * K * mcells, st));
     FwdPlaceArgs pa;
@@ -1725,6 +1823,25 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
     if (ndims == 3) {
       MRSR_REQUIRE(mcells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "forward model grid of 2^32 cells or more");
       k_interp3<<<spread_blocks(sl.set.n), 256, 0, st>>>(ia);
+    } else if (tiled) {
+      InterpTiledArgs ta;
+      ta.M0 = (int)M[0];
+      ta.M1 = (int)M[1];
+      ta.K = K;
+      ta.c = c;
+      ta.u_complex = u_is_complex;
+      ta.ntx = ts.ntx;
+      ta.nt = nt;
+      ta.ns_tot = ns_per_frame * nt;
+      ta.U = U;
+      ta.g = gridi.as<float2>();
+      ta.data = reinterpret_cast<float2*>(data_out);
+      ta.rec = ts.rec.as<TapRec>();
+      ta.items = ts.items.as<int4>();
+      ta.nitems = ts.nitems.as<int>();
+      ta.next = ts.next.as<int>();
+      MRSR_CHECK_CUDA(cudaMemsetAsync(ts.next.p, 0, sizeof(int), st));
+      k_interp_tiled<<<152 * 2, kTiledThreads, win_bytes, st>>>(ta);
     } else {
       k_interp<<<(unsigned)std::min<int64_t>(std::max<int64_t>(cdiv(sl.set.n, 256), 1), 152 * 64), 256, 0, st>>>(ia);
     }
