@@ -1498,11 +1498,12 @@ __global__ void __launch_bounds__(kTiledThreads, 2) k_interp_tiled(InterpTiledAr
     if (it >= nitems) break;
     const int4 item = a.items[it];
     const int ox = (item.x % a.ntx) * kTile, oy = (item.x / a.ntx) * kTile;
-    for (int e = threadIdx.x; e < kWinCells * K; e += blockDim.x) {
-      const int cw = e / K, k = e - cw * K;
+    for (int cw = threadIdx.x; cw < kWinCells; cw += blockDim.x) {
       const int row = cw / kWin, col = cw - row * kWin;
-      const int64_t gc = wrap32(ox + col, a.M0) + (int64_t)a.M0 * wrap32(oy + row, a.M1);
-      wk[e] = a.g[gc * K + k];
+      const float2* src = a.g + (wrap32(ox + col, a.M0) + (int64_t)a.M0 * wrap32(oy + row, a.M1)) * K;
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (k < K) wk[cw * K + k] = src[k];
     }
     __syncthreads();
     for (int sidx = threadIdx.x; sidx < item.z; sidx += blockDim.x) {
@@ -1600,6 +1601,95 @@ __global__ void __launch_bounds__(256) k_interp3(InterpArgs a) {
       }
     }
     if (lane == 0) a.data[li + ns_tot * a.c] = y;
+  }
+}
+
+// 3D on the tile sort (the backprojection's 8^3 tiles and tap records): a work item, up to
+// 1024 samples whose first tap lies in one tile, loads the tile's 15^3-cell window of the K
+// interleaved planes into shared memory once (216 KB for K = 8); a warp per sample, lanes over
+// its 512 taps as in k_interp3 (lane = x tap + 8 y tap, 16 taps each), one shuffle reduction
+// per plane.
+struct InterpTiled3Args {
+  int M0, M1, M2, K, c, u_complex, ntx, nty;
+  int64_t nt, ns_tot;
+  const void* U;
+  const float2* g;         // [mcells][K]
+  float2* data;            // (ns_pf, nt, ncoils)
+  const TapRec3* rec;      // tap records in sorted order
+  const int4* items;       // (tile, first sorted position, count, -)
+  const int* nitems;
+  int* next;               // work counter, zeroed before the launch
+};
+
+__global__ void __launch_bounds__(kTiledThreads, 1) k_interp_tiled3(InterpTiled3Args a) {
+  extern __shared__ float2 wk[];  // [kWin3Cells][K]
+  __shared__ int s_item;
+  const int K = a.K;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int t1 = lane & 7, t2a = lane >> 3;
+  const int nitems = *a.nitems;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.next, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= nitems) break;
+    const int4 item = a.items[it];
+    const int tx = item.x % a.ntx, ty = (item.x / a.ntx) % a.nty, tz = item.x / (a.ntx * a.nty);
+    const int ox = tx * kTile3, oy = ty * kTile3, oz = tz * kTile3;
+    for (int cw = threadIdx.x; cw < kWin3Cells; cw += blockDim.x) {
+      const int wz = cw / (kWin3 * kWin3), r2 = cw - wz * kWin3 * kWin3, wy = r2 / kWin3, wx = r2 - wy * kWin3;
+      const float2* src = a.g + (wrap32(ox + wx, a.M0) +
+                                 (int64_t)a.M0 * (wrap32(oy + wy, a.M1) + (int64_t)a.M1 * wrap32(oz + wz, a.M2))) * K;
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (k < K) wk[cw * K + k] = src[k];
+    }
+    __syncthreads();
+    for (int sidx = warp; sidx < item.z; sidx += nwarps) {
+      const TapRec3& r = a.rec[item.y + sidx];
+      const int li = r.li, t = r.t, lx0 = r.lx0, ly0 = r.ly0, lz0 = r.lz0;
+      const int lx = lx0 - ox, ly = ly0 - oy, lz = lz0 - oz;
+      const bool in_win = (unsigned)lx < (unsigned)kTile3 && (unsigned)ly < (unsigned)kTile3 && (unsigned)lz < (unsigned)kTile3;
+      const float wxl = r.wx[t1];
+      float2 z[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) z[k] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int t2 = t2a + 4 * (j & 1), t3 = j >> 1;
+        const float w = (wxl * r.wy[t2]) * r.wz[t3];
+        // the sort put the first tap in this tile (the same float arithmetic); a sample
+        // outside it would read the grid itself
+        const float2* cell =
+            in_win ? wk + (((lz + t3) * kWin3 + ly + t2) * kWin3 + lx + t1) * K
+                   : a.g + (wrap32(lx0 + t1, a.M0) +
+                            (int64_t)a.M0 * (wrap32(ly0 + t2, a.M1) + (int64_t)a.M1 * wrap32(lz0 + t3, a.M2))) * K;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (k < K) {
+            const float2 gv = cell[k];
+            z[k].x = fmaf(w, gv.x, z[k].x);
+            z[k].y = fmaf(w, gv.y, z[k].y);
+          }
+      }
+      float2 y = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (k < K) {
+          float2 v = z[k];
+          for (int o = 16; o > 0; o >>= 1) {
+            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+          }
+          if (a.u_complex)
+            y = cadd(y, cmul(reinterpret_cast<const float2*>(a.U)[t + a.nt * k], v));
+          else
+            y = cadd(y, cscale(v, reinterpret_cast<const float*>(a.U)[t + a.nt * k]));
+        }
+      }
+      if (lane == 0) a.data[li + a.ns_tot * a.c] = y;
+    }
+    __syncthreads();
   }
 }
 
@@ -1787,16 +1877,24 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
   DevBuf grid, gridi;
   MRSR_TRY(grid.alloc(sizeof(float2) * K * mcells));
   MRSR_TRY(gridi.alloc(sizeof(float2) * K * mcells));
-  // 2D: the interpolation runs on the tile sort of the samples (built once for all coils)
+  // the interpolation runs on the tile sort of the samples (built once for all coils)
   TileSort ts;
-  const bool tiled = ndims == 2 && sl.set.n < (1ll << 31) && M[0] < (1ll << 24) && M[1] < (1ll << 24) &&
-                     ns_per_frame * nt < (1ll << 31);
+  const bool small = sl.set.n < (1ll << 31) && ns_per_frame * nt < (1ll << 31);
+  const bool tiled = ndims == 2 && small && M[0] < (1ll << 24) && M[1] < (1ll << 24);
+  const int64_t ntiles3 = cdiv(M[0], kTile3) * cdiv(M[1], kTile3) * cdiv(M[2], kTile3);
+  const bool tiled3 = ndims == 3 && small && ntiles3 < (1ll << 31) && mcells < (1ll << 32);
   if (tiled) {
     MRSR_TRY(ts.build(sl.set, M[0], M[1], st));
     MRSR_TRY(ts.prep(sl.set, MRSR_DCF_NONE, nullptr, st));
+  } else if (tiled3) {
+    MRSR_TRY(ts.build3(sl.set, M, st));
+    MRSR_TRY(ts.prep3(sl.set, MRSR_DCF_NONE, nullptr, st));
   }
   const size_t win_bytes = sizeof(float2) * kWinCells * (size_t)K;
+  const size_t win3_bytes = sizeof(float2) * kWin3Cells * (size_t)K;
   if (tiled) MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_interp_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)win_bytes));
+  if (tiled3)
+    MRSR_CHECK_CUDA(cudaFuncSetAttribute(k_interp_tiled3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)win3_bytes));
   for (int c = 0; c < ncoils; ++c) {
     MRSR_CHECK_CUDA(cudaMemsetAsync(grid.p, 0, sizeof(float2) * K * mcells, st));
     FwdPlaceArgs pa;
@@ -1820,7 +1918,28 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
     MRSR_LAUNCH_CHECK();
     InterpArgs ia{sl.set, {M[0], M[1], M[2]}, mcells, K, c, u_is_complex, U, gridi.as<float2>(),
                   reinterpret_cast<float2*>(data_out)};
-    if (ndims == 3) {
+    if (tiled3) {
+      InterpTiled3Args ta;
+      ta.M0 = (int)M[0];
+      ta.M1 = (int)M[1];
+      ta.M2 = (int)M[2];
+      ta.K = K;
+      ta.c = c;
+      ta.u_complex = u_is_complex;
+      ta.ntx = ts.ntx;
+      ta.nty = ts.nty;
+      ta.nt = nt;
+      ta.ns_tot = ns_per_frame * nt;
+      ta.U = U;
+      ta.g = gridi.as<float2>();
+      ta.data = reinterpret_cast<float2*>(data_out);
+      ta.rec = ts.rec.as<TapRec3>();
+      ta.items = ts.items.as<int4>();
+      ta.nitems = ts.nitems.as<int>();
+      ta.next = ts.next.as<int>();
+      MRSR_CHECK_CUDA(cudaMemsetAsync(ts.next.p, 0, sizeof(int), st));
+      k_interp_tiled3<<<152, kTiledThreads, win3_bytes, st>>>(ta);
+    } else if (ndims == 3) {
       MRSR_REQUIRE(mcells < (1ll << 32), MRSR_ERR_UNSUPPORTED, "forward model grid of 2^32 cells or more");
       k_interp3<<<spread_blocks(sl.set.n), 256, 0, st>>>(ia);
     } else if (tiled) {
