@@ -125,11 +125,6 @@ int es_inv_psi_table(int64_t M, int64_t jmin, int64_t count, const float** out) 
   return MRSR_OK;
 }
 
-__device__ __forceinline__ int64_t wrap(int64_t l, int64_t M) {
-  l %= M;
-  return l < 0 ? l + M : l;
-}
-
 // --------------------------------------------------------- spreading ---
 
 // one fixed-point term: a = value * 2^(e - 21), added as round(a * 2^21)
@@ -141,6 +136,53 @@ __device__ __forceinline__ int wrap32(int l, int M) {
   l %= M;
   return l < 0 ? l + M : l;
 }
+
+// l mod M for -M < l < M (no division)
+__device__ __forceinline__ int64_t wrap_near(int64_t l, int64_t M) { return l < 0 ? l + M : l; }
+
+// Element e of an array of `planes` planes of (N0, N1, N2) cells -> plane and per-axis
+// position.  Below 2^31 elements by magic-number divisions (FastDiv); this GPU divides 64-bit
+// integers in software, tens of instructions each.
+struct Decomp {
+  int d = 0;
+  bool fast = false;
+  int64_t cells = 1, N[3] = {1, 1, 1};
+  FastDiv fcells, fN[2];
+  void init(int dims, const int64_t* n, int64_t planes) {
+    d = dims;
+    cells = 1;
+    for (int i = 0; i < 3; ++i) {
+      N[i] = i < dims ? n[i] : 1;
+      cells *= N[i];
+    }
+    fast = cells * planes < (1ll << 31);
+    if (fast) {
+      fcells = FastDiv((uint32_t)cells);
+      fN[0] = FastDiv((uint32_t)N[0]);
+      fN[1] = FastDiv((uint32_t)N[1]);
+    }
+  }
+  __device__ __forceinline__ int split(int64_t e, int64_t* pos) const {
+    if (fast) {
+      const uint32_t ue = (uint32_t)e, pl = fcells.div(ue);
+      uint32_t r = ue - pl * fcells.d;
+      const uint32_t q0 = fN[0].div(r);
+      pos[0] = r - q0 * fN[0].d;
+      r = q0;
+      const uint32_t q1 = fN[1].div(r);
+      pos[1] = r - q1 * fN[1].d;
+      pos[2] = q1;
+      return (int)pl;
+    }
+    const int pl = (int)(e / cells);
+    int64_t r = e - (int64_t)pl * cells;
+    pos[0] = r % N[0];
+    r /= N[0];
+    pos[1] = r % N[1];
+    pos[2] = r / N[1];
+    return pl;
+  }
+};
 
 // Taps of one sample owned by a lane of its warp: lane = t1 + 8 * t2a (t1 < 8, t2a < 4), and
 // its J = w^d / 32 taps are t2 = t2a + 4 (j & 1), t3 = j >> 1.  Weights (times `sc`) and
@@ -1150,6 +1192,7 @@ struct FoldArgs {
   int64_t gcells, mcells;
   int P;
   int real_u;
+  Decomp dc;              // element -> (p, cell position) over (G0, G1, G2) x P
   const float2* g;        // [P][mcells] after the inverse DFT
   const float* ipsi[3];   // 1/psi_hat(j) for j = -G/2 .. G/2
   float2* c;              // [P][gcells]
@@ -1162,13 +1205,8 @@ struct FoldArgs {
 __global__ void k_lambda_fold(FoldArgs a) {
   const int64_t total = a.gcells * a.P;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int p = (int)(e / a.gcells);
-    int64_t cell = e - (int64_t)p * a.gcells;
     int64_t pd[3] = {0, 0, 0};
-    pd[0] = cell % a.G[0];
-    cell /= a.G[0];
-    pd[1] = cell % a.G[1];
-    pd[2] = cell / a.G[1];
+    const int p = a.dc.split(e, pd);
     float scale = 1.f;
     int64_t l = 0, mul = 1;
     bool zero = false;
@@ -1187,7 +1225,7 @@ __global__ void k_lambda_fold(FoldArgs a) {
         j = pd[dd] < half ? pd[dd] : pd[dd] - Gd;
       }
       scale *= a.ipsi[dd][j + half];
-      l += wrap(j, a.M[dd]) * mul;
+      l += wrap_near(j, a.M[dd]) * mul;
       mul *= a.M[dd];
     }
     float2 v = zero ? make_float2(0.f, 0.f) : a.g[(int64_t)p * a.mcells + l];
@@ -1295,6 +1333,7 @@ static int compute_lambda(int d, const int64_t* G, const SampleSet& S, const voi
     fa.gcells = gcells;
     fa.mcells = mcells;
     fa.P = np;
+    fa.dc.init(d, G, np);
     fa.real_u = u_complex ? 0 : 1;
     fa.g = grid.as<float2>();
     fa.c = cgrid.as<float2>() + (int64_t)p0 * gcells;
@@ -1316,6 +1355,7 @@ struct BpFoldArgs {
   int d;
   int64_t N[3], M[3], nimg, mcells;
   int K, c0, nc, ncoils;
+  Decomp dc;              // element -> (k, image position) over img x K
   const float2* g;        // [(c - c0) K + k][mcells]
   const float* ipsi[3];   // 1/psi_hat(j), j = -N/2 ...
   const float2* cmaps;    // (img..., ncoils) or null -> per-coil output
@@ -1327,16 +1367,16 @@ struct BpFoldArgs {
 __global__ void k_bp_fold(BpFoldArgs a) {
   const int64_t total = a.nimg * a.K;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(e / a.nimg);
+    int64_t pos[3];
+    const int k = a.dc.split(e, pos);
     const int64_t r = e - (int64_t)k * a.nimg;
-    int64_t rr = r, l = 0, mul = 1;
+    int64_t l = 0, mul = 1;
     float sc = 1.f;
     for (int dd = 0; dd < a.d; ++dd) {
-      const int64_t rd = rr % a.N[dd];
-      rr /= a.N[dd];
+      const int64_t rd = pos[dd];
       const int64_t j = rd - a.N[dd] / 2;
       sc *= a.ipsi[dd][rd];
-      l += wrap(j, a.M[dd]) * mul;
+      l += wrap_near(j, a.M[dd]) * mul;
       mul *= a.M[dd];
     }
     if (a.cmaps) {
@@ -1361,6 +1401,7 @@ struct FwdPlaceArgs {
   int d;
   int64_t N[3], M[3], nimg, mcells;
   int K, c;
+  Decomp dc;             // element -> (k, image position) over img x K
   const float2* x;       // (img..., K)
   const float2* cmaps;   // (img..., ncoils) or null
   const float* ipsi[3];
@@ -1370,15 +1411,15 @@ struct FwdPlaceArgs {
 __global__ void k_fwd_place(FwdPlaceArgs a) {
   const int64_t total = a.nimg * a.K;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int k = (int)(e / a.nimg);
+    int64_t pos[3];
+    const int k = a.dc.split(e, pos);
     const int64_t r = e - (int64_t)k * a.nimg;
-    int64_t rr = r, l = 0, mul = 1;
+    int64_t l = 0, mul = 1;
     float sc = 1.f;
     for (int dd = 0; dd < a.d; ++dd) {
-      const int64_t rd = rr % a.N[dd];
-      rr /= a.N[dd];
+      const int64_t rd = pos[dd];
       sc *= a.ipsi[dd][rd];
-      l += wrap(rd - a.N[dd] / 2, a.M[dd]) * mul;
+      l += wrap_near(rd - a.N[dd] / 2, a.M[dd]) * mul;
       mul *= a.M[dd];
     }
     float2 v = a.x[e];
@@ -1839,6 +1880,7 @@ extern "C" int mrsr_backprojection(int ndims, const int64_t* img_shape, int64_t 
     fa.nimg = nimg;
     fa.mcells = mcells;
     fa.K = K;
+    fa.dc.init(ndims, N, K);
     fa.c0 = c0;
     fa.nc = nc;
     fa.ncoils = ncoils;
@@ -1907,6 +1949,7 @@ extern "C" int mrsr_forward_model(int ndims, const int64_t* img_shape, int64_t n
     pa.nimg = nimg;
     pa.mcells = mcells;
     pa.K = K;
+    pa.dc.init(ndims, N, K);
     pa.c = c;
     pa.x = reinterpret_cast<const float2*>(x);
     pa.cmaps = reinterpret_cast<const float2*>(cmaps);
