@@ -898,6 +898,8 @@ extern "C" int mrsr_normalop_apply_host(mrsr_normalop* op, const float* x, float
   MRSR_CALL_SCOPE(reinterpret_cast<cudaStream_t>(stream));
   MRSR_REQUIRE(op && x && y, MRSR_ERR_ARG, "NULL argument to mrsr_normalop_apply_host");
   MRSR_REQUIRE((const void*)x != (const void*)y, MRSR_ERR_ARG, "x and y must not alias");
+  MRSR_REQUIRE(((uintptr_t)x & 7) == 0 && ((uintptr_t)y & 7) == 0, MRSR_ERR_ARG,
+               "x and y must be aligned to their ComplexF32 elements (8 bytes)");
   const cudaStream_t st = as_stream(stream);
   OpUse use{op, st};
   const OpGeom& g = op->geo;
