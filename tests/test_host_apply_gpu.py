@@ -86,3 +86,9 @@ def test_host_apply_rejects_bad_arguments(mr, cuda):
         A.mul_host(good, good)
     with pytest.raises(ValueError):  # row-major (C-order) multi-dimensional data
         A.mul_host(good, torch.zeros((16, 16, 2), dtype=torch.complex64))
+    # the C entry point itself: host pointers off their 8-byte ComplexF32 alignment
+    lib = mr._lib.load()
+    buf = torch.zeros(2 * n + 2, dtype=torch.float32).pin_memory()
+    status = lib.mrsr_normalop_apply_host(A.handle, buf.data_ptr() + 4, good.data_ptr(), 1.0, 0.0, 0.0, 0.0,
+                                          torch.cuda.current_stream().cuda_stream)
+    assert status == mr._lib.MRSR_ERR_ARG
