@@ -1,5 +1,5 @@
 // Three-step line transforms of the float32 operator's passes (apply_lam8.cu: the Λ pass,
-// apply_rows8.cu: the row passes) for L = R1 x 8 x 8 with R1 = 8 (512 points) or 4 (256):
+// apply_rows8.cu: the inverse row pass) for L = R1 x 8 x 8 with R1 = 8 (512 points) or 4 (256):
 //   n = 64 n1 + 8 n2 + n3,  f = f1 + R1 f2 + 8 R1 f3,
 //   X[f] = sum_n3 w8^(n3 f3) w64^(n3 f2) sum_n2 w8^(n2 f2) [wL^((8 n2 + n3) f1) sum_n1 wR1^(n1 f1) x[n]]
 // on lines zero-padded to twice their length (input n1 < R1 / 2) whose inverse keeps the
