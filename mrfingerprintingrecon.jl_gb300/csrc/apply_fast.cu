@@ -23,7 +23,7 @@ __global__ void __launch_bounds__(512) k4_rows_fwd(RowsFwdArgs a, Slots sl) {
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* sm = smem + L;
-  load_twiddles(tw, a.pl);
+  load_twiddles_a<SP>(tw, a.pl);
   const int cl = blockIdx.y;
   const int c = a.c0 + cl;
   const int64_t row0 = (int64_t)blockIdx.x * a.rpc;
@@ -40,9 +40,9 @@ __global__ void __launch_bounds__(512) k4_rows_fwd(RowsFwdArgs a, Slots sl) {
     return v;
   };
   if constexpr (PR)
-    step_a_pf<SP, -1, nload>(sm, sl, NO, tw, ld);  // the zero-padded half leaves registers for the prefetch
+    step_a_pf<SP, -1, nload, true>(sm, sl, NO, tw, ld);  // the zero-padded half leaves registers for the prefetch
   else
-    step_a<SP, -1>(sm, sl, NO, tw, nload, ld);
+    step_a<SP, -1, true>(sm, sl, NO, tw, nload, ld);
   __syncthreads();
   step_b<SP, -1>(sm, sl, NO, R2, [&](int lo, int, int f1, int f2, float2 v) {
     const int rl = lo / a.K, k = lo - rl * a.K;
@@ -56,14 +56,14 @@ __global__ void __launch_bounds__(512) k4_rows_inv(RowsInvArgs a, Slots sl) {
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* sm = smem + L;
-  load_twiddles(tw, a.pl);
+  load_twiddles_a<SP>(tw, a.pl);
   const int k = blockIdx.y;
   const int64_t row0 = (int64_t)blockIdx.x * a.rpc;
   const int nr = (int)min((int64_t)a.rpc, a.nrows - row0);
   const int NO = a.rpc * a.ncg;
   constexpr int nkeep = PR ? R2 / 2 : R2;
   __syncthreads();
-  step_a_pf<SP, +1, R1>(sm, sl, NO, tw, [&](int lo, int, int m) -> float2 {
+  step_a_pf<SP, +1, R1, true>(sm, sl, NO, tw, [&](int lo, int, int m) -> float2 {
     const int rl = lo / a.ncg, cl = lo - rl * a.ncg;
     if (rl >= nr) return make_float2(0.f, 0.f);
     return a.stack[(((int64_t)cl * a.K + k) * a.nrows + row0 + rl) * L + m];
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(512) k4_mid(MidArgs a, Slots sl) {
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* sm = smem + L;
-  load_twiddles(tw, a.pl);
+  load_twiddles_a<SP>(tw, a.pl);
   const int64_t col0 = (int64_t)blockIdx.x * a.TC;
   const int64_t o0 = (int64_t)blockIdx.y * a.NOo;
   const int no = (int)min((int64_t)a.NOo, a.n3 - o0);
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(512) k4_mid(MidArgs a, Slots sl) {
   constexpr int nload = (PR && S < 0) ? R1 / 2 : R1;
   constexpr int nkeep = (PR && S > 0) ? R2 / 2 : R2;
   __syncthreads();
-  step_a<SP, S>(sm, sl, a.NOo, tw, nload, [&](int o, int li, int n) -> float2 {
+  step_a<SP, S, true>(sm, sl, a.NOo, tw, nload, [&](int o, int li, int n) -> float2 {
     return (o < no && ((PR && S < 0) || n < a.nin)) ? ib[((int64_t)o * a.nin + n) * a.width + li]
                                                     : make_float2(0.f, 0.f);
   });

@@ -99,11 +99,23 @@ __device__ __forceinline__ float2 twl(const float2* tw, int m, int) {
   return w;
 }
 
+// Step-A twiddles in the order step A's lanes read them: tw[f1 * R2 + n2] = W_L^{n2 f1}
+// (the lanes of a warp vary n2, so a read is consecutive entries, bank-conflict free; the
+// table indexed n2 f1 puts the lanes of an even f1 on shared banks, gcd(f1, 16)-way).
+template <class SP>
+__device__ __forceinline__ void load_twiddles_a(float2* tw_s, const FftPlan& pl) {
+  for (int i = threadIdx.x; i < SP::L; i += blockDim.x) {
+    const int f1 = i / SP::R2, n2 = i - f1 * SP::R2;
+    tw_s[i] = pl.tw[n2 * f1];  // n2 f1 < R1 R2 = L
+  }
+}
+
 // Step A of a forward or inverse transform.  Task (lo, li, n2) loads
 // x[R2 n1 + n2] (n1 < nload) through ld(lo, li, n), applies the R1-point DFT
 // and the twiddle, and writes slot(lo, li, f1, n2).  nload = R1 or R1/2
-// (lower-half input, zero-padded embedding).
-template <class SP, int S, class SL, class LD>
+// (lower-half input, zero-padded embedding).  LT: tw is load_twiddles_a's table, else
+// load_twiddles' (tw[p] = W_L^p).
+template <class SP, int S, bool LT = false, class SL, class LD>
 __device__ __forceinline__ void step_a(float2* sm, const SL& sl, int NO, const float2* tw, int nload, LD ld) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   const int ntask = (NO * R2) << sl.tcs;
@@ -118,7 +130,7 @@ __device__ __forceinline__ void step_a(float2* sm, const SL& sl, int NO, const f
     RDft<R1, S>::run(v);
 #pragma unroll
     for (int f1 = 0; f1 < R1; ++f1) {
-      const float2 w = (f1 == 0) ? make_float2(1.f, 0.f) : twl<S>(tw, n2 * f1, L);
+      const float2 w = (f1 == 0) ? make_float2(1.f, 0.f) : twl<S>(tw, LT ? f1 * R2 + n2 : n2 * f1, L);
       sm[sl.at(lo, f1, n2, li, R1)] = (f1 == 0) ? v[0] : cmul(v[f1], w);
     }
   }
@@ -127,7 +139,7 @@ __device__ __forceinline__ void step_a(float2* sm, const SL& sl, int NO, const f
 // Step A with the task loop software-pipelined: the inputs of the thread's next task are
 // loaded before the current task's DFT, so their latency overlaps it.  NLOAD inputs per
 // task are read (the rest are zero), which costs NLOAD extra registers.
-template <class SP, int S, int NLOAD, class SL, class LD>
+template <class SP, int S, int NLOAD, bool LT = false, class SL, class LD>
 __device__ __forceinline__ void step_a_pf(float2* sm, const SL& sl, int NO, const float2* tw, LD ld) {
   constexpr int R1 = SP::R1, R2 = SP::R2, L = SP::L;
   const int ntask = (NO * R2) << sl.tcs;
@@ -153,7 +165,7 @@ __device__ __forceinline__ void step_a_pf(float2* sm, const SL& sl, int NO, cons
     RDft<R1, S>::run(v);
 #pragma unroll
     for (int f1 = 0; f1 < R1; ++f1) {
-      const float2 w = (f1 == 0) ? make_float2(1.f, 0.f) : twl<S>(tw, n2 * f1, L);
+      const float2 w = (f1 == 0) ? make_float2(1.f, 0.f) : twl<S>(tw, LT ? f1 * R2 + n2 : n2 * f1, L);
       sm[sl.at(lo, f1, n2, li, R1)] = (f1 == 0) ? v[0] : cmul(v[f1], w);
     }
   }

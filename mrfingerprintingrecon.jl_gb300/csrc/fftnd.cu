@@ -61,13 +61,13 @@ __global__ void __launch_bounds__(256) k_axis_fast(AxisArgs a, Slots sl) {
   extern __shared__ float2 smem[];
   float2* tw = smem;
   float2* sm = smem + L;
-  load_twiddles(tw, a.pl);
+  load_twiddles_a<SP>(tw, a.pl);
   const int64_t tile = blockIdx.x % a.ntile;
   const int64_t o0 = (blockIdx.x / a.ntile) * a.NOo;
   const int no = (int)min((int64_t)a.NOo, a.nouter - o0);
   float2* base = a.data + o0 * L * a.width + tile * a.TC;
   __syncthreads();
-  step_a<SP, S>(sm, sl, a.NOo, tw, R1, [&](int o, int li, int n) -> float2 {
+  step_a<SP, S, true>(sm, sl, a.NOo, tw, R1, [&](int o, int li, int n) -> float2 {
     return (o < no) ? base[((int64_t)o * L + n) * a.width + li] : make_float2(0.f, 0.f);
   });
   __syncthreads();
